@@ -1,0 +1,174 @@
+/*
+ * pof.h -- C ABI of the GB300 (sm_103a) parallel-in-time IEKS library
+ * (libpof.so).
+ *
+ * The reference (nathanaelbosch/parallel-in-time-ode-filters, package `pof`)
+ * is a JAX library with no FFI of its own; its hot path is a set of Python
+ * functions over JAX arrays.  Each entry point below replaces one of those
+ * functions and keeps its argument meaning; a JAX-FFI or ctypes binding
+ * passes device pointers straight through.
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers, row-major, C-contiguous, of the
+ *    element type selected by `dtype` (POF_F64: double, POF_F32: float),
+ *    except `out_scalars` / `info`, which are always device double arrays.
+ *  - n_steps = N - 1 time steps, D = d (q + 1) state dimension, d the ODE /
+ *    observation dimension.  Shapes: x0_mean (D), x0_chol (D, D);
+ *    F, QL (D, D) when ft_stride == 0, else (n_steps, D, D) with
+ *    ft_stride == D*D; H (n_steps, d, D); c (n_steps, d);
+ *    R (d, d) when r_stride == 0, (n_steps, d, d) when r_stride == d*d, or
+ *    NULL for R = 0; means (N, D); chols (N, D, D).
+ *  - `stream` is a cudaStream_t (NULL: the legacy default stream).  All work
+ *    is enqueued on it; calls return without waiting unless stated.
+ *  - The caller owns every buffer, including the workspace (size from the
+ *    matching *_workspace_bytes query).  The library allocates no device
+ *    memory.
+ *  - Return value: POF_OK (0), a negative usage / CUDA error, never a trap.
+ *    Numerical failure (NaN) propagates into the outputs, as in the
+ *    reference, and is reported through the scalars.
+ */
+#ifndef POF_H_
+#define POF_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  POF_OK = 0,
+  POF_ERR_ARG = -1,       /* null pointer, non-positive size, bad stride */
+  POF_ERR_SHAPE = -2,     /* (D, d) combination not compiled into this build */
+  POF_ERR_WORKSPACE = -3, /* workspace smaller than *_workspace_bytes */
+  POF_ERR_CUDA = -4,      /* a CUDA runtime call failed (see pof_last_cuda_error) */
+  POF_ERR_FIELD = -5,     /* unknown built-in field or d mismatch */
+  POF_ERR_DTYPE = -6      /* dtype not POF_F64 / POF_F32 */
+};
+
+enum { POF_F64 = 0, POF_F32 = 1 };
+
+/* Layout of the `out_scalars` block written by the filter/smoother entry
+ * points (device doubles). */
+enum {
+  POF_S_NLL = 0,      /* -sum log N(obs) of the filter (filter.py:96-102)   */
+  POF_S_OBJ = 1,      /* smoother objective (smoother.py:20)                */
+  POF_S_SSQ = 2,      /* sigma^2 (filter.py:105-114, whiten quirk)           */
+  POF_S_FOBJ = 3,     /* filter objective (filter.py:43-45)                 */
+  POF_S_NOTCLOSE = 4, /* # mean entries not isclose(old, new, 1e-13, 1e-8) */
+  POF_S_COUNT = 8
+};
+
+/* Layout of the `info` block written by pof_ieks_solve (device doubles). */
+enum {
+  POF_I_ITERATIONS = 0,
+  POF_I_NLL = 1,
+  POF_I_OBJ = 2,
+  POF_I_SSQ = 3,
+  POF_I_COUNT = 4
+};
+
+/* Built-in vector fields for on-device EK1 linearization (pof/ivp.py). */
+enum {
+  POF_FIELD_USER = 0,
+  POF_FIELD_LOGISTIC = 1,       /* (r)                pof/ivp.py:7-14   */
+  POF_FIELD_LOTKAVOLTERRA = 2,  /* (a, b, c, d)       pof/ivp.py:17-31  */
+  POF_FIELD_VANDERPOL = 3,      /* (mu)               pof/ivp.py:34-41  */
+  POF_FIELD_FITZHUGHNAGUMO = 4, /* (a, b, 1/tau, I)   pof/ivp.py:44-60  */
+  POF_FIELD_FHN_CLASSIC = 5,    /* (a, b, c)                            */
+  POF_FIELD_ROBER = 6,          /* (k1, k2, k3)       pof/ivp.py:63-79  */
+  POF_FIELD_RIGID_BODY = 7,     /* (p0, p1, p2)       pof/ivp.py:82-90  */
+  POF_FIELD_SEIR = 8,           /* (p0..p3)           pof/ivp.py:93-108 */
+  POF_FIELD_THREEBODY = 9,      /* (mu)               pof/ivp.py:111-126 */
+  POF_FIELD_HENONHEILES = 10    /* (p)                pof/ivp.py:137-152 */
+};
+
+const char* pof_status_string(int status);
+const char* pof_last_cuda_error(void);
+int pof_version(void);
+
+/* 1 if the (D, d) pair is compiled into this build, else 0. */
+int pof_shape_supported(int32_t D, int32_t d);
+
+size_t pof_filtsmooth_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32_t d);
+
+/* pof.parallel_filtsmooth.linear_filtsmooth(x0, dtm, dom)
+ *   (pof/parallel_filtsmooth/__init__.py:5-10): filter then smoother.
+ * Writes the smoothed states into out_mean (N, D) / out_chol (N, D, D) and
+ * out_scalars[POF_S_NLL, POF_S_OBJ (smoother), POF_S_SSQ, POF_S_FOBJ]. */
+int pof_linear_filtsmooth(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, const void* x0_mean,
+                          const void* x0_chol, const void* F, const void* QL, int64_t ft_stride, const void* H,
+                          const void* c, const void* R, int64_t r_stride, void* out_mean, void* out_chol,
+                          double* out_scalars, void* workspace, size_t workspace_bytes, void* stream);
+
+/* pof.parallel_filtsmooth.linear_noiseless_filtering(x0, dtm, dom)
+ *   (pof/parallel_filtsmooth/filter.py:18-47): filtered states and
+ * out_scalars[POF_S_NLL, POF_S_SSQ, POF_S_FOBJ] (the filter's obj is
+ * reported in POF_S_FOBJ and copied to POF_S_OBJ). */
+int pof_linear_noiseless_filtering(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, const void* x0_mean,
+                                   const void* x0_chol, const void* F, const void* QL, int64_t ft_stride,
+                                   const void* H, const void* c, const void* R, int64_t r_stride, void* out_mean,
+                                   void* out_chol, double* out_scalars, void* workspace, size_t workspace_bytes,
+                                   void* stream);
+
+/* pof.parallel_filtsmooth.smoothing(dtm, filter_trajectory)
+ *   (pof/parallel_filtsmooth/smoother.py:8-22): smoothed states from the
+ * filtered ones (filt_mean/filt_chol, (N, D) / (N, D, D)); the smoother
+ * objective goes to out_scalars[POF_S_OBJ]. */
+int pof_smoothing(int32_t dtype, int64_t n_steps, int32_t D, const void* F, const void* QL, int64_t ft_stride,
+                  const void* filt_mean, const void* filt_chol, void* out_mean, void* out_chol, double* out_scalars,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* EK1 linearization of a built-in field at means[1:]
+ *   (pof/step.py:12-22, pof/observations.py:35-40) with the Nordsieck-scaled
+ * projections of pof/convenience.py:24-28 (step size h): writes
+ * H (n_steps, d, D) and c (n_steps, d); cholR is zero.  `params` is a device
+ * array of the field's parameters in `dtype`. */
+int pof_linearize(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field, const void* params,
+                  double h, const void* means, void* H, void* c, void* stream);
+
+/* pof.sequential_filtsmooth.linear_filtsmooth(x0, dtm, dom)
+ *   (pof/sequential_filtsmooth/__init__.py:13-16): the square-root Kalman
+ * filter (filter.py:33-56) and RTS smoother (smoother.py:8-28) step after
+ * step on one GPU thread -- the reference's sequential twin.  Writes the
+ * smoothed states (the filtered ones when smooth == 0) and
+ * out_scalars[POF_S_NLL] = +sum log-likelihood (the sequential twin's sign,
+ * filter.py:23-30), [POF_S_OBJ] (0 when smooth == 0), [POF_S_SSQ].
+ * No workspace. */
+int pof_sequential_linear_filtsmooth(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, const void* x0_mean,
+                                     const void* x0_chol, const void* F, const void* QL, int64_t ft_stride,
+                                     const void* H, const void* c, const void* R, int64_t r_stride, int32_t smooth,
+                                     void* out_mean, void* out_chol, double* out_scalars, void* stream);
+
+/* pof.sequential_filtsmooth.filtsmooth(x0, dtm, om) for a built-in field
+ *   (pof/sequential_filtsmooth/__init__.py:5-10): extended Kalman filter that
+ * linearizes at each predicted mean (filter.py:9-30), then the RTS smoother.
+ * Same outputs as pof_sequential_linear_filtsmooth; h is the step size of
+ * the Nordsieck projections. */
+int pof_sequential_eks(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field, const void* params,
+                       double h, const void* x0_mean, const void* x0_chol, const void* F, const void* QL,
+                       int64_t ft_stride, int32_t smooth, void* out_mean, void* out_chol, double* out_scalars,
+                       void* stream);
+
+size_t pof_ieks_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32_t d);
+
+/* pof.solver.solve(f, y0, ts, order, init, calibrate, maxiters)
+ *   (pof/solver.py:11-73) for a built-in field, in preconditioned
+ * coordinates: the IEKS loop of solver.py:36-57 (ieks_step, step.py:33-45,
+ * and crit, convergence_criteria.py:4-13) runs on the device.
+ *   in:  means (N, D) the initial trajectory (pof/convenience.py:76-92), x0,
+ *        F = QL-pair of the preconditioned IWP prior (constant, (D, D)).
+ *   out: means (N, D), chols (N, D, D) -- the final states, calibrated twice
+ *        when `calibrate` (solver.py:66-69); info[POF_I_*].
+ * The call waits on `stream` once per iteration to read the loop condition. */
+int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field, const void* params,
+                   double h, const void* x0_mean, const void* x0_chol, const void* F, const void* QL, void* means,
+                   void* chols, int64_t maxiters, int32_t calibrate, double* info, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* POF_H_ */

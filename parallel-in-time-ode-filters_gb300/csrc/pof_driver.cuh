@@ -1,0 +1,202 @@
+// Host-side orchestration of the chunked filter/smoother for one (T, D, DY):
+// kernel launches in stream order over a caller-provided workspace.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pof_kernels.cuh"
+#include "pof_plan.h"
+
+namespace pof {
+
+enum Scalar : int {
+  S_NLL = 0, S_OBJ = 1, S_SSQ = 2, S_FOBJ = 3, S_NOTCLOSE = 4,
+  S_OBJ_OLD = 5, S_NLL_OLD = 6, S_ITER = 7, S_CONT = 8, S_COUNT = 16
+};
+
+template <typename T>
+__global__ void k_finalize_filter(const double* __restrict__ partials, int64_t n1, int64_t n, int DY,
+                                  double* __restrict__ scalars, T* __restrict__ scale) {
+  const double ssq = block_sum_fixed<256>(partials + P_SSQ * n1, n1);
+  const double nll = block_sum_fixed<256>(partials + P_NLL * n1, n1);
+  const double fobj = block_sum_fixed<256>(partials + P_FOBJ * n1, n1);
+  if (threadIdx.x == 0) {
+    const double s = ssq / (double)n / (double)DY;
+    scalars[S_SSQ] = s;
+    scalars[S_NLL] = nll;
+    scalars[S_FOBJ] = fobj;
+    *scale = (T)sqrt(s);
+  }
+}
+
+static __global__ void k_finalize_smoother(const double* __restrict__ partials, int64_t n1, double* __restrict__ scalars) {
+  const double sobj = block_sum_fixed<256>(partials + P_SOBJ * n1, n1);
+  const double nc = block_sum_fixed<256>(partials + P_NOTCLOSE * n1, n1);
+  if (threadIdx.x == 0) {
+    scalars[S_OBJ] = sobj;
+    scalars[S_NOTCLOSE] = nc;
+  }
+}
+
+// Loop control of pof/solver.py:36-57 after one more ieks_step:
+// crit (pof/convergence_criteria.py:4-13) with rtol = 1e-6, atol = 1e-9 on
+// the objective and isclose(rtol = 1e-13, atol = 1e-8) on every mean.
+static __global__ void k_ieks_control(double* __restrict__ scalars, int64_t maxiters) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double k = scalars[S_ITER] + 1.0;
+  scalars[S_ITER] = k;
+  const double obj = scalars[S_OBJ], nll = scalars[S_NLL];
+  const double oo = scalars[S_OBJ_OLD];
+  const bool nan = isnan(obj) || isnan(nll);
+  bool objc;
+  if (isfinite(oo) && isfinite(obj))
+    objc = fabs(oo - obj) <= 1e-9 + 1e-6 * fabs(obj);
+  else
+    objc = (oo == obj);
+  const bool meansc = scalars[S_NOTCLOSE] == 0.0;
+  const bool conv = nan || objc || meansc;
+  const bool cont = (k < 1.0) || (!conv && k <= (double)maxiters);
+  scalars[S_CONT] = cont ? 1.0 : 0.0;
+  scalars[S_OBJ_OLD] = obj;
+  scalars[S_NLL_OLD] = nll;
+}
+
+static __global__ void k_init_scalars(double* __restrict__ scalars) {
+  if (threadIdx.x < S_COUNT) scalars[threadIdx.x] = 0.0;
+}
+
+template <typename T>
+__global__ void k_scale_inplace(T* __restrict__ x, int64_t count, const T* __restrict__ scale) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < count) x[i] *= *scale;
+}
+
+static __global__ void k_copy_scalars(const double* __restrict__ src, double* __restrict__ dst, int which) {
+  if (threadIdx.x != 0) return;
+  if (which == 0) {  // out_scalars of the filter/smoother entry points
+    dst[0] = src[S_NLL];
+    dst[1] = src[S_OBJ];
+    dst[2] = src[S_SSQ];
+    dst[3] = src[S_FOBJ];
+    dst[4] = src[S_NOTCLOSE];
+  } else {  // info of the solver
+    dst[0] = src[S_ITER];
+    dst[1] = src[S_NLL];
+    dst[2] = src[S_OBJ];
+    dst[3] = src[S_SSQ];
+  }
+}
+
+inline unsigned grid_for(int64_t count, int block) { return (unsigned)((count + block - 1) / block); }
+
+template <typename T, int D, int DY>
+struct Driver {
+  static constexpr int kBlock = 64;
+
+  struct Bufs {
+    char* ws;
+    const Plan* p;
+    template <typename U>
+    U* at(size_t off) const {
+      return reinterpret_cast<U*>(ws + off);
+    }
+  };
+
+  // Filter (phases 1-3) then finalize.  Leaves filtered states in means/chols
+  // and the smoother elements in the workspace.
+  static void filter(const Plan& p, char* ws, const StepModel& sm, const T* x0m, const T* x0L, T* means, T* chols,
+                     cudaStream_t st) {
+    Bufs b{ws, &p};
+    const int64_t n = p.n;
+    const int64_t n1 = p.cnt[1];
+    k_filt_l0_reduce<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(n, p.C0, sm, x0m, x0L,
+                                                                         b.template at<T>(p.felem[1]), n1);
+    for (int l = 1; l < p.nlev; ++l)
+      k_filt_reduce<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
+          b.template at<T>(p.felem[l]), p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
+    k_filt_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.felem[p.nlev]), p.cnt[p.nlev], x0m, x0L,
+                                       b.template at<T>(p.fstate[p.nlev]));
+    for (int l = p.nlev - 1; l >= 1; --l)
+      k_filt_down<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
+          b.template at<T>(p.felem[l]), p.cnt[l], p.Cg, b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
+          b.template at<T>(p.fstate[l]));
+    k_filt_l0_down<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
+        n, p.C0, sm, b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
+        b.template at<double>(p.partials));
+    k_finalize_filter<T><<<1, 256, 0, st>>>(b.template at<double>(p.partials), n1, n, DY,
+                                            b.template at<double>(p.scalars), b.template at<T>(p.scale));
+  }
+
+  // Smoother from the elements left by filter() (or built by
+  // build_smoother_elements) and the terminal state in means/chols[n].
+  static void smoother(const Plan& p, char* ws, const T* F, const T* QL, int64_t ft_stride, T* means, T* chols,
+                       bool calibrate, const T* means_old, cudaStream_t st) {
+    Bufs b{ws, &p};
+    const int64_t n = p.n;
+    const int64_t n1 = p.cnt[1];
+    k_smo_reduce<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(b.template at<T>(p.selem), n, p.C0,
+                                                                b.template at<T>(p.gelem[1]), n1);
+    for (int l = 1; l < p.nlev; ++l)
+      k_smo_reduce<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
+          b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
+    k_smo_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.gelem[p.nlev]), p.cnt[p.nlev], means + n * D,
+                                      chols + n * D * D, b.template at<T>(p.gend[p.nlev]));
+    for (int l = p.nlev - 1; l >= 1; --l)
+      k_smo_down<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
+          b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg, b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
+          b.template at<T>(p.gend[l]));
+    k_smo_l0_down<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
+        n, p.C0, F, QL, ft_stride, b.template at<T>(p.selem), b.template at<T>(p.gend[1]), n1, means, chols,
+        calibrate ? b.template at<T>(p.scale) : nullptr, means_old, b.template at<double>(p.partials));
+    k_finalize_smoother<<<1, 256, 0, st>>>(b.template at<double>(p.partials), n1, b.template at<double>(p.scalars));
+  }
+
+  static void linearize(int64_t n, int field, const T* params, T p0, T p1, const T* means, T* H, T* c,
+                        cudaStream_t st) {
+    k_linearize<T, D, DY><<<grid_for(n, 128), 128, 0, st>>>(n, field, params, p0, p1, means, H, c);
+  }
+};
+
+// Smoother elements from given filtered states (used by pof_smoothing, where
+// the filtered trajectory comes from the caller).
+template <typename T, int D>
+__global__ void __launch_bounds__(64) k_smo_elements(int64_t n, const T* __restrict__ F, const T* __restrict__ QL,
+                                                     int64_t ft_stride, const T* __restrict__ fmeans,
+                                                     const T* __restrict__ fchols, T* __restrict__ selems) {
+  using GL = SmoLayout<D>;
+  constexpr int D2 = 2 * D;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const T* Fk = F + k * ft_stride;
+  const T* Qk = QL + k * ft_stride;
+  const T* m = fmeans + k * D;
+  const T* L = fchols + k * D * D;
+  T X[D * D2], Y[D * D2];
+  mm<T, D, D, D, D, D, D2>(Fk, L, X);
+  copy<T, D, D, D, D2>(Qk, X + D);
+  copy<T, D, D, D, D2>(L, Y);
+  zero<T, D, D, D2>(Y + D);
+  tria_top<T, D, D, D2, D2, D2>(X, Y);
+  tria<T, D, D, D2>(Y + D);
+  T ge[GL::NG];
+  T Et[D * D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) Et[i * D + j] = Y[j * D2 + i];
+  trsm_lt<T, D, D, D2, D>(X, Et);
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) ge[GL::E + i * D + j] = Et[j * D + i];
+  T mm_[D], Emp[D];
+  mv<T, D, D, D>(Fk, m, mm_);
+  mv<T, D, D, D>(ge + GL::E, mm_, Emp);
+#pragma unroll
+  for (int i = 0; i < D; ++i) ge[GL::G + i] = m[i] - Emp[i];
+  copy<T, D, D, D2, D>(Y + D, ge + GL::DM);
+  st_soa<T, GL::NG>(selems, n, k, ge);
+}
+
+}  // namespace pof

@@ -1,0 +1,10 @@
+// float64 kernels for D = 10, d = 2 (one translation unit per shape so the
+// build compiles shapes in parallel).
+#include "pof_table.cuh"
+
+namespace pof {
+template <>
+const Ops* ops_shape<10, 2>(int dtype) {
+  return dtype == 0 ? OpsImpl<double, 10, 2>::get() : nullptr;
+}
+}  // namespace pof

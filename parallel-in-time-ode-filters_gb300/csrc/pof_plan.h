@@ -1,0 +1,86 @@
+// Level structure and workspace layout of the chunked filter/smoother.
+// Host-only; shared by the workspace-size queries and the launches so both
+// always agree.
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+namespace pof {
+
+constexpr int kMaxLevels = 24;
+constexpr int kTop = 8;  // at most this many elements are scanned by one thread
+
+struct Plan {
+  int64_t n = 0;  // time steps
+  int D = 0, DY = 0, esz = 8;
+  int C0 = 4;  // steps per level-0 chunk
+  int Cg = 8;  // elements per chunk at levels >= 1
+  int nlev = 1;
+  int64_t cnt[kMaxLevels] = {0};  // cnt[l], l = 1..nlev (cnt[nlev] <= kTop)
+  size_t felem[kMaxLevels] = {0}, fstate[kMaxLevels] = {0}, gelem[kMaxLevels] = {0}, gend[kMaxLevels] = {0};
+  size_t selem = 0, partials = 0, scalars = 0, scale = 0;
+  size_t H = 0, c = 0, means2 = 0, params = 0;
+  size_t total = 0;
+};
+
+inline int pick_c0(int64_t n) {
+  // Enough level-0 chunks to give every SM several threads, and long enough
+  // chunks that the per-step work (cheapest formulas) dominates the levels
+  // above (general combines, ~3x the per-step flops).
+  int c = 4;
+  while (c < 64 && n / c > 16384) c *= 2;
+  return c;
+}
+
+inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+// with_solver: also reserve the EK1 (H, c) buffers, a second means buffer
+// and a parameter slot used by the IEKS loop.
+inline Plan make_plan(int64_t n, int D, int DY, int esz, bool with_solver, int C0 = 0, int Cg = 0) {
+  Plan p;
+  p.n = n;
+  p.D = D;
+  p.DY = DY;
+  p.esz = esz;
+  p.C0 = C0 > 0 ? C0 : pick_c0(n);
+  p.Cg = Cg > 1 ? Cg : 8;
+  const int64_t NF = 3LL * D * D + 2 * D;  // filter element (A, b, U, eta, Z)
+  const int64_t NS = D + (int64_t)D * D;   // state (m, L)
+  const int64_t NG = D + 2LL * D * D;      // smoother element (g, E, Dm)
+  p.cnt[1] = (n + p.C0 - 1) / p.C0;
+  int l = 1;
+  while (p.cnt[l] > kTop && l + 1 < kMaxLevels) {
+    p.cnt[l + 1] = (p.cnt[l] + p.Cg - 1) / p.Cg;
+    ++l;
+  }
+  p.nlev = l;
+  size_t off = 0;
+  auto take = [&](int64_t elems) {
+    size_t o = off;
+    off = align_up(off + (size_t)elems * (size_t)esz);
+    return o;
+  };
+  for (int k = 1; k <= p.nlev; ++k) {
+    p.felem[k] = take(NF * p.cnt[k]);
+    p.fstate[k] = take(NS * p.cnt[k]);
+    p.gelem[k] = take(NG * p.cnt[k]);
+    p.gend[k] = take(NS * p.cnt[k]);
+  }
+  p.selem = take(NG * n);
+  p.partials = off;
+  off = align_up(off + sizeof(double) * 5 * (size_t)p.cnt[1]);
+  p.scalars = off;
+  off = align_up(off + sizeof(double) * 16);
+  p.scale = take(4);
+  if (with_solver) {
+    p.H = take((int64_t)DY * D * n);
+    p.c = take((int64_t)DY * n);
+    p.means2 = take((int64_t)D * (n + 1));
+    p.params = take(16);
+  }
+  p.total = off + 256;
+  return p;
+}
+
+}  // namespace pof

@@ -1,0 +1,37 @@
+// Dispatch from runtime (D, d) to the compiled shapes (one translation unit
+// per shape: pof_inst_D<D>_d<d>.cu).
+#include "pof_table.cuh"
+
+namespace pof {
+
+template <> const Ops* ops_shape<2, 1>(int dtype);
+template <> const Ops* ops_shape<3, 1>(int dtype);
+template <> const Ops* ops_shape<4, 1>(int dtype);
+template <> const Ops* ops_shape<6, 1>(int dtype);
+template <> const Ops* ops_shape<4, 2>(int dtype);
+template <> const Ops* ops_shape<6, 2>(int dtype);
+template <> const Ops* ops_shape<8, 2>(int dtype);
+template <> const Ops* ops_shape<10, 2>(int dtype);
+template <> const Ops* ops_shape<6, 3>(int dtype);
+template <> const Ops* ops_shape<9, 3>(int dtype);
+template <> const Ops* ops_shape<8, 4>(int dtype);
+
+const Ops* find_shape(int dtype, int D, int DY) {
+  if (DY < 1 || DY > 9) return nullptr;
+  switch (D * 10 + DY) {
+    case 21: return ops_shape<2, 1>(dtype);
+    case 31: return ops_shape<3, 1>(dtype);
+    case 41: return ops_shape<4, 1>(dtype);
+    case 61: return ops_shape<6, 1>(dtype);
+    case 42: return ops_shape<4, 2>(dtype);
+    case 62: return ops_shape<6, 2>(dtype);
+    case 82: return ops_shape<8, 2>(dtype);
+    case 102: return ops_shape<10, 2>(dtype);
+    case 63: return ops_shape<6, 3>(dtype);
+    case 93: return ops_shape<9, 3>(dtype);
+    case 84: return ops_shape<8, 4>(dtype);
+    default: return nullptr;
+  }
+}
+
+}  // namespace pof

@@ -1,0 +1,96 @@
+"""Drop-in solver API (pof/solver.py)."""
+
+import torch
+
+from . import _lib
+from . import convergence_criteria
+from .convenience import get_initial_trajectory, set_up_solver
+from .sequential_filtsmooth import filtsmooth as seq_fs
+from .step import ieks_step
+from .utils import MVNSqrt, gmul_stack
+
+
+def _solve_builtin(setup, states, calibrate, maxiters):
+    """The whole IEKS loop in libpof (pof_ieks_solve): linearization, chunked
+    filter/smoother, calibration and the convergence test all on the device."""
+    om = setup["om"]
+    name, params = om.field
+    x0 = setup["x0"]
+    means = states.mean.to(torch.float64).contiguous().clone()
+    N, D = means.shape
+    n = N - 1
+    d = setup["iwp"].wiener_process_dimension
+    dev = means.device
+    F = setup["dtm"].F[0].contiguous()
+    QL = setup["dtm"].QL[0].contiguous()
+    chols = torch.empty((N, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+    p = torch.tensor(params if params else (0.0,), dtype=torch.float64, device=dev)
+    lib = _lib.lib()
+    wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+    ws = _lib.workspace(wsb, dev)
+    m0 = x0.mean.contiguous()
+    L0 = x0.chol.contiguous()
+    rc = lib.pof_ieks_solve(_lib.POF_F64, n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]), _lib.ptr(m0),
+                            _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means), _lib.ptr(chols), int(maxiters),
+                            int(bool(calibrate)), _lib.ptr(info), _lib.ptr(ws), wsb, _lib.stream_handle())
+    _lib.check(rc, "pof_ieks_solve")
+    info_dict = {
+        "iterations": info[_lib.I_ITERATIONS].to(torch.int64),
+        "nll": info[_lib.I_NLL],
+        "obj": info[_lib.I_OBJ],
+        "sigma_squared": info[_lib.I_SSQ],
+        "calibrated": bool(calibrate),
+    }
+    return MVNSqrt(means, chols), info_dict
+
+
+def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, sequential=False):
+    """Parallel-in-time IEKS (pof/solver.py:11-73).
+
+    Returns (MVNSqrt(means (N, d), chol_covs (N, d, D)), info) with
+    info = {iterations, nll, obj, sigma_squared, calibrated}.  Built-in fields
+    (pof.ivp) run the whole loop on the device; other torch vector fields are
+    linearized with torch.func on the device and filtered/smoothed by libpof,
+    with the loop test read back each iteration."""
+    setup = set_up_solver(f=f, y0=y0, ts=ts, order=order)
+    dtm = setup["dtm"]
+    om = setup["om"]
+    x0 = setup["x0"]
+    states = get_initial_trajectory(setup, method=init)
+
+    if om.field is not None and not sequential and _lib.shape_supported(x0.mean.shape[0], setup["iwp"].wiener_process_dimension):
+        states, info_dict = _solve_builtin(setup, states, calibrate, maxiters)
+        return gmul_stack(setup["E0"], states), info_dict
+
+    dev = x0.mean.device
+    z = torch.zeros((), dtype=torch.float64, device=dev)
+    nll = obj = ssq = z
+    states_old, nll_old, obj_old = states, z, z
+    k = 0
+    while True:
+        # cond (solver.py:36-45)
+        if not (k < 1 or (not bool(convergence_criteria.crit(obj, obj_old, nll, nll_old, states, states_old))
+                          and k <= maxiters)):
+            break
+        # body (solver.py:47-55)
+        states_old, nll_old, obj_old = states, nll, obj
+        states, nll, obj, ssq = ieks_step(om=om, dtm=dtm, x0=x0, states=states_old, sequential=sequential)
+        k += 1
+    info_dict = {"iterations": torch.tensor(k), "nll": nll, "obj": obj, "sigma_squared": ssq, "calibrated": False}
+    if calibrate:
+        states = MVNSqrt(states.mean, ssq**0.5 * states.chol)
+        info_dict["calibrated"] = True
+    return gmul_stack(setup["E0"], states), info_dict
+
+
+def sequential_eks_solve(*, f, y0, ts, order, return_full_states=False, calibrate=True):
+    """One extended Kalman smoother pass (pof/solver.py:76-96)."""
+    setup = set_up_solver(f=f, y0=y0, ts=ts, order=order)
+    states, nll, obj, ssq = seq_fs(setup["x0"], setup["dtm"], setup["om"])
+    info_dict = {"nll": nll, "obj": obj, "sigma_squared": ssq, "calibrated": False}
+    if calibrate:
+        states = MVNSqrt(states.mean, ssq**0.5 * states.chol)
+        info_dict["calibrated"] = True
+    M = setup["P"] if return_full_states else setup["E0"]
+    return gmul_stack(M, states), info_dict

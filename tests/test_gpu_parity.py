@@ -1,0 +1,207 @@
+"""libpof (CUDA, sm_103a) against the NumPy float64 oracle on identical
+inputs.  Tolerances: means and covariances (compared as L L^T, square roots
+are sign/rotation ambiguous) 1e-10 relative (normwise); NLL and objectives
+1e-10 relative; sigma^2 1e-10 relative for d = 1 and against the oracle run
+with the kernels' chunking for d >= 2 (the reference's whiten quirk,
+pof/utils.py:110-112, makes sigma^2 depend on the factors' sign pattern)."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import blocked, filtsmooth as ofs, ivp as oivp, solver as osolver
+from pof import _lib, ivp as pivp, parallel_filtsmooth as pfs, sequential_filtsmooth as sfs, solver as psolver
+from pof.utils import MVNSqrt
+from pof.transitions import TransitionModel
+from pof.observations import AffineModel
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def T(x):
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device="cuda")
+
+
+def N_(x):
+    return x.detach().cpu().numpy()
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def covrel(a, b):
+    A = a @ np.swapaxes(a, -1, -2)
+    B = b @ np.swapaxes(b, -1, -2)
+    return rel(A, B)
+
+
+def chunking(n):
+    """The GPU plan's level-0 chunk and the level sizes (pof_plan.h)."""
+    c0 = 4
+    while c0 < 64 and n // c0 > 16384:
+        c0 *= 2
+    return c0, (8,) * 24
+
+
+PROBLEMS = {
+    "logistic_q2": (lambda: oivp.logistic(r=3.0), 77, 2, 30),
+    "lv_q1": (lambda: oivp.lotkavolterra(), 50, 1, 30),
+    "vdp_q3": (lambda: oivp.vanderpol(stiffness_constant=1.0), 130, 3, 30),
+    "fhn_q3": (lambda: oivp.fhn_classic(tmax=10.0), 200, 3, 40),
+    "rigid_q2": (lambda: oivp.rigid_body(), 100, 2, 30),
+    "hh_q1": (lambda: oivp.henonheiles(tmax=10.0), 64, 1, 30),
+    "logistic_q5": (lambda: oivp.logistic(r=3.0), 300, 5, 30),
+}
+
+
+def problem(key):
+    ivpf, N, q, iters = PROBLEMS[key]
+    ivp = ivpf()
+    ts = np.linspace(ivp.t0, ivp.tmax, N)
+    states, info, st = osolver.solve(ivp, ts, q, init="constant", maxiters=iters, return_full=True)
+    dom = osolver.linearize_at_previous_states(st, states[0])
+    return st, (st.F, st.QL), dom
+
+
+def gpu_args(st, dtm, dom):
+    x0 = MVNSqrt(T(st.x0[0]), T(st.x0[1]))
+    gdtm = TransitionModel(T(dtm[0]), T(dtm[1]))
+    gdom = AffineModel(T(dom[0]), T(dom[1]), T(dom[2]))
+    return x0, gdtm, gdom
+
+
+@pytest.mark.parametrize("key", list(PROBLEMS))
+def test_linear_filtsmooth_parity(key):
+    st, dtm, dom = problem(key)
+    (om, oL), onll, oobj, ossq = ofs.linear_filtsmooth(st.x0, dtm, dom)
+    (gm, gL), gnll, gobj, gssq = pfs.linear_filtsmooth(*gpu_args(st, dtm, dom))
+    gm, gL = N_(gm), N_(gL)
+    assert rel(gm, om) <= TOL
+    assert covrel(gL, oL) <= TOL
+    assert abs(float(gnll) - onll) <= TOL * abs(onll)
+    assert abs(float(gobj) - oobj) <= TOL * abs(oobj)
+    d = dom[1].shape[-1]
+    if d == 1:
+        assert abs(float(gssq) - ossq) <= TOL * abs(ossq)
+    else:
+        c0, cs = chunking(dom[0].shape[0])
+        _, _, _, bssq, _ = blocked.filter_blocked(st.x0, dtm, dom, C0=c0, Cs=cs)
+        assert abs(float(gssq) - bssq) <= 1e-8 * abs(bssq)
+
+
+@pytest.mark.parametrize("key", ["logistic_q2", "vdp_q3", "fhn_q3"])
+def test_filtering_and_smoothing_entry_points(key):
+    st, dtm, dom = problem(key)
+    (fm, fL), fnll, fobj, _ = ofs.linear_noiseless_filtering(st.x0, dtm, dom)
+    x0, gdtm, gdom = gpu_args(st, dtm, dom)
+    (gm, gL), gnll, gobj, _ = pfs.linear_noiseless_filtering(x0, gdtm, gdom)
+    assert rel(N_(gm), fm) <= TOL and covrel(N_(gL), fL) <= TOL
+    assert abs(float(gnll) - fnll) <= TOL * abs(fnll)
+    assert abs(float(gobj) - fobj) <= TOL * abs(fobj)
+    # the smoother alone, from the oracle's filtered trajectory
+    (sm, sL), sobj = ofs.smoothing(dtm, (fm, fL))
+    (hm, hL), hobj = pfs.smoothing(gdtm, MVNSqrt(T(fm), T(fL)))
+    assert rel(N_(hm), sm) <= TOL and covrel(N_(hL), sL) <= TOL
+    assert abs(float(hobj) - sobj) <= TOL * abs(sobj)
+
+
+@pytest.mark.parametrize("key", ["logistic_q2", "vdp_q3", "rigid_q2"])
+def test_sequential_twin_parity(key):
+    st, dtm, dom = problem(key)
+    (om, oL), oell, oobj, ossq = ofs.sequential_linear_filtsmooth(st.x0, dtm, dom)
+    (gm, gL), gell, gobj, gssq = sfs.linear_filtsmooth(*gpu_args(st, dtm, dom))
+    assert rel(N_(gm), om) <= TOL and covrel(N_(gL), oL) <= TOL
+    assert abs(float(gell) - oell) <= TOL * abs(oell)
+    assert abs(float(gobj) - oobj) <= TOL * abs(oobj)
+    assert abs(float(gssq) - ossq) <= 1e-8 * abs(ossq)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 9, 31, 32, 33, 35, 257, 5001])
+def test_ragged_sizes(n):
+    """Chunk and level boundaries: n not a multiple of the chunk sizes, one
+    step, several hierarchy levels."""
+    ivp = oivp.logistic(r=3.0)
+    ts = np.linspace(0.0, 1.0, n + 1)
+    st = osolver.set_up_solver(ivp, ts, 2)
+    states = osolver.get_initial_trajectory(st, "constant")
+    dom = osolver.linearize_at_previous_states(st, states[0])
+    dtm = (st.F, st.QL)
+    (om, oL), onll, oobj, ossq = ofs.linear_filtsmooth(st.x0, dtm, dom)
+    (gm, gL), gnll, gobj, gssq = pfs.linear_filtsmooth(*gpu_args(st, dtm, dom))
+    assert rel(N_(gm), om) <= TOL and covrel(N_(gL), oL) <= TOL
+    assert abs(float(gnll) - onll) <= TOL * abs(onll)
+    assert abs(float(gobj) - oobj) <= TOL * max(abs(oobj), 1e-300)
+    assert abs(float(gssq) - ossq) <= TOL * abs(ossq)
+
+
+def test_deterministic():
+    st, dtm, dom = problem("fhn_q3")
+    args = gpu_args(st, dtm, dom)
+    a = pfs.linear_filtsmooth(*args)
+    b = pfs.linear_filtsmooth(*args)
+    assert torch.equal(a[0].mean, b[0].mean) and torch.equal(a[0].chol, b[0].chol)
+    assert float(a[1]) == float(b[1]) and float(a[2]) == float(b[2]) and float(a[3]) == float(b[3])
+
+
+SOLVES = [
+    ("logistic", lambda: (pivp.logistic(r=3.0), oivp.logistic(r=3.0)), 200, 3),
+    ("logistic_ref", lambda: (pivp.logistic(), oivp.logistic()), 64, 2),
+    ("vdp0", lambda: (pivp.vanderpol(stiffness_constant=1.0), oivp.vanderpol(stiffness_constant=1.0)), 128, 3),
+    ("rigid", lambda: (pivp.rigid_body(), oivp.rigid_body()), 128, 2),
+    ("lv", lambda: (pivp.lotkavolterra(), oivp.lotkavolterra()), 256, 1),
+]
+
+
+@pytest.mark.parametrize("name,mk,N,q", SOLVES)
+def test_solve_parity(name, mk, N, q):
+    """pof.solver.solve runs the whole IEKS loop in libpof: same iteration
+    count as the oracle, means and covariances within 1e-10."""
+    p, o = mk()
+    ts = np.linspace(o.t0, o.tmax, N)
+    (om, oL), oinfo = osolver.solve(o, ts, q, init="constant", maxiters=1000)
+    out, info = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant", maxiters=1000)
+    assert int(info["iterations"]) == oinfo["iterations"]
+    assert rel(N_(out.mean), om) <= TOL
+    assert covrel(N_(out.chol), oL) <= 1e-9 if o.y0.shape[0] > 1 else covrel(N_(out.chol), oL) <= TOL
+    assert abs(float(info["obj"]) - oinfo["obj"]) <= 1e-9 * abs(oinfo["obj"]) + 1e-12
+    assert abs(float(info["nll"]) - oinfo["nll"]) <= 1e-9 * abs(oinfo["nll"])
+
+
+def test_solve_user_field_matches_builtin():
+    """A plain torch vector field (linearized with torch.func on the GPU)
+    gives the built-in field's result."""
+    p = pivp.logistic(r=3.0)
+    ts = np.linspace(0.0, 10.0, 100)
+
+    def f(t, y):
+        return 3.0 * y * (1 - y)
+
+    a, ia = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=3, init="constant")
+    b, ib = psolver.solve(f=f, y0=p.y0, ts=ts, order=3, init="constant")
+    assert int(ia["iterations"]) == int(ib["iterations"])
+    assert rel(N_(b.mean), N_(a.mean)) <= TOL
+
+
+@pytest.mark.parametrize("init", ["prior", "coarse"])
+def test_solve_other_inits(init):
+    p, o = pivp.logistic(), oivp.logistic()
+    ts = np.linspace(0.0, 10.0, 60)
+    (om, oL), oinfo = osolver.solve(o, ts, 2, init=init, maxiters=1000)
+    out, info = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=2, init=init, maxiters=1000)
+    assert int(info["iterations"]) == oinfo["iterations"]
+    assert rel(N_(out.mean), om) <= 1e-9
+
+
+def test_sequential_solves():
+    p, o = pivp.vanderpol(stiffness_constant=1.0), oivp.vanderpol(stiffness_constant=1.0)
+    ts = np.linspace(0.0, 6.3, 100)
+    (om, oL), oinfo = osolver.sequential_eks_solve(o, ts, 3)
+    out, info = psolver.sequential_eks_solve(f=p.f, y0=p.y0, ts=ts, order=3)
+    assert rel(N_(out.mean), om) <= TOL and covrel(N_(out.chol), oL) <= 1e-9
+    (sm, sL), sinfo = osolver.solve(o, ts, 3, init="constant", sequential=True, maxiters=1000)
+    out2, info2 = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=3, init="constant", sequential=True, maxiters=1000)
+    assert int(info2["iterations"]) == sinfo["iterations"]
+    assert rel(N_(out2.mean), sm) <= TOL

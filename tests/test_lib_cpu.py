@@ -1,0 +1,109 @@
+"""libpof.so loads and exports every entry point of include/pof.h; host-side
+logic that needs no GPU (CPU only)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "pof.h")
+
+
+def header_functions():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(pof_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pof import _build, _lib
+
+    _build.build(verbose=False)  # no-op when up to date
+    return _lib.lib()
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    for n in ("pof_linear_filtsmooth", "pof_linear_noiseless_filtering", "pof_smoothing", "pof_ieks_solve",
+              "pof_linearize", "pof_sequential_linear_filtsmooth", "pof_sequential_eks"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_header():
+    from pof import _lib
+
+    assert set(header_functions()) == set(_lib.exported_symbols())
+
+
+def test_status_strings(lib):
+    assert lib.pof_status_string(0) == b"ok"
+    assert b"workspace" in lib.pof_status_string(-3)
+    assert lib.pof_version() >= 1
+
+
+def test_shapes_and_workspace_queries(lib):
+    from pof import _lib
+
+    assert _lib.shape_supported(8, 2) and _lib.shape_supported(4, 1)
+    assert not _lib.shape_supported(7, 2)
+    w1 = lib.pof_filtsmooth_workspace_bytes(0, 999, 8, 2)
+    w2 = lib.pof_filtsmooth_workspace_bytes(0, 9999, 8, 2)
+    assert 0 < w1 < w2
+    assert lib.pof_ieks_workspace_bytes(0, 999, 8, 2) > w1
+    assert lib.pof_filtsmooth_workspace_bytes(0, 0, 8, 2) == 0
+
+
+def test_argument_errors_without_gpu(lib):
+    """Invalid arguments are rejected on the host before any CUDA call."""
+    null = ctypes.c_void_p(0)
+    rc = lib.pof_linear_filtsmooth(0, 10, 7, 2, null, null, null, null, 0, null, null, null, 0, null, null, null,
+                                   null, 0, null)
+    assert rc == -2  # shape not compiled
+    rc = lib.pof_linear_filtsmooth(5, 10, 8, 2, null, null, null, null, 0, null, null, null, 0, null, null, null,
+                                   null, 0, null)
+    assert rc == -6  # dtype
+    rc = lib.pof_linear_filtsmooth(0, 10, 8, 2, null, null, null, null, 0, null, null, null, 0, null, null, null,
+                                   null, 0, null)
+    assert rc == -1  # null pointers
+    rc = lib.pof_linearize(0, 10, 8, 2, 1, null, 0.1, null, null, null, null)
+    assert rc == -5  # logistic is d = 1
+
+
+def test_transitions_match_oracle():
+    import numpy as np
+    import torch
+
+    from oracle import core
+    from pof import transitions as tr
+
+    iwp = tr.IWP(wiener_process_dimension=2, num_derivatives=3)
+    A, L = tr.preconditioned_discretize(iwp, device=torch.device("cpu"))
+    oA, oL = core.preconditioned_discretize(2, 3)
+    assert np.array_equal(A.numpy(), oA) and np.array_equal(L.numpy(), oL)
+    P, PI = tr.nordsieck_preconditioner(iwp, 0.1, device=torch.device("cpu"))
+    oP, oPI = core.nordsieck_preconditioner(2, 3, 0.1)
+    assert np.allclose(P.numpy(), oP, rtol=1e-15) and np.allclose(PI.numpy(), oPI, rtol=1e-15)
+
+
+@pytest.mark.parametrize("name,ctor,q", [("fhn_classic", "fhn_classic", 4), ("logistic", "logistic", 3),
+                                         ("threebody", "threebody", 3), ("lotkavolterra", "lotkavolterra", 5)])
+def test_taylor_mode_matches_oracle(name, ctor, q):
+    """torch.func nested-jvp Taylor mode == the oracle's Taylor arithmetic."""
+    import numpy as np
+
+    from oracle import ivp as oivp, taylor
+    from pof import initialization, ivp
+
+    p = getattr(ivp, ctor)()
+    o = getattr(oivp, ctor)()
+    a = initialization.taylor_derivatives(p.f, p.y0, q).numpy()
+    b = taylor.taylor_derivatives(o.components, o.y0, q)
+    assert np.allclose(a, b, rtol=1e-13, atol=1e-13)
