@@ -1,0 +1,405 @@
+"""Benchmark: plain float64 parallel-in-time IEKS, one IVP per launch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload NAME]
+
+A step is one complete solve -- pof.solver.solve(f, y0, ts, order,
+init="constant") iterated to the reference's convergence criterion -- of the
+named workload (default: FitzHugh-Nagumo, (a, b, c) = (0.2, 0.2, 3), q = 3,
+D = 8, on a uniform grid).  Metric: IVP*steps/s = (N - 1) / solve time.
+
+value        device-resident: inputs already in HBM, the whole IEKS loop in
+             libpof (pof_ieks_solve), per-solve CUDA events, L2 flushed
+             between solves.
+e2e          the same solve through the public API with host (numpy) inputs,
+             results copied back to host memory.
+roofline     the dominant kernel's achieved FP64 rate (flop model
+             pof/_flops.py / its launch time from libpof's event profiler)
+             against the FP64 FMA throughput measured on this GPU by
+             pof_fp64_probe.
+cpu_baseline the NumPy float64 oracle (the reference's algorithm) on a
+             bounded sample of the same workload.
+--impl reference  the CPU restatement of the reference (oracle) alone, on the
+             same workload and metric (the reference itself needs JAX, which
+             is not installed on these machines).
+
+Multi-GPU: each rank solves its own copy of the workload (replicas; the path
+does not shard a single solve), value = sum over ranks.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "parallel-in-time-ode-filters_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    # name: (ivp constructor (pof.ivp / oracle.ivp name, kwargs), t1, q, N)
+    "fhn_q3_N16384": ("fhn_classic", {}, 100.0, 3, 2**14),
+    "fhn_q3_N65536": ("fhn_classic", {}, 100.0, 3, 2**16),
+    "fhn_q3_N262144": ("fhn_classic", {}, 100.0, 3, 2**18),
+    "fhn_q3_N1048576": ("fhn_classic", {}, 100.0, 3, 2**20),
+    "logistic_q3_N65536": ("logistic", {"r": 3.0}, 10.0, 3, 2**16),
+    "logistic_q3_N1048576": ("logistic", {"r": 3.0}, 10.0, 3, 2**20),
+    "fhn_q3_N1000": ("fhn_classic", {}, 100.0, 3, 1000),
+}
+DEFAULT_WORKLOAD = "fhn_q3_N65536"
+MAXITERS = 10_000  # the reference's default (pof/solver.py:12)
+
+
+def jprint(obj):
+    print(json.dumps(obj), flush=True)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle (NumPy float64 restatement of the reference)
+# ---------------------------------------------------------------------------
+
+
+def cpu_sample(workload, budget_s=20.0, iterations=None):
+    """Per-step-iteration cost of the reference's algorithm (oracle,
+    associative-scan tree of jax.lax.associative_scan) on a contiguous
+    sub-grid of the workload, grown until the sample takes ~budget_s / 4;
+    the full solve's time is that cost x (N - 1) x iterations."""
+    from oracle import ivp as oivp, solver as osolver
+
+    name, kw, t1, q, N = WORKLOADS[workload]
+    ivp = getattr(oivp, name)(**kw)
+    dt = (t1 - ivp.t0) / (N - 1)
+    M = 256
+    best = None
+    while True:
+        ts = ivp.t0 + dt * np.arange(M + 1)
+        st = osolver.set_up_solver(ivp, ts, q)
+        states = osolver.get_initial_trajectory(st, "constant")
+        t0 = time.perf_counter()
+        osolver.ieks_step(st, states)
+        el = time.perf_counter() - t0
+        best = (M, el)
+        if el > budget_s / 4 or M >= N - 1:
+            break
+        M = min(M * 4, N - 1)
+    M, el = best
+    per_step_iter = el / M
+    its = iterations
+    solve_s = per_step_iter * (N - 1) * its
+    return {
+        "per_step_iter_s": per_step_iter,
+        "solve_s": solve_s,
+        "value": (N - 1) / solve_s,
+        "sample": "one IEKS iteration (ieks_step) of the oracle on the first %d steps of the grid; solve time "
+        "extrapolated as cost per step-iteration x (N-1) x %d iterations (the GPU solve's count)" % (M, its),
+        "cores": 1,
+    }
+
+
+def run_reference(args, workload):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    iters = EXPECTED_ITERATIONS.get(workload)
+    samples = []
+    for _ in range(args.warmup):
+        cpu_sample(workload, budget_s=4.0, iterations=iters or 1)
+    for _ in range(args.steps):
+        samples.append(cpu_sample(workload, budget_s=8.0, iterations=iters or 1))
+    name, kw, t1, q, N = WORKLOADS[workload]
+    solve_s = float(np.median([s["solve_s"] for s in samples]))
+    value = (N - 1) / solve_s
+    jprint(
+        {
+            "impl": "reference",
+            "metric": "IVP*steps/s (parallel IEKS solve, float64)",
+            "value": value,
+            "unit": "IVP*steps/s",
+            "n_gpus": args.gpus,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": solve_s * 1e3,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": workload, "ivp": name, "q": q, "N": N, "t1": t1, "init": "constant",
+                       "iterations": iters},
+            "cpu_baseline": {"value": value, "unit": "IVP*steps/s", "cores": 1, "kind": "port",
+                             "sample": samples[-1]["sample"]},
+            "e2e": {"value": value, "unit": "IVP*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference is JAX (not installed here); this arm times the NumPy float64 restatement of its "
+                    "algorithm (oracle/), single-threaded LAPACK calls",
+        }
+    )
+
+
+# IEKS iteration counts of the workloads (measured by the GPU arm, which
+# reports its own count); the CPU arm extrapolates its sample with them
+EXPECTED_ITERATIONS = {}
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except Exception:
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp64_peak(torch, lib, _lib):
+    """FP64 FMA throughput of this GPU (GFLOP/s), pof_fp64_probe."""
+    dev = torch.cuda.current_device()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    sink = torch.zeros(blocks, dtype=torch.float64, device="cuda")
+    s = _lib.stream_handle()
+    best = 0.0
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.check(lib.pof_fp64_probe(iters, blocks, threads, _lib.ptr(sink), s), "pof_fp64_probe")
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = max(best, 16.0 * iters * blocks * threads / (ms * 1e-3) / 1e9)
+    return best
+
+
+def run_gpu(args, workload):
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from pof import _build, _flops, _lib, ivp as pivp, solver as psolver
+    from pof.convenience import get_initial_trajectory, set_up_solver
+
+    _build.build(verbose=False)
+    lib = _lib.lib()
+    name, kw, t1, q, N = WORKLOADS[workload]
+    p = getattr(pivp, name)(**kw)
+    ts_host = np.linspace(p.t0, t1, N)
+    setup = set_up_solver(f=p.f, y0=p.y0, ts=ts_host, order=q)
+    init = get_initial_trajectory(setup, "constant")
+    D = init.mean.shape[1]
+    d = setup["iwp"].wiener_process_dimension
+    n = N - 1
+    fname, params = setup["om"].field
+    dev = torch.device("cuda", local)
+    means0 = init.mean.contiguous()
+    means = torch.empty_like(means0)
+    chols = torch.empty((N, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+    prm = torch.tensor(params, dtype=torch.float64, device=dev)
+    F = setup["dtm"].F[0].contiguous()
+    QL = setup["dtm"].QL[0].contiguous()
+    m0 = setup["x0"].mean.contiguous()
+    L0 = setup["x0"].chol.contiguous()
+    wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+    ws = _lib.workspace(wsb, dev)
+    flush = torch.empty(256 * 2**20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def solve_resident():
+        means.copy_(means0)
+        rc = lib.pof_ieks_solve(_lib.POF_F64, n, D, d, _lib.FIELDS[fname], _lib.ptr(prm), float(setup["dt"]),
+                                _lib.ptr(m0), _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means),
+                                _lib.ptr(chols), MAXITERS, 1, _lib.ptr(info), _lib.ptr(ws), wsb,
+                                _lib.stream_handle())
+        _lib.check(rc, "pof_ieks_solve")
+
+    for _ in range(args.warmup):
+        solve_resident()
+    torch.cuda.synchronize()
+    iterations = int(info[_lib.I_ITERATIONS].item())
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # timed region: K solves, per-solve events, L2 flushed between solves
+    times = []
+    barrier()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            solve_resident()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        barrier()
+    ms = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms * 1e-3)
+
+    # per-kernel times of one more solve (profiler on; not part of the timing)
+    _lib.profile_enable(True)
+    _lib.profile_read(reset=True)
+    solve_resident()
+    torch.cuda.synchronize()
+    prof = _lib.profile_read(reset=True)
+    _lib.profile_enable(False)
+    launches_per_solve = sum(c for _, c in prof.values()) + 3  # + init, final scale, info copy
+    it_flops = _flops.iteration_flops(n, D, d)
+    kern = {k: v for k, v in prof.items() if v[1] > 0 and k in it_flops}
+    dom_kind = max(kern, key=lambda k: kern[k][0])
+    dom_ms_per_launch = kern[dom_kind][0] / kern[dom_kind][1]
+    C0, cnt = _flops.plan_levels(n)
+    launches_per_iter_dom = kern[dom_kind][1] / iterations
+    dom_flops = it_flops[dom_kind] / launches_per_iter_dom
+    peak = fp64_peak(torch, lib, _lib)
+    achieved = dom_flops / (dom_ms_per_launch * 1e-3) / 1e9
+    total_prof_ms = sum(v[0] for v in prof.values())
+
+    # end to end through the public API with host inputs / outputs
+    e2e_times = []
+    h2d = d2h = 0
+    y0_host = p.y0.numpy()
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ys, inf = psolver.solve(f=p.f, y0=y0_host, ts=ts_host, order=q, init="constant", maxiters=MAXITERS)
+        m_host = ys.mean.cpu().numpy()
+        c_host = ys.chol.cpu().numpy()
+        it_host = int(inf["iterations"])
+        el = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_times.append(el)
+        h2d = ts_host.nbytes + y0_host.nbytes
+        d2h = m_host.nbytes + c_host.nbytes + 8
+    e2e_s = float(np.mean(e2e_times))
+    e2e_value = world * n / e2e_s
+
+    if rank != 0:
+        return
+    out = {
+        "metric": "IVP*steps/s (parallel IEKS solve, float64)",
+        "value": value,
+        "unit": "IVP*steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload, "ivp": name, "params": list(params), "q": q, "D": D, "N": N, "t1": t1,
+                   "init": "constant", "iterations": iterations, "maxiters": MAXITERS,
+                   "l2": "flushed between solves (256 MiB write)", "C0": C0, "levels": cnt[1:]},
+        "e2e": {"value": e2e_value, "unit": "IVP*steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                "path": "pof.solver.solve(numpy y0, ts) -> means/chols .cpu()"},
+        "roofline": {"bound": "fp64", "kernel": dom_kind, "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured on this GPU by pof_fp64_probe (FP64 FMA chains); "
+                                    "MEASURED_PEAKS.json has no FP64 figure",
+                     "flops_per_launch": dom_flops, "ms_per_launch": dom_ms_per_launch},
+        "kernels": {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in prof.items() if v[1]},
+        "gpu_launches": int(launches_per_solve * args.steps),
+        "solve_flops": sum(it_flops.values()) * iterations,
+        "solve_gflops": sum(it_flops.values()) * iterations / (total_prof_ms * 1e-3) / 1e9,
+        "reference_equivalent_gflops": _flops.reference_step_flops(D, d) * n * iterations / (ms * 1e-3) / 1e9,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        EXPECTED_ITERATIONS[workload] = iterations
+        cb = cpu_sample(workload, budget_s=20.0, iterations=iterations)
+        out["cpu_baseline"] = {"value": cb["value"], "unit": "IVP*steps/s", "cores": cb["cores"], "kind": "port",
+                               "sample": cb["sample"]}
+    jprint(out)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args, args.workload)
+    else:
+        run_gpu(args, args.workload)
+
+
+if __name__ == "__main__":
+    main()

@@ -167,6 +167,23 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
                    void* chols, int64_t maxiters, int32_t calibrate, double* info, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* Per-kernel timing.  When enabled, every libpof launch is bracketed by CUDA
+ * events on its stream; pof_profile_read waits for them and returns the
+ * summed milliseconds and launch counts per kernel kind (POF_PK_*), in
+ * arrays of nkinds entries; returns the number of kinds.  One host thread. */
+enum {
+  POF_PK_LINEARIZE = 0, POF_PK_FILT_L0_REDUCE, POF_PK_FILT_REDUCE, POF_PK_FILT_TOP, POF_PK_FILT_DOWN,
+  POF_PK_FILT_L0_DOWN, POF_PK_FILT_FINALIZE, POF_PK_SMO_L0_REDUCE, POF_PK_SMO_REDUCE, POF_PK_SMO_TOP,
+  POF_PK_SMO_DOWN, POF_PK_SMO_L0_DOWN, POF_PK_SMO_FINALIZE, POF_PK_CONTROL, POF_PK_SEQUENTIAL, POF_PK_COUNT
+};
+void pof_profile_enable(int32_t on);
+/* FP64 FMA throughput probe (the roofline denominator of the float64
+ * kernels): blocks x threads threads each run 8 independent chains of
+ * `iters` fused multiply-adds (16 * iters flops per thread). `sink` is a
+ * device array of `blocks` doubles that is (almost) never written. */
+int pof_fp64_probe(int64_t iters, int32_t blocks, int32_t threads, double* sink, void* stream);
+int pof_profile_read(double* ms_out, int64_t* count_out, int32_t nkinds, int32_t reset);
+
 #ifdef __cplusplus
 }
 #endif

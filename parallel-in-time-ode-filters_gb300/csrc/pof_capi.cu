@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/pof.h"
 #include "pof_table.cuh"
@@ -61,9 +62,109 @@ char* aligned_ws(void* ws) {
   return reinterpret_cast<char*>(a);
 }
 
+// ---------------------------------------------------------------------------
+// Per-kernel timing (pof_profile_*): event pairs from a pool, recorded on
+// the launching stream, summed per kind when collected.  Single host thread.
+// ---------------------------------------------------------------------------
+struct ProfPair {
+  int kind;
+  cudaEvent_t b, e;
+};
+struct ProfState {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<ProfPair> open, done;
+  double ms[PK_COUNT] = {0};
+  int64_t count[PK_COUNT] = {0};
+};
+ProfState g_prof;
+
+cudaEvent_t prof_event() {
+  if (!g_prof.pool.empty()) {
+    cudaEvent_t e = g_prof.pool.back();
+    g_prof.pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void prof_collect() {
+  for (const ProfPair& pp : g_prof.done) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(pp.e) == cudaSuccess && cudaEventElapsedTime(&ms, pp.b, pp.e) == cudaSuccess) {
+      g_prof.ms[pp.kind] += ms;
+      g_prof.count[pp.kind] += 1;
+    }
+    g_prof.pool.push_back(pp.b);
+    g_prof.pool.push_back(pp.e);
+  }
+  g_prof.done.clear();
+}
+
 }  // namespace
 
+namespace pof {
+bool prof_on() { return g_prof.on; }
+void prof_begin(int kind, cudaStream_t st) {
+  ProfPair pp{kind, prof_event(), prof_event()};
+  cudaEventRecord(pp.b, st);
+  g_prof.open.push_back(pp);
+}
+void prof_end(int kind, cudaStream_t st) {
+  for (size_t i = g_prof.open.size(); i-- > 0;) {
+    if (g_prof.open[i].kind == kind) {
+      cudaEventRecord(g_prof.open[i].e, st);
+      g_prof.done.push_back(g_prof.open[i]);
+      g_prof.open.erase(g_prof.open.begin() + i);
+      return;
+    }
+  }
+}
+}  // namespace pof
+
 extern "C" {
+
+// FP64 FMA throughput probe: 8 independent dependency chains per thread.
+__global__ void k_fp64_probe(int64_t iters, double* sink) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double b = 0.999999999, c = 1e-12;
+  for (int64_t i = 0; i < iters; ++i) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) sink[blockIdx.x] = s;  // keeps the chains alive
+}
+
+int pof_fp64_probe(int64_t iters, int32_t blocks, int32_t threads, double* sink, void* stream) {
+  if (iters < 1 || blocks < 1 || threads < 1 || threads > 1024 || !sink) return POF_ERR_ARG;
+  k_fp64_probe<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(iters, sink);
+  return launch_status();
+}
+
+void pof_profile_enable(int32_t on) {
+  prof_collect();
+  g_prof.on = on != 0;
+}
+
+int pof_profile_read(double* ms_out, int64_t* count_out, int32_t nkinds, int32_t reset) {
+  prof_collect();
+  const int k = nkinds < PK_COUNT ? nkinds : PK_COUNT;
+  for (int i = 0; i < k; ++i) {
+    if (ms_out) ms_out[i] = g_prof.ms[i];
+    if (count_out) count_out[i] = g_prof.count[i];
+  }
+  if (reset) {
+    for (int i = 0; i < PK_COUNT; ++i) {
+      g_prof.ms[i] = 0.0;
+      g_prof.count[i] = 0;
+    }
+  }
+  return PK_COUNT;
+}
 
 const char* pof_status_string(int status) {
   switch (status) {
@@ -270,7 +371,10 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
     ops->linearize(n_steps, field, params, p0, p1, mold, Hb, cb, st);
     ops->filter(p, w, sm, x0_mean, x0_chol, mnew, chols, st);
     ops->smoother(p, w, F, QL, 0, mnew, chols, calibrate != 0, mold, st);
-    k_ieks_control<<<1, 32, 0, st>>>(scal, maxiters);
+    {
+      ProfScope ps(PK_CONTROL, st);
+      k_ieks_control<<<1, 32, 0, st>>>(scal, maxiters);
+    }
     rc = launch_status();
     if (rc) return rc;
     cur ^= 1;
@@ -278,6 +382,7 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
     cudaError_t e = cudaMemcpyAsync(&cont, scal + S_CONT, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_status(e);
+    if (g_prof.on) prof_collect();
     if (cont == 0.0) break;
   }
   if (bufs[cur] != means) {

@@ -7,6 +7,7 @@
 
 #include "pof_kernels.cuh"
 #include "pof_plan.h"
+#include "pof_prof.h"
 
 namespace pof {
 
@@ -90,6 +91,18 @@ static __global__ void k_copy_scalars(const double* __restrict__ src, double* __
 
 inline unsigned grid_for(int64_t count, int block) { return (unsigned)((count + block - 1) / block); }
 
+// Brackets one launch with profiler events when profiling is on.
+struct ProfScope {
+  int kind;
+  cudaStream_t st;
+  ProfScope(int k, cudaStream_t s) : kind(k), st(s) {
+    if (prof_on()) prof_begin(kind, st);
+  }
+  ~ProfScope() {
+    if (prof_on()) prof_end(kind, st);
+  }
+};
+
 template <typename T, int D, int DY>
 struct Driver {
   static constexpr int kBlock = 64;
@@ -110,50 +123,84 @@ struct Driver {
     Bufs b{ws, &p};
     const int64_t n = p.n;
     const int64_t n1 = p.cnt[1];
-    k_filt_l0_reduce<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(n, p.C0, sm, x0m, x0L,
-                                                                         b.template at<T>(p.felem[1]), n1);
-    for (int l = 1; l < p.nlev; ++l)
+    {
+      ProfScope ps(PK_FILT_L0_REDUCE, st);
+      k_filt_l0_reduce<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(n, p.C0, sm, x0m, x0L,
+                                                                           b.template at<T>(p.felem[1]), n1);
+    }
+    for (int l = 1; l < p.nlev; ++l) {
+      ProfScope ps(PK_FILT_REDUCE, st);
       k_filt_reduce<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
           b.template at<T>(p.felem[l]), p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
-    k_filt_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.felem[p.nlev]), p.cnt[p.nlev], x0m, x0L,
-                                       b.template at<T>(p.fstate[p.nlev]));
-    for (int l = p.nlev - 1; l >= 1; --l)
+    }
+    {
+      ProfScope ps(PK_FILT_TOP, st);
+      k_filt_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.felem[p.nlev]), p.cnt[p.nlev], x0m, x0L,
+                                         b.template at<T>(p.fstate[p.nlev]));
+    }
+    for (int l = p.nlev - 1; l >= 1; --l) {
+      ProfScope ps(PK_FILT_DOWN, st);
       k_filt_down<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
           b.template at<T>(p.felem[l]), p.cnt[l], p.Cg, b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
           b.template at<T>(p.fstate[l]));
-    k_filt_l0_down<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
-        n, p.C0, sm, b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
-        b.template at<double>(p.partials));
-    k_finalize_filter<T><<<1, 256, 0, st>>>(b.template at<double>(p.partials), n1, n, DY,
-                                            b.template at<double>(p.scalars), b.template at<T>(p.scale));
+    }
+    {
+      ProfScope ps(PK_FILT_L0_DOWN, st);
+      k_filt_l0_down<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
+          n, p.C0, sm, b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
+          b.template at<double>(p.partials));
+    }
+    {
+      ProfScope ps(PK_FILT_FINALIZE, st);
+      k_finalize_filter<T><<<1, 256, 0, st>>>(b.template at<double>(p.partials), n1, n, DY,
+                                              b.template at<double>(p.scalars), b.template at<T>(p.scale));
+    }
   }
 
-  // Smoother from the elements left by filter() (or built by
-  // build_smoother_elements) and the terminal state in means/chols[n].
+  // Smoother from the elements left by filter() (or by k_smo_elements) and
+  // the terminal state in means/chols[n].
   static void smoother(const Plan& p, char* ws, const T* F, const T* QL, int64_t ft_stride, T* means, T* chols,
                        bool calibrate, const T* means_old, cudaStream_t st) {
     Bufs b{ws, &p};
     const int64_t n = p.n;
     const int64_t n1 = p.cnt[1];
-    k_smo_reduce<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(b.template at<T>(p.selem), n, p.C0,
-                                                                b.template at<T>(p.gelem[1]), n1);
-    for (int l = 1; l < p.nlev; ++l)
+    {
+      ProfScope ps(PK_SMO_L0_REDUCE, st);
+      k_smo_reduce<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(b.template at<T>(p.selem), n, p.C0,
+                                                                  b.template at<T>(p.gelem[1]), n1);
+    }
+    for (int l = 1; l < p.nlev; ++l) {
+      ProfScope ps(PK_SMO_REDUCE, st);
       k_smo_reduce<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
           b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
-    k_smo_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.gelem[p.nlev]), p.cnt[p.nlev], means + n * D,
-                                      chols + n * D * D, b.template at<T>(p.gend[p.nlev]));
-    for (int l = p.nlev - 1; l >= 1; --l)
+    }
+    {
+      ProfScope ps(PK_SMO_TOP, st);
+      k_smo_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.gelem[p.nlev]), p.cnt[p.nlev], means + n * D,
+                                        chols + n * D * D, b.template at<T>(p.gend[p.nlev]));
+    }
+    for (int l = p.nlev - 1; l >= 1; --l) {
+      ProfScope ps(PK_SMO_DOWN, st);
       k_smo_down<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
           b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg, b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
           b.template at<T>(p.gend[l]));
-    k_smo_l0_down<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
-        n, p.C0, F, QL, ft_stride, b.template at<T>(p.selem), b.template at<T>(p.gend[1]), n1, means, chols,
-        calibrate ? b.template at<T>(p.scale) : nullptr, means_old, b.template at<double>(p.partials));
-    k_finalize_smoother<<<1, 256, 0, st>>>(b.template at<double>(p.partials), n1, b.template at<double>(p.scalars));
+    }
+    {
+      ProfScope ps(PK_SMO_L0_DOWN, st);
+      k_smo_l0_down<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
+          n, p.C0, F, QL, ft_stride, b.template at<T>(p.selem), b.template at<T>(p.gend[1]), n1, means, chols,
+          calibrate ? b.template at<T>(p.scale) : nullptr, means_old, b.template at<double>(p.partials));
+    }
+    {
+      ProfScope ps(PK_SMO_FINALIZE, st);
+      k_finalize_smoother<<<1, 256, 0, st>>>(b.template at<double>(p.partials), n1,
+                                             b.template at<double>(p.scalars));
+    }
   }
 
   static void linearize(int64_t n, int field, const T* params, T p0, T p1, const T* means, T* H, T* c,
                         cudaStream_t st) {
+    ProfScope ps(PK_LINEARIZE, st);
     k_linearize<T, D, DY><<<grid_for(n, 128), 128, 0, st>>>(n, field, params, p0, p1, means, H, c);
   }
 };

@@ -51,6 +51,7 @@ struct OpsImpl {
   static void sequential(int64_t n, const StepModel& sm, int field, const void* params, double p0, double p1,
                          const void* x0m, const void* x0L, int smooth, void* means, void* chols, double* scalars,
                          cudaStream_t st) {
+    ProfScope ps(PK_SEQUENTIAL, st);
     k_seq_filtsmooth<T, D, DY><<<1, 32, 0, st>>>(n, sm, field, static_cast<const T*>(params), (T)p0, (T)p1,
                                                  static_cast<const T*>(x0m), static_cast<const T*>(x0L), smooth,
                                                  static_cast<T*>(means), static_cast<T*>(chols), scalars);

@@ -75,7 +75,28 @@ _SIGS = {
         _c.c_int,
         [_i32, _i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _dp, _vp, _sz, _vp],
     ),
+    "pof_profile_enable": (None, [_i32]),
+    "pof_profile_read": (_c.c_int, [_vp, _vp, _i32, _i32]),
+    "pof_fp64_probe": (_c.c_int, [_i64, _i32, _i32, _dp, _vp]),
 }
+
+PROFILE_KINDS = [
+    "linearize", "filt_l0_reduce", "filt_reduce", "filt_top", "filt_down", "filt_l0_down", "filt_finalize",
+    "smo_l0_reduce", "smo_reduce", "smo_top", "smo_down", "smo_l0_down", "smo_finalize", "control", "sequential",
+]
+
+
+def profile_enable(on=True):
+    lib().pof_profile_enable(int(bool(on)))
+
+
+def profile_read(reset=True):
+    """{kind: (milliseconds, launches)} of the libpof launches since the last reset."""
+    n = len(PROFILE_KINDS)
+    ms = (ctypes.c_double * n)()
+    cnt = (ctypes.c_int64 * n)()
+    lib().pof_profile_read(ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(cnt, ctypes.c_void_p), n, int(bool(reset)))
+    return {k: (ms[i], cnt[i]) for i, k in enumerate(PROFILE_KINDS)}
 
 
 def lib():
