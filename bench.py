@@ -319,7 +319,7 @@ def run_gpu(args, workload):
     kern = {k: v for k, v in prof.items() if v[1] > 0 and k in it_flops}
     dom_kind = max(kern, key=lambda k: kern[k][0])
     dom_ms_per_launch = kern[dom_kind][0] / kern[dom_kind][1]
-    C0, cnt = _flops.plan_levels(n)
+    C0, cnt = _flops.plan_levels(n, D)
     launches_per_iter_dom = kern[dom_kind][1] / iterations
     dom_flops = it_flops[dom_kind] / launches_per_iter_dom
     peak = fp64_peak(torch, lib, _lib)

@@ -102,6 +102,28 @@ def get_sigma_squared(dtm, dom, means, cholcovs):
     return np.sum(ress * ress) / N / d
 
 
+def sigma_squared_envelope(dtm, dom, means, cholcovs):
+    """Range of the reference's sigma^2 (filter.py:105-114) over the column
+    signs of the observation chols.
+
+    ``whiten`` (utils.py:110-112) solves with L^T, so a step's term
+    r^T (L^T L)^{-1} r changes when columns of L flip sign (L -> L S); every
+    lower-triangular factor of the (full-rank) observation covariance is such
+    an L S, and which one a QR returns is decided by rounding for
+    rank-deficient filtered covariances.  Returns (lo, hi): sigma^2 with the
+    smallest / largest term per step."""
+    import itertools
+
+    N, d = dom[1].shape
+    om_, oc_ = get_obs(*dtm, *dom, means[:-1], cholcovs[:-1])
+    G = np.linalg.inv(T(oc_) @ oc_)  # (L^T L)^{-1}
+    signs = [np.array((1.0,) + s) for s in itertools.product((1.0, -1.0), repeat=d - 1)]
+    vals = np.stack([np.einsum("ni,nij,nj->n", om_ * s, G, om_ * s) for s in signs])
+    lo = vals.min(0).sum() / N / d
+    hi = vals.max(0).sum() / N / d
+    return lo, hi
+
+
 def filter_objective(dtm, means):
     """``filter.py:43-45``: argument order swapped as in the reference."""
     F, QL = dtm

@@ -6,6 +6,7 @@
 #include <math.h>
 
 #include "pof_kernels.cuh"
+#include "pof_team_kernels.cuh"
 #include "pof_plan.h"
 #include "pof_prof.h"
 
@@ -103,9 +104,24 @@ struct ProfScope {
   }
 };
 
+// Launch a team kernel over `nteams` teams (TeamBlock teams per block, one
+// shared-memory workspace per team).
+template <typename WS, int TS, typename... KArgs, typename... Args>
+inline void launch_team(void (*kern)(KArgs...), int64_t nteams, cudaStream_t st, Args... args) {
+  using B = TeamBlock<WS, TS>;
+  const unsigned grid = (unsigned)((nteams + B::teams - 1) / B::teams);
+  kern<<<grid, B::threads, B::teams * sizeof(WS), st>>>(args...);
+}
+
 template <typename T, int D, int DY>
 struct Driver {
   static constexpr int kBlock = 64;
+  static constexpr int TS = TeamSize<D>::v;
+  static constexpr bool kTeamL0 = D >= 6;  // pof_plan.h l0_lanes
+  using FWS = FiltTeamWs<T, D>;
+  using SWS = SmoTeamWs<T, D>;
+  using L0WS = L0TeamWs<T, D, DY>;
+  using SL0WS = SmoL0TeamWs<T, D>;
 
   struct Bufs {
     char* ws;
@@ -125,30 +141,39 @@ struct Driver {
     const int64_t n1 = p.cnt[1];
     {
       ProfScope ps(PK_FILT_L0_REDUCE, st);
-      k_filt_l0_reduce<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(n, p.C0, sm, x0m, x0L,
-                                                                           b.template at<T>(p.felem[1]), n1);
+      if constexpr (kTeamL0)
+        launch_team<L0WS, TS>(k_filt_l0_reduce_team<T, D, DY, TS>, n1, st, n, p.C0, sm, x0m, x0L,
+                              b.template at<T>(p.felem[1]), n1);
+      else
+        k_filt_l0_reduce<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(n, p.C0, sm, x0m, x0L,
+                                                                             b.template at<T>(p.felem[1]), n1);
     }
     for (int l = 1; l < p.nlev; ++l) {
       ProfScope ps(PK_FILT_REDUCE, st);
-      k_filt_reduce<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
-          b.template at<T>(p.felem[l]), p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
+      launch_team<FWS, TS>(k_filt_reduce_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
+                           p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
     }
     {
       ProfScope ps(PK_FILT_TOP, st);
-      k_filt_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.felem[p.nlev]), p.cnt[p.nlev], x0m, x0L,
-                                         b.template at<T>(p.fstate[p.nlev]));
+      launch_team<FWS, TS>(k_filt_top_team<T, D, TS>, 1, st, (const T*)b.template at<T>(p.felem[p.nlev]),
+                           p.cnt[p.nlev], x0m, x0L, b.template at<T>(p.fstate[p.nlev]));
     }
     for (int l = p.nlev - 1; l >= 1; --l) {
       ProfScope ps(PK_FILT_DOWN, st);
-      k_filt_down<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
-          b.template at<T>(p.felem[l]), p.cnt[l], p.Cg, b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
-          b.template at<T>(p.fstate[l]));
+      launch_team<FWS, TS>(k_filt_down_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
+                           p.cnt[l], p.Cg, (const T*)b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
+                           b.template at<T>(p.fstate[l]));
     }
     {
       ProfScope ps(PK_FILT_L0_DOWN, st);
-      k_filt_l0_down<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
-          n, p.C0, sm, b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
-          b.template at<double>(p.partials));
+      if constexpr (kTeamL0)
+        launch_team<L0WS, TS>(k_filt_l0_down_team<T, D, DY, TS>, n1, st, n, p.C0, sm,
+                              (const T*)b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
+                              b.template at<double>(p.partials));
+      else
+        k_filt_l0_down<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
+            n, p.C0, sm, b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
+            b.template at<double>(p.partials));
     }
     {
       ProfScope ps(PK_FILT_FINALIZE, st);
@@ -166,30 +191,41 @@ struct Driver {
     const int64_t n1 = p.cnt[1];
     {
       ProfScope ps(PK_SMO_L0_REDUCE, st);
-      k_smo_reduce<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(b.template at<T>(p.selem), n, p.C0,
-                                                                  b.template at<T>(p.gelem[1]), n1);
+      if constexpr (kTeamL0)
+        launch_team<SWS, TS>(k_smo_reduce_team<T, D, TS>, n1, st, (const T*)b.template at<T>(p.selem), n, p.C0,
+                             b.template at<T>(p.gelem[1]), n1);
+      else
+        k_smo_reduce<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(b.template at<T>(p.selem), n, p.C0,
+                                                                    b.template at<T>(p.gelem[1]), n1);
     }
     for (int l = 1; l < p.nlev; ++l) {
       ProfScope ps(PK_SMO_REDUCE, st);
-      k_smo_reduce<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
-          b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
+      launch_team<SWS, TS>(k_smo_reduce_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
+                           p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
     }
     {
       ProfScope ps(PK_SMO_TOP, st);
-      k_smo_top<T, D><<<1, 32, 0, st>>>(b.template at<T>(p.gelem[p.nlev]), p.cnt[p.nlev], means + n * D,
-                                        chols + n * D * D, b.template at<T>(p.gend[p.nlev]));
+      launch_team<SWS, TS>(k_smo_top_team<T, D, TS>, 1, st, (const T*)b.template at<T>(p.gelem[p.nlev]),
+                           p.cnt[p.nlev], (const T*)(means + n * D), (const T*)(chols + n * D * D),
+                           b.template at<T>(p.gend[p.nlev]));
     }
     for (int l = p.nlev - 1; l >= 1; --l) {
       ProfScope ps(PK_SMO_DOWN, st);
-      k_smo_down<T, D><<<grid_for(p.cnt[l + 1], kBlock), kBlock, 0, st>>>(
-          b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg, b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
-          b.template at<T>(p.gend[l]));
+      launch_team<SWS, TS>(k_smo_down_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
+                           p.cnt[l], p.Cg, (const T*)b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
+                           b.template at<T>(p.gend[l]));
     }
     {
       ProfScope ps(PK_SMO_L0_DOWN, st);
-      k_smo_l0_down<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
-          n, p.C0, F, QL, ft_stride, b.template at<T>(p.selem), b.template at<T>(p.gend[1]), n1, means, chols,
-          calibrate ? b.template at<T>(p.scale) : nullptr, means_old, b.template at<double>(p.partials));
+      const T* scl = calibrate ? b.template at<T>(p.scale) : nullptr;
+      if constexpr (kTeamL0)
+        launch_team<SL0WS, TS>(k_smo_l0_down_team<T, D, TS>, n1, st, n, p.C0, F, QL, ft_stride,
+                               (const T*)b.template at<T>(p.selem), (const T*)b.template at<T>(p.gend[1]), n1,
+                               means, chols, scl, means_old, b.template at<double>(p.partials));
+      else
+        k_smo_l0_down<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
+            n, p.C0, F, QL, ft_stride, b.template at<T>(p.selem), b.template at<T>(p.gend[1]), n1, means, chols,
+            scl, means_old, b.template at<double>(p.partials));
     }
     {
       ProfScope ps(PK_SMO_FINALIZE, st);

@@ -24,12 +24,19 @@ struct Plan {
   size_t total = 0;
 };
 
-inline int pick_c0(int64_t n) {
-  // Enough level-0 chunks to give every SM several threads, and long enough
-  // chunks that the per-step work (cheapest formulas) dominates the levels
-  // above (general combines, ~3x the per-step flops).
-  int c = 4;
-  while (c < 64 && n / c > 16384) c *= 2;
+// Lanes that work on one level-0 chunk: 1 (thread per chunk, state in
+// registers) for small D, a team of 16 or 32 lanes (state in shared memory)
+// from D = 6 on, where per-thread state would spill.  Must match
+// Driver::kTeamL0 / TeamSize.
+inline int l0_lanes(int D) { return D >= 6 ? (2 * D <= 16 ? 16 : 32) : 1; }
+
+inline int pick_c0(int64_t n, int lanes) {
+  // Enough level-0 chunks to keep every SM sub-partition's FP64 pipe fed
+  // (~16k lanes), chunks long enough that the per-step work (cheapest
+  // formulas) dominates the general combines of the levels above.
+  int c = lanes == 1 ? 4 : 2;
+  const int64_t target = lanes == 1 ? 16384 : (65536 / lanes > 1024 ? 65536 / lanes : 1024);
+  while (c < 64 && n / c > target) c *= 2;
   return c;
 }
 
@@ -43,7 +50,7 @@ inline Plan make_plan(int64_t n, int D, int DY, int esz, bool with_solver, int C
   p.D = D;
   p.DY = DY;
   p.esz = esz;
-  p.C0 = C0 > 0 ? C0 : pick_c0(n);
+  p.C0 = C0 > 0 ? C0 : pick_c0(n, l0_lanes(D));
   p.Cg = Cg > 1 ? Cg : 8;
   const int64_t NF = 3LL * D * D + 2 * D;  // filter element (A, b, U, eta, Z)
   const int64_t NS = D + (int64_t)D * D;   // state (m, L)

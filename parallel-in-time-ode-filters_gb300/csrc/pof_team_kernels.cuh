@@ -1,0 +1,512 @@
+// Levels >= 1 of the chunked scan with team-cooperative combines: one team
+// of TS lanes per chunk (pof_team.cuh).  Same buffers and element order as
+// the thread-per-chunk kernels of pof_kernels.cuh.
+#pragma once
+
+#include "pof_kernels.cuh"
+#include "pof_team.cuh"
+
+namespace pof {
+
+template <int D>
+struct TeamSize {
+  static constexpr int v = (2 * D <= 8) ? 8 : (2 * D <= 16 ? 16 : 32);
+};
+
+template <typename WS, int TS>
+struct TeamBlock {
+  // teams per 64-thread block, fewer when the workspaces exceed ~40 KB
+  static constexpr int per_warp_max = 64 / TS;
+  static constexpr int fit = (int)(40960 / sizeof(WS));
+  static constexpr int teams = fit < 1 ? 1 : (fit < per_warp_max ? fit : per_warp_max);
+  static constexpr int threads = teams * TS;
+};
+
+// SoA element <-> team workspace slot
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_load_filt(const Team<TS>& tm, const T* base, int64_t n, int64_t e, T* A, T* b,
+                                            T* U, T* eta, T* Z) {
+  using FL = FiltLayout<D>;
+  constexpr int L1 = Ld<D>::v;
+  for (int f = tm.r; f < FL::NF; f += TS) {
+    const T v = base[f * n + e];
+    if (f < FL::B)
+      A[(f / D) * L1 + f % D] = v;
+    else if (f < FL::U)
+      b[f - FL::B] = v;
+    else if (f < FL::ETA)
+      U[((f - FL::U) / D) * L1 + (f - FL::U) % D] = v;
+    else if (f < FL::Z)
+      eta[f - FL::ETA] = v;
+    else
+      Z[((f - FL::Z) / D) * L1 + (f - FL::Z) % D] = v;
+  }
+}
+
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_store_filt(const Team<TS>& tm, T* base, int64_t n, int64_t e, const T* A,
+                                             const T* b, const T* U, const T* eta, const T* Z) {
+  using FL = FiltLayout<D>;
+  constexpr int L1 = Ld<D>::v;
+  for (int f = tm.r; f < FL::NF; f += TS) {
+    T v;
+    if (f < FL::B)
+      v = A[(f / D) * L1 + f % D];
+    else if (f < FL::U)
+      v = b[f - FL::B];
+    else if (f < FL::ETA)
+      v = U[((f - FL::U) / D) * L1 + (f - FL::U) % D];
+    else if (f < FL::Z)
+      v = eta[f - FL::ETA];
+    else
+      v = Z[((f - FL::Z) / D) * L1 + (f - FL::Z) % D];
+    base[f * n + e] = v;
+  }
+}
+
+// state (m, L) <-> slot
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_load_state(const Team<TS>& tm, const T* base, int64_t n, int64_t e, T* m, T* L) {
+  constexpr int L1 = Ld<D>::v;
+  for (int f = tm.r; f < D + D * D; f += TS) {
+    const T v = base[f * n + e];
+    if (f < D)
+      m[f] = v;
+    else
+      L[((f - D) / D) * L1 + (f - D) % D] = v;
+  }
+}
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_store_state(const Team<TS>& tm, T* base, int64_t n, int64_t e, const T* m,
+                                              const T* L) {
+  constexpr int L1 = Ld<D>::v;
+  for (int f = tm.r; f < D + D * D; f += TS) base[f * n + e] = (f < D) ? m[f] : L[((f - D) / D) * L1 + (f - D) % D];
+}
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_load_state_plain(const Team<TS>& tm, const T* m0, const T* L0, T* m, T* L) {
+  constexpr int L1 = Ld<D>::v;
+  for (int f = tm.r; f < D + D * D; f += TS) {
+    if (f < D)
+      m[f] = m0[f];
+    else
+      L[((f - D) / D) * L1 + (f - D) % D] = L0[f - D];
+  }
+}
+
+// smoother element (g, E, Dm) <-> slot
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_load_smo(const Team<TS>& tm, const T* base, int64_t n, int64_t e, T* g, T* E,
+                                           T* Dm) {
+  using GL = SmoLayout<D>;
+  constexpr int L1 = Ld<D>::v;
+  for (int f = tm.r; f < GL::NG; f += TS) {
+    const T v = base[f * n + e];
+    if (f < GL::E)
+      g[f] = v;
+    else if (f < GL::DM)
+      E[((f - GL::E) / D) * L1 + (f - GL::E) % D] = v;
+    else
+      Dm[((f - GL::DM) / D) * L1 + (f - GL::DM) % D] = v;
+  }
+}
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_store_smo(const Team<TS>& tm, T* base, int64_t n, int64_t e, const T* g,
+                                            const T* E, const T* Dm) {
+  using GL = SmoLayout<D>;
+  constexpr int L1 = Ld<D>::v;
+  for (int f = tm.r; f < GL::NG; f += TS) {
+    T v;
+    if (f < GL::E)
+      v = g[f];
+    else if (f < GL::DM)
+      v = E[((f - GL::E) / D) * L1 + (f - GL::E) % D];
+    else
+      v = Dm[((f - GL::DM) / D) * L1 + (f - GL::DM) % D];
+    base[f * n + e] = v;
+  }
+}
+
+#define POF_TEAM_PROLOGUE(WS)                                             \
+  using B_ = TeamBlock<WS, TS>;                                           \
+  extern __shared__ __align__(16) unsigned char smem_raw_[];              \
+  const int team_in_block = threadIdx.x / TS;                             \
+  WS& w = reinterpret_cast<WS*>(smem_raw_)[team_in_block];               \
+  const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;     \
+  Team<TS> tm;
+
+// Filter up-sweep at level l >= 1: fold C consecutive elements per team.
+template <typename T, int D, int TS>
+__global__ void k_filt_reduce_team(const T* __restrict__ in, int64_t nin, int C, T* __restrict__ out, int64_t nout) {
+  using WS = FiltTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t >= nout) return;
+  const int64_t i0 = t * C;
+  const int64_t i1 = (i0 + C < nin) ? i0 + C : nin;
+  t_load_filt<T, TS, D>(tm, in, nin, i0, w.A1, w.b1, w.U1, w.e1, w.Z1);
+  for (int64_t i = i0 + 1; i < i1; ++i) {
+    t_load_filt<T, TS, D>(tm, in, nin, i, w.A2, w.b2, w.U2, w.e2, w.Z2);
+    tm.sync();
+    t_filt_combine<T, TS, D>(tm, w);
+  }
+  tm.sync();
+  t_store_filt<T, TS, D>(tm, out, nout, t, w.A1, w.b1, w.U1, w.e1, w.Z1);
+}
+
+// state before element i+1 from the state before element i (element 0 of a
+// level holds x0 and is absolute).
+template <typename T, int D, int TS>
+__device__ __forceinline__ void t_filt_advance(const Team<TS>& tm, FiltTeamWs<T, D>& w, const T* elems, int64_t n,
+                                               int64_t i) {
+  if (i == 0) {
+    T* scratch = w.M;  // A, eta, Z of element 0 are not needed
+    t_load_filt<T, TS, D>(tm, elems, n, 0, scratch, w.b1, w.U1, w.v1, scratch);
+    tm.sync();
+  } else {
+    t_load_filt<T, TS, D>(tm, elems, n, i, w.A2, w.b2, w.U2, w.e2, w.Z2);
+    tm.sync();
+    t_filt_apply<T, TS, D>(tm, w);
+  }
+}
+
+template <typename T, int D, int TS>
+__global__ void k_filt_down_team(const T* __restrict__ elems, int64_t n, int C, const T* __restrict__ states_up,
+                                 int64_t nup, T* __restrict__ states) {
+  using WS = FiltTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t >= nup) return;
+  const int64_t i0 = t * C;
+  const int64_t i1 = (i0 + C < n) ? i0 + C : n;
+  t_load_state<T, TS, D>(tm, states_up, nup, t, w.b1, w.U1);
+  tm.sync();
+  for (int64_t i = i0; i < i1; ++i) {
+    t_store_state<T, TS, D>(tm, states, n, i, w.b1, w.U1);
+    tm.sync();
+    if (i + 1 < i1) t_filt_advance<T, D, TS>(tm, w, elems, n, i);
+  }
+}
+
+template <typename T, int D, int TS>
+__global__ void k_filt_top_team(const T* __restrict__ elems, int64_t n, const T* __restrict__ x0m,
+                                const T* __restrict__ x0L, T* __restrict__ states) {
+  using WS = FiltTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t != 0) return;
+  t_load_state_plain<T, TS, D>(tm, x0m, x0L, w.b1, w.U1);
+  tm.sync();
+  for (int64_t i = 0; i < n; ++i) {
+    t_store_state<T, TS, D>(tm, states, n, i, w.b1, w.U1);
+    tm.sync();
+    if (i + 1 < n) t_filt_advance<T, D, TS>(tm, w, elems, n, i);
+  }
+}
+
+// Smoother up-sweep at level l >= 1.
+template <typename T, int D, int TS>
+__global__ void k_smo_reduce_team(const T* __restrict__ in, int64_t nin, int C, T* __restrict__ out, int64_t nout) {
+  using WS = SmoTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t >= nout) return;
+  const int64_t i0 = t * C;
+  const int64_t i1 = (i0 + C < nin) ? i0 + C : nin;
+  t_load_smo<T, TS, D>(tm, in, nin, i0, w.g2, w.E2, w.D2m);
+  for (int64_t i = i0 + 1; i < i1; ++i) {
+    t_load_smo<T, TS, D>(tm, in, nin, i, w.g1, w.E1, w.D1);
+    tm.sync();
+    t_smooth_combine<T, TS, D>(tm, w);
+  }
+  tm.sync();
+  t_store_smo<T, TS, D>(tm, out, nout, t, w.g2, w.E2, w.D2m);
+}
+
+template <typename T, int D, int TS>
+__global__ void k_smo_down_team(const T* __restrict__ elems, int64_t n, int C, const T* __restrict__ ends_up,
+                                int64_t nup, T* __restrict__ ends) {
+  using WS = SmoTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t >= nup) return;
+  const int64_t i0 = t * C;
+  const int64_t i1 = (i0 + C < n) ? i0 + C : n;
+  t_load_state<T, TS, D>(tm, ends_up, nup, t, w.g1, w.D1);
+  tm.sync();
+  for (int64_t i = i1 - 1; i >= i0; --i) {
+    t_store_state<T, TS, D>(tm, ends, n, i, w.g1, w.D1);
+    if (i > i0) {
+      t_load_smo<T, TS, D>(tm, elems, n, i, w.g2, w.E2, w.D2m);
+      tm.sync();
+      t_smooth_apply<T, TS, D>(tm, w);
+    }
+    tm.sync();
+  }
+}
+
+template <typename T, int D, int TS>
+__global__ void k_smo_top_team(const T* __restrict__ elems, int64_t n, const T* __restrict__ mT,
+                               const T* __restrict__ LT, T* __restrict__ ends) {
+  using WS = SmoTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t != 0) return;
+  t_load_state_plain<T, TS, D>(tm, mT, LT, w.g1, w.D1);
+  tm.sync();
+  for (int64_t i = n - 1; i >= 0; --i) {
+    t_store_state<T, TS, D>(tm, ends, n, i, w.g1, w.D1);
+    if (i > 0) {
+      t_load_smo<T, TS, D>(tm, elems, n, i, w.g2, w.E2, w.D2m);
+      tm.sync();
+      t_smooth_apply<T, TS, D>(tm, w);
+    }
+    tm.sync();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Level 0 with teams (large D, where per-thread state does not fit registers)
+// ---------------------------------------------------------------------------
+
+template <typename T, int D, int DY>
+struct L0TeamWs {
+  StepTeamWs<T, D, DY> s;
+  T QLi[D * Ld<D>::v];  // QL^{-1} (objective terms)
+  T mold[D], r[D];
+};
+
+template <typename T, int TS, int D, int DY>
+__device__ __forceinline__ void t_load_FQ(const Team<TS>& tm, StepTeamWs<T, D, DY>& w, const StepModel& sm,
+                                          int64_t s) {
+  constexpr int L1 = Ld<D>::v;
+  const T* F = static_cast<const T*>(sm.F) + s * sm.ft_stride;
+  const T* QL = static_cast<const T*>(sm.QL) + s * sm.ft_stride;
+  for (int f = tm.r; f < D * D; f += TS) {
+    w.F[(f / D) * L1 + f % D] = F[f];
+    w.QL[(f / D) * L1 + f % D] = QL[f];
+  }
+}
+
+// QL^{-1} by forward substitution on the identity (objective terms)
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_inv_lower(const Team<TS>& tm, const T* QL, T* QLi) {
+  constexpr int L1 = Ld<D>::v;
+  t_fill<T, TS, D, D, L1>(tm, QLi, T(0), T(1));
+  tm.sync();
+  t_trsm_l<T, TS, D, D, L1, L1>(tm, QL, QLi);
+  tm.sync();
+}
+
+// || QL^{-1} (a - F b) ||^2 with QLi = QL^{-1}; every lane gets the value.
+template <typename T, int TS, int D>
+__device__ __forceinline__ T t_objective(const Team<TS>& tm, const T* F, const T* QLi, const T* a, const T* b,
+                                         T* r) {
+  constexpr int L1 = Ld<D>::v;
+  for (int i = tm.r; i < D; i += TS) {
+    T s = a[i];
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(-F[i * L1 + k], b[k], s);
+    r[i] = s;
+  }
+  tm.sync();
+  T part = T(0);
+  for (int i = tm.r; i < D; i += TS) {
+    T s = T(0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(QLi[i * L1 + k], r[k], s);
+    part = fma(s, s, part);
+  }
+  const T tot = tm.sum(part);
+  tm.sync();
+  return tot;
+}
+
+#define POF_TEAM_PROLOGUE0(WS)                                            \
+  using B_ = TeamBlock<WS, TS>;                                           \
+  extern __shared__ __align__(16) unsigned char smem_raw_[];              \
+  const int team_in_block = threadIdx.x / TS;                             \
+  WS& ws_ = reinterpret_cast<WS*>(smem_raw_)[team_in_block];             \
+  const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;     \
+  Team<TS> tm;
+
+template <typename T, int D, int DY, int TS>
+__global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* __restrict__ x0m,
+                                      const T* __restrict__ x0L, T* __restrict__ out, int64_t n1) {
+  using WS = L0TeamWs<T, D, DY>;
+  POF_TEAM_PROLOGUE0(WS)
+  if (t >= n1) return;
+  StepTeamWs<T, D, DY>& w = ws_.s;
+  constexpr int L1 = Ld<D>::v;
+  const int64_t s0 = t * C0;
+  const int64_t s1 = (s0 + C0 < n) ? s0 + C0 : n;
+  t_load_FQ<T, TS, D, DY>(tm, w, sm, s0);
+  if (t == 0) {
+    t_load_state_plain<T, TS, D>(tm, x0m, x0L, w.m, w.L);
+    for (int64_t s = s0; s < s1; ++s) {
+      if (sm.ft_stride && s > s0) t_load_FQ<T, TS, D, DY>(tm, w, sm, s);
+      StepView<T, D, DY> v(sm, s);
+      t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
+      tm.sync();
+      t_kf_step<T, TS, D, DY, false>(tm, w);
+    }
+    t_fill<T, TS, D, D, L1>(tm, w.A, T(0), T(0));
+    t_fill<T, TS, D, D, L1>(tm, w.Z, T(0), T(0));
+    for (int i = tm.r; i < D; i += TS) w.eta[i] = T(0);
+    tm.sync();
+    t_store_filt<T, TS, D>(tm, out, n1, t, w.A, w.m, w.L, w.eta, w.Z);
+  } else {
+    t_fill<T, TS, D, D, L1>(tm, w.A, T(0), T(1));
+    t_fill<T, TS, D, D, L1>(tm, w.L, T(0), T(0));
+    t_fill<T, TS, D, D, L1>(tm, w.Z, T(0), T(0));
+    for (int i = tm.r; i < D; i += TS) {
+      w.b[i] = T(0);
+      w.eta[i] = T(0);
+    }
+    for (int64_t s = s0; s < s1; ++s) {
+      if (sm.ft_stride && s > s0) t_load_FQ<T, TS, D, DY>(tm, w, sm, s);
+      StepView<T, D, DY> v(sm, s);
+      t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
+      tm.sync();
+      t_cond_fold_step<T, TS, D, DY>(tm, w);
+    }
+    tm.sync();
+    t_store_filt<T, TS, D>(tm, out, n1, t, w.A, w.b, w.L, w.eta, w.Z);
+  }
+}
+
+template <typename T, int D, int DY, int TS>
+__global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __restrict__ states1, int64_t n1,
+                                    T* __restrict__ means, T* __restrict__ chols, T* __restrict__ selems,
+                                    double* __restrict__ partials) {
+  using WS = L0TeamWs<T, D, DY>;
+  POF_TEAM_PROLOGUE0(WS)
+  if (t >= n1) return;
+  StepTeamWs<T, D, DY>& w = ws_.s;
+  using GL = SmoLayout<D>;
+  constexpr int L1 = Ld<D>::v, L2 = Ld<2 * D>::v;
+  const int64_t s0 = t * C0;
+  const int64_t s1 = (s0 + C0 < n) ? s0 + C0 : n;
+  t_load_FQ<T, TS, D, DY>(tm, w, sm, s0);
+  t_load_state<T, TS, D>(tm, states1, n1, t, w.m, w.L);
+  tm.sync();
+  t_inv_lower<T, TS, D>(tm, w.QL, ws_.QLi);
+  if (t == 0) {
+    for (int f = tm.r; f < D + D * D; f += TS) {
+      if (f < D)
+        means[f] = w.m[f];
+      else
+        chols[f - D] = w.L[((f - D) / D) * L1 + (f - D) % D];
+    }
+  }
+  double ssq = 0.0, nll = 0.0, fobj = 0.0;
+  for (int64_t s = s0; s < s1; ++s) {
+    if (sm.ft_stride && s > s0) {
+      t_load_FQ<T, TS, D, DY>(tm, w, sm, s);
+      tm.sync();
+      t_inv_lower<T, TS, D>(tm, w.QL, ws_.QLi);
+    }
+    StepView<T, D, DY> v(sm, s);
+    t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
+    for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
+    tm.sync();
+    t_kf_step<T, TS, D, DY, true>(tm, w);
+    ssq += (double)w.sc[0];
+    nll += (double)w.sc[1];
+    fobj += (double)t_objective<T, TS, D>(tm, w.F, ws_.QLi, ws_.mold, w.m, ws_.r);
+    // smoother element of grid s: g, E (stored transposed in w.E), Dm = Y[:, D:]
+    for (int f = tm.r; f < GL::NG; f += TS) {
+      T val;
+      if (f < GL::E)
+        val = w.g[f];
+      else if (f < GL::DM)
+        val = w.E[((f - GL::E) % D) * L1 + (f - GL::E) / D];
+      else
+        val = w.Y[((f - GL::DM) / D) * L2 + D + (f - GL::DM) % D];
+      selems[f * n + s] = val;
+    }
+    for (int f = tm.r; f < D + D * D; f += TS) {
+      if (f < D)
+        means[(s + 1) * D + f] = w.m[f];
+      else
+        chols[(s + 1) * D * D + f - D] = w.L[((f - D) / D) * L1 + (f - D) % D];
+    }
+    tm.sync();
+  }
+  if (tm.r == 0) {
+    partials[P_SSQ * n1 + t] = ssq;
+    partials[P_NLL * n1 + t] = nll;
+    partials[P_FOBJ * n1 + t] = fobj;
+  }
+}
+
+template <typename T, int D>
+struct SmoL0TeamWs {
+  SmoTeamWs<T, D> s;
+  T F[D * Ld<D>::v], QL[D * Ld<D>::v], QLi[D * Ld<D>::v];
+  T mnext[D], r[D];
+};
+
+template <typename T, int D, int TS>
+__global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, const T* __restrict__ QL,
+                                   int64_t ft_stride, const T* __restrict__ selems, const T* __restrict__ ends1,
+                                   int64_t n1, T* __restrict__ means, T* __restrict__ chols,
+                                   const T* __restrict__ scale, const T* __restrict__ means_old,
+                                   double* __restrict__ partials) {
+  using WS = SmoL0TeamWs<T, D>;
+  POF_TEAM_PROLOGUE0(WS)
+  if (t >= n1) return;
+  SmoTeamWs<T, D>& w = ws_.s;
+  constexpr int L1 = Ld<D>::v;
+  const int64_t s0 = t * C0;
+  const int64_t s1 = (s0 + C0 < n) ? s0 + C0 : n;
+  const T sc = scale ? *scale : T(1);
+  auto load_FQ = [&](int64_t k) {
+    for (int f = tm.r; f < D * D; f += TS) {
+      ws_.F[(f / D) * L1 + f % D] = F[k * ft_stride + f];
+      ws_.QL[(f / D) * L1 + f % D] = QL[k * ft_stride + f];
+    }
+    tm.sync();
+    t_inv_lower<T, TS, D>(tm, ws_.QL, ws_.QLi);
+  };
+  load_FQ(s1 - 1);
+  t_load_state<T, TS, D>(tm, ends1, n1, t, w.g1, w.D1);
+  tm.sync();
+  double sobj = 0.0, notclose = 0.0;
+  auto close_count = [&](int64_t k) {
+    if (!means_old) return;
+    for (int i = tm.r; i < D; i += TS) {
+      const double a = (double)means_old[k * D + i], b = (double)w.g1[i];
+      bool ok;
+      if (isfinite(a) && isfinite(b))
+        ok = fabs(a - b) <= 1e-8 + 1e-13 * fabs(b);
+      else
+        ok = (a == b);
+      notclose += ok ? 0.0 : 1.0;
+    }
+  };
+  if (s1 == n) {
+    close_count(n);
+    if (scale)
+      for (int f = tm.r; f < D * D; f += TS) chols[n * D * D + f] = w.D1[(f / D) * L1 + f % D] * sc;
+  }
+  for (int64_t k = s1 - 1; k >= s0; --k) {
+    if (ft_stride && k < s1 - 1) load_FQ(k);
+    for (int i = tm.r; i < D; i += TS) ws_.mnext[i] = w.g1[i];
+    t_load_smo<T, TS, D>(tm, selems, n, k, w.g2, w.E2, w.D2m);
+    tm.sync();
+    t_smooth_apply<T, TS, D>(tm, w);
+    sobj += (double)t_objective<T, TS, D>(tm, ws_.F, ws_.QLi, w.g1, ws_.mnext, ws_.r);
+    close_count(k);
+    for (int f = tm.r; f < D + D * D; f += TS) {
+      if (f < D)
+        means[k * D + f] = w.g1[f];
+      else
+        chols[k * D * D + f - D] = w.D1[((f - D) / D) * L1 + (f - D) % D] * sc;
+    }
+    tm.sync();
+  }
+  notclose = (double)tm.sum(notclose);
+  if (tm.r == 0) {
+    partials[P_SOBJ * n1 + t] = sobj;
+    partials[P_NOTCLOSE * n1 + t] = notclose;
+  }
+}
+
+#undef POF_TEAM_PROLOGUE0
+#undef POF_TEAM_PROLOGUE
+
+}  // namespace pof

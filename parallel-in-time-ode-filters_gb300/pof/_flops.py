@@ -134,11 +134,18 @@ def kernel_flops(kind, n, D, d, C0, cnt):
     return 0
 
 
-def plan_levels(n, C0=None, Cg=8, top=8):
+def l0_lanes(D):
+    """Lanes per level-0 chunk (csrc/pof_plan.h l0_lanes)."""
+    return (16 if 2 * D <= 16 else 32) if D >= 6 else 1
+
+
+def plan_levels(n, D=4, C0=None, Cg=8, top=8):
     """The level sizes libpof uses (csrc/pof_plan.h make_plan)."""
     if C0 is None:
-        C0 = 4
-        while C0 < 64 and n // C0 > 16384:
+        lanes = l0_lanes(D)
+        C0 = 4 if lanes == 1 else 2
+        target = 16384 if lanes == 1 else max(1024, 65536 // lanes)
+        while C0 < 64 and n // C0 > target:
             C0 *= 2
     cnt = [None, (n + C0 - 1) // C0]
     while cnt[-1] > top:
@@ -148,7 +155,7 @@ def plan_levels(n, C0=None, Cg=8, top=8):
 
 def iteration_flops(n, D, d):
     """All kernels of one IEKS iteration (filter + smoother), by kind."""
-    C0, cnt = plan_levels(n)
+    C0, cnt = plan_levels(n, D)
     kinds = ["filt_l0_reduce", "filt_reduce", "filt_top", "filt_down", "filt_l0_down", "smo_l0_reduce",
              "smo_reduce", "smo_top", "smo_down", "smo_l0_down"]
     return {k: kernel_flops(k, n, D, d, C0, cnt) for k in kinds}

@@ -170,3 +170,20 @@ def test_scan_orders_agree():
     assert np.allclose(a, np.cumsum(x, 0)) and np.allclose(b, np.cumsum(x, 0))
     (r,) = scan.associative_scan(add, (x,), reverse=True)
     assert np.allclose(r, np.cumsum(x[::-1], 0)[::-1])
+
+
+@pytest.mark.parametrize("ivpf,N,q", [(lambda: oivp.fhn_classic(tmax=10.0), 200, 3), (oivp.lotkavolterra, 50, 1),
+                                      (oivp.rigid_body, 100, 2)])
+def test_sigma_squared_envelope_contains_reference_orders(ivpf, N, q):
+    """sigma^2 of d >= 2 problems differs between evaluation orders of the
+    reference's own arithmetic (whiten quirk); all of them lie in the sign
+    envelope that the GPU tests check against."""
+    from oracle.scan import sequential_scan
+
+    st, dtm, dom = _converged_problem(ivpf(), N, q, 30)
+    (fm, fL), _, _, t = ofs.linear_noiseless_filtering(st.x0, dtm, dom)
+    _, _, _, s = ofs.linear_noiseless_filtering(st.x0, dtm, dom, scan=sequential_scan)
+    _, _, _, b, _ = blocked.filter_blocked(st.x0, dtm, dom, C0=4, Cs=(8,) * 24)
+    lo, hi = ofs.sigma_squared_envelope(dtm, dom, fm, fL)
+    for v in (t, s, b):
+        assert lo * (1 - 1e-9) <= v <= hi * (1 + 1e-9)
