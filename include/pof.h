@@ -167,6 +167,31 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
                    void* chols, int64_t maxiters, int32_t calibrate, double* info, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* Scratch size of pof_linear_filtsmooth_noalloc (16 MiB per GPU). */
+#define POF_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+
+/* pof_linear_filtsmooth without a workspace argument.  It has no
+ * counterpart in the reference: it exists for callers that cannot allocate
+ * device memory -- code that runs while a CUDA graph is being captured,
+ * hosts whose device allocator belongs to someone else, real-time loops that
+ * forbid cudaMalloc after start-up -- and can only pass inputs and outputs.
+ * Arguments and results are those of pof_linear_filtsmooth.
+ *  - Scratch is a fixed 16 MiB device array inside libpof, held by every GPU
+ *    that loads the library until the process exits.  Problems whose
+ *    pof_filtsmooth_workspace_bytes exceeds POF_NOALLOC_SCRATCH_BYTES are
+ *    refused with POF_ERR_WORKSPACE before any GPU work (about 13k steps at
+ *    D = 8, d = 2 in float64).
+ *  - The first call on a device looks up the array's address on that device
+ *    (the current device); make that first call before any stream capture.
+ *  - Every call shares the array: calls whose work overlaps on the GPU
+ *    (other streams, other host threads) race and must be serialized by the
+ *    caller.  Nothing needs clearing between calls.
+ *  - It allocates no device memory. */
+int pof_linear_filtsmooth_noalloc(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, const void* x0_mean,
+                                  const void* x0_chol, const void* F, const void* QL, int64_t ft_stride,
+                                  const void* H, const void* c, const void* R, int64_t r_stride, void* out_mean,
+                                  void* out_chol, double* out_scalars, void* stream);
+
 /* Per-kernel timing.  When enabled, every libpof launch is bracketed by CUDA
  * events on its stream; pof_profile_read waits for them and returns the
  * summed milliseconds and launch counts per kernel kind (POF_PK_*), in

@@ -61,6 +61,10 @@ _SIGS = {
         _c.c_int,
         [_i32, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _dp, _vp, _sz, _vp],
     ),
+    "pof_linear_filtsmooth_noalloc": (
+        _c.c_int,
+        [_i32, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _dp, _vp],
+    ),
     "pof_smoothing": (_c.c_int, [_i32, _i64, _i32, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _dp, _vp, _sz, _vp]),
     "pof_linearize": (_c.c_int, [_i32, _i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp]),
     "pof_sequential_linear_filtsmooth": (
