@@ -307,6 +307,44 @@ def run_gpu(args, workload):
         ms = float(t.item())
     value = world * n / (ms * 1e-3)
 
+    # mixed precision (float32 iterations + float64 polish) on the same
+    # workload, timed the same way; error against the float64 result
+    mixed = None
+    if not args.no_mixed:
+        ref_means = means.clone()
+        mws_b = lib.pof_ieks_mixed_workspace_bytes(n, D, d)
+        mws = _lib.workspace(mws_b, dev)
+        minfo = torch.zeros(_lib.I_COUNT + 1, dtype=torch.float64, device=dev)
+
+        def solve_mixed():
+            means.copy_(means0)
+            rc = lib.pof_ieks_solve_mixed(n, D, d, _lib.FIELDS[fname], _lib.ptr(prm), float(setup["dt"]),
+                                          _lib.ptr(m0), _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means),
+                                          _lib.ptr(chols), MAXITERS, 1e-5, MAXITERS, 1, _lib.ptr(minfo),
+                                          _lib.ptr(mws), mws_b, _lib.stream_handle())
+            _lib.check(rc, "pof_ieks_solve_mixed")
+
+        for _ in range(args.warmup):
+            solve_mixed()
+        mtimes = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            solve_mixed()
+            e1.record()
+            e1.synchronize()
+            mtimes.append(e0.elapsed_time(e1))
+        mms = float(np.mean(mtimes))
+        E0 = setup["E0"]
+        ya, yb = means @ E0.T, ref_means @ E0.T
+        err = float(((ya - yb).abs().max() / yb.abs().max()).item())
+        mixed = {"value": world * n / (mms * 1e-3), "unit": "IVP*steps/s", "ms_per_step": mms,
+                 "iterations_float32": int(minfo[_lib.I_COUNT].item()),
+                 "iterations_float64": int(minfo[_lib.I_ITERATIONS].item()),
+                 "max_rel_err_vs_float64": err, "speedup_vs_float64": ms / mms}
+        del mws
+
     # per-kernel times of one more solve (profiler on; not part of the timing)
     _lib.profile_enable(True)
     _lib.profile_read(reset=True)
@@ -378,6 +416,8 @@ def run_gpu(args, workload):
         "reference_equivalent_gflops": _flops.reference_step_flops(D, d) * n * iterations / (ms * 1e-3) / 1e9,
         "clocks": clk.summary(),
     }
+    if mixed is not None:
+        out["mixed_precision"] = mixed
     if not args.no_cpu_baseline:
         EXPECTED_ITERATIONS[workload] = iterations
         cb = cpu_sample(workload, budget_s=20.0, iterations=iterations)
@@ -394,6 +434,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args, args.workload)

@@ -167,6 +167,30 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
                    void* chols, int64_t maxiters, int32_t calibrate, double* info, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
+
+/* pof.solver.solve with precision="mixed".  Float32 iterations first: each
+ * linearizes in float64 at the current float64 trajectory, row-normalizes the
+ * noiseless observation model (same constraint, smaller range), runs the
+ * filter and smoother in float32 and converts the means back; it is kept if
+ * finite.  The float32 phase ends when the largest change of the projected
+ * trajectory y = E0 m falls below rtol_f32 relative to max |y|, when that
+ * change failed to shrink eight times in a row, after a non-finite float32 iterate
+ * (discarded) or after maxiters_f32 iterations; a float32 phase whose
+ * smallest change never came within 100 rtol_f32 is dropped (float32 is too
+ * coarse for that problem) and the float64 loop starts from the input
+ * trajectory.  Otherwise the float64 loop of
+ * pof_ieks_solve runs from the last kept trajectory with the reference's
+ * criterion, so the result is a float64 IEKS fixed point.  No reference
+ * counterpart (the reference is float64 throughout).  All arrays float64 as
+ * in pof_ieks_solve; info has POF_I_COUNT + 1 entries, the last being the
+ * number of kept float32 iterations (POF_I_ITERATIONS counts the float64
+ * ones).  Waits on `stream` once per iteration. */
+int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, const double* params, double h,
+                         const double* x0_mean, const double* x0_chol, const double* F, const double* QL,
+                         double* means, double* chols, int64_t maxiters_f32, double rtol_f32, int64_t maxiters,
+                         int32_t calibrate, double* info, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Scratch size of pof_linear_filtsmooth_noalloc (16 MiB per GPU). */
 #define POF_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
 

@@ -33,14 +33,15 @@ const Ops* find_ops(int dtype, int D, int DY) {
 
 int esz(int dtype) { return dtype == POF_F32 ? 4 : 8; }
 
-// Optional overrides of the chunk sizes (tuning): POF_C0, POF_CG.
+// Optional overrides (tuning): POF_C0, POF_CG chunk sizes; POF_TEAM_WIDE_L0=1
+// runs level 0 with the wide team kernels.
 int env_int(const char* name) {
   const char* v = getenv(name);
   return v ? atoi(v) : 0;
 }
 
 Plan plan_for(int dtype, int64_t n, int D, int DY, bool solver) {
-  return make_plan(n, D, DY, esz(dtype), solver, env_int("POF_C0"), env_int("POF_CG"));
+  return make_plan(n, D, DY, esz(dtype), solver, env_int("POF_C0"), env_int("POF_CG"), env_int("POF_TEAM_WIDE_L0") != 0);
 }
 
 int check_common(int dtype, int64_t n, int D, int DY, const Ops** ops) {
@@ -340,6 +341,163 @@ int pof_sequential_eks(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int
   return launch_status();
 }
 
+}  // extern "C"
+
+namespace {
+
+__global__ void k_d2f(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+__global__ void k_f2d(const float* __restrict__ in, double* __restrict__ out, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+
+struct Loop {
+  const Ops* ops;
+  const Plan* p;
+  char* w;           // aligned workspace of this plan
+  int field;
+  const void* params;
+  double p0, p1;
+  const void* x0m;
+  const void* x0L;
+  const void* F;
+  const void* QL;
+  void* means;       // in: initial trajectory, out: result
+  void* chols;
+  size_t esz;
+  int64_t maxiters;
+  bool calibrate;
+  double rtol, atol;  // objective test of crit
+};
+
+// The IEKS loop of pof/solver.py:36-57 on the device (one host read of the
+// loop condition per iteration).  Leaves the result in l.means and the
+// scalars (nll, obj, ssq, iterations) in the plan's scalar block.
+int ieks_loop(const Loop& l, cudaStream_t st) {
+  const Plan& p = *l.p;
+  char* w = l.w;
+  double* scal = reinterpret_cast<double*>(w + p.scalars);
+  void* Hb = w + p.H;
+  void* cb = w + p.c;
+  void* bufs[2] = {l.means, w + p.means2};
+  k_init_scalars<<<1, 32, 0, st>>>(scal);
+  StepModel sm{l.F, l.QL, 0, Hb, cb, nullptr, 0};
+  int cur = 0;  // bufs[cur] holds the current states
+  for (;;) {
+    void* mold = bufs[cur];
+    void* mnew = bufs[cur ^ 1];
+    l.ops->linearize(p.n, l.field, l.params, l.p0, l.p1, mold, Hb, cb, st);
+    l.ops->filter(p, w, sm, l.x0m, l.x0L, mnew, l.chols, st);
+    l.ops->smoother(p, w, l.F, l.QL, 0, mnew, l.chols, l.calibrate, mold, st);
+    {
+      ProfScope ps(PK_CONTROL, st);
+      k_ieks_control<<<1, 32, 0, st>>>(scal, l.maxiters, l.rtol, l.atol);
+    }
+    int rc = launch_status();
+    if (rc) return rc;
+    cur ^= 1;
+    double cont = 0.0;
+    cudaError_t e = cudaMemcpyAsync(&cont, scal + S_CONT, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (g_prof.on) prof_collect();
+    if (cont == 0.0) break;
+  }
+  if (bufs[cur] != l.means) {
+    cudaError_t e = cudaMemcpyAsync(l.means, bufs[cur], l.esz * p.D * (p.n + 1), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  return POF_OK;
+}
+
+// Workspace of the mixed-precision solve: the float64 solver plan, the
+// float32 filter/smoother plan, float copies of the problem, and a float64
+// candidate trajectory.
+struct MixedLayout {
+  Plan p64, p32;
+  size_t off32, fmeans, fchols, fx0m, fx0L, fF, fQL, fH, fc, cand, keep, red, total;
+};
+
+MixedLayout mixed_layout(int64_t n, int D, int d) {
+  MixedLayout m;
+  m.p64 = plan_for(POF_F64, n, D, d, true);
+  m.p32 = plan_for(POF_F32, n, D, d, false);
+  size_t off = align_up(m.p64.total);
+  m.off32 = off;
+  off = align_up(off + m.p32.total);
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes);
+    return o;
+  };
+  m.fmeans = take(sizeof(float) * D * (n + 1));
+  m.fchols = take(sizeof(float) * D * D * (n + 1));
+  m.fx0m = take(sizeof(float) * D);
+  m.fx0L = take(sizeof(float) * D * D);
+  m.fF = take(sizeof(float) * D * D);
+  m.fQL = take(sizeof(float) * D * D);
+  m.fH = take(sizeof(float) * d * D * n);
+  m.fc = take(sizeof(float) * d * n);
+  m.cand = take(sizeof(double) * D * (n + 1));
+  m.keep = take(sizeof(double) * D * (n + 1));
+  m.red = take(sizeof(unsigned long long) * 4);
+  m.total = off + 256;
+  return m;
+}
+
+// Rows of a noiseless observation model can be scaled freely (0 = H x + c
+// is the same constraint as 0 = (H x + c) / s): normalize each row of
+// (H, c) and convert to float32, which keeps the float32 filter clear of the
+// huge Jacobians of early IEKS iterates.
+__global__ void k_rows_to_f32(const double* __restrict__ H, const double* __restrict__ c, float* __restrict__ Hf,
+                              float* __restrict__ cf, int64_t rows, int D) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  double s = 0.0;
+  for (int k = 0; k < D; ++k) s = fma(H[r * D + k], H[r * D + k], s);
+  const double inv = s > 0.0 ? 1.0 / sqrt(s) : 1.0;
+  for (int k = 0; k < D; ++k) Hf[r * D + k] = (float)(H[r * D + k] * inv);
+  cf[r] = (float)(c[r] * inv);
+}
+
+// max |y_new - y_old|, max |y_old| over the projected states y = p0 m[i(q+1)]
+// (bit patterns of non-negative doubles order like the values, so atomicMax
+// on them is exact and order-independent), and a non-finite flag.
+__global__ void k_ychange(const double* __restrict__ mnew, const double* __restrict__ mold, int64_t N, int D, int d,
+                          double p0, unsigned long long* __restrict__ red) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int Q1 = D / d;
+  double dy = 0.0, ay = 0.0;
+  bool bad = false;
+  if (idx < N * d) {
+    const int64_t k = idx / d;
+    const int i = (int)(idx % d);
+    const double a = mnew[k * D + i * Q1], b = mold[k * D + i * Q1];
+    bad = !isfinite(a);
+    dy = fabs(p0 * (a - b));
+    ay = fabs(p0 * b);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    dy = fmax(dy, __shfl_xor_sync(0xffffffffu, dy, o));
+    ay = fmax(ay, __shfl_xor_sync(0xffffffffu, ay, o));
+    bad = bad || __shfl_xor_sync(0xffffffffu, (int)bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicOr(&red[2], 1ull);
+    if (isfinite(dy)) atomicMax(&red[0], (unsigned long long)__double_as_longlong(dy));
+    if (isfinite(ay)) atomicMax(&red[1], (unsigned long long)__double_as_longlong(ay));
+  }
+}
+
+unsigned g1d(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+}  // namespace
+
+extern "C" {
+
 int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field, const void* params,
                    double h, const void* x0_mean, const void* x0_chol, const void* F, const void* QL, void* means,
                    void* chols, int64_t maxiters, int32_t calibrate, double* info, void* workspace,
@@ -357,40 +515,121 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
   if (rc) return rc;
   char* w = aligned_ws(workspace);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const size_t es = esz(dtype);
-  double* scal = reinterpret_cast<double*>(w + p.scalars);
-  void* Hb = w + p.H;
-  void* cb = w + p.c;
-  void* bufs[2] = {means, w + p.means2};
-  k_init_scalars<<<1, 32, 0, st>>>(scal);
-  StepModel sm{F, QL, 0, Hb, cb, nullptr, 0};
-  int cur = 0;  // bufs[cur] holds the current states
-  for (;;) {
-    void* mold = bufs[cur];
-    void* mnew = bufs[cur ^ 1];
-    ops->linearize(n_steps, field, params, p0, p1, mold, Hb, cb, st);
-    ops->filter(p, w, sm, x0_mean, x0_chol, mnew, chols, st);
-    ops->smoother(p, w, F, QL, 0, mnew, chols, calibrate != 0, mold, st);
-    {
-      ProfScope ps(PK_CONTROL, st);
-      k_ieks_control<<<1, 32, 0, st>>>(scal, maxiters);
-    }
+  Loop l{ops, &p, w, field, params, p0, p1, x0_mean, x0_chol, F, QL, means, chols, (size_t)esz(dtype),
+         maxiters, calibrate != 0, 1e-6, 1e-9};
+  rc = ieks_loop(l, st);
+  if (rc) return rc;
+  if (calibrate) ops->scale_inplace(chols, (int64_t)D * D * (n_steps + 1), w + p.scale, st);
+  if (info) k_copy_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(w + p.scalars), info, 1);
+  return launch_status();
+}
+
+size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d) {
+  if (n_steps < 1 || D < 1) return 0;
+  return mixed_layout(n_steps, D, d).total;
+}
+
+int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, const double* params, double h,
+                         const double* x0_mean, const double* x0_chol, const double* F, const double* QL,
+                         double* means, double* chols, int64_t maxiters_f32, double rtol_f32, int64_t maxiters,
+                         int32_t calibrate, double* info, void* workspace, size_t workspace_bytes, void* stream) {
+  const Ops* ops64 = nullptr;
+  const Ops* ops32 = nullptr;
+  int rc = check_common(POF_F64, n_steps, D, d, &ops64);
+  if (rc) return rc;
+  rc = check_common(POF_F32, n_steps, D, d, &ops32);
+  if (rc) return rc;
+  if (field <= 0 || field >= FIELD_COUNT || field_dim(field) != d) return POF_ERR_FIELD;
+  if (!params || !x0_mean || !x0_chol || !F || !QL || !means || !chols || !workspace || maxiters < 0 ||
+      maxiters_f32 < 0 || !(rtol_f32 > 0))
+    return POF_ERR_ARG;
+  MixedLayout m = mixed_layout(n_steps, D, d);
+  if (workspace_bytes < m.total) return POF_ERR_WORKSPACE;
+  double p0, p1;
+  rc = nordsieck_p01(D, d, h, &p0, &p1);
+  if (rc) return rc;
+  char* w = aligned_ws(workspace);
+  char* w32 = w + m.off32;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int64_t N = n_steps + 1;
+  const int64_t NM = (int64_t)D * N;
+  float* fm = reinterpret_cast<float*>(w + m.fmeans);
+  float* fL = reinterpret_cast<float*>(w + m.fchols);
+  float* fx0m = reinterpret_cast<float*>(w + m.fx0m);
+  float* fx0L = reinterpret_cast<float*>(w + m.fx0L);
+  float* fF = reinterpret_cast<float*>(w + m.fF);
+  float* fQL = reinterpret_cast<float*>(w + m.fQL);
+  float* fH = reinterpret_cast<float*>(w + m.fH);
+  float* fc = reinterpret_cast<float*>(w + m.fc);
+  double* cand = reinterpret_cast<double*>(w + m.cand);
+  double* keep = reinterpret_cast<double*>(w + m.keep);
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(w + m.red);
+  double* H64 = reinterpret_cast<double*>(w + m.p64.H);
+  double* c64 = reinterpret_cast<double*>(w + m.p64.c);
+  k_d2f<<<1, 256, 0, st>>>(x0_mean, fx0m, D);
+  k_d2f<<<g1d(D * D), 256, 0, st>>>(x0_chol, fx0L, D * D);
+  k_d2f<<<g1d(D * D), 256, 0, st>>>(F, fF, D * D);
+  k_d2f<<<g1d(D * D), 256, 0, st>>>(QL, fQL, D * D);
+  k_init_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(w32 + m.p32.scalars));
+  StepModel sm32{fF, fQL, 0, fH, fc, nullptr, 0};
+  // float32 phase: linearize in float64, filter/smooth in float32, judge the
+  // step in float64
+  int64_t it32 = 0;
+  double prev = 1e300, best = 1e300;
+  int worse = 0;
+  {
+    cudaError_t e = cudaMemcpyAsync(keep, means, sizeof(double) * NM, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  while (it32 < maxiters_f32) {
+    ops64->linearize(n_steps, field, params, p0, p1, means, H64, c64, st);
+    k_rows_to_f32<<<g1d(n_steps * d), 256, 0, st>>>(H64, c64, fH, fc, n_steps * d, D);
+    ops32->filter(m.p32, w32, sm32, fx0m, fx0L, fm, fL, st);
+    ops32->smoother(m.p32, w32, fF, fQL, 0, fm, fL, false, nullptr, st);
+    k_f2d<<<g1d(NM), 256, 0, st>>>(fm, cand, NM);
+    cudaError_t e = cudaMemsetAsync(red, 0, sizeof(unsigned long long) * 4, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    k_ychange<<<g1d(N * d), 256, 0, st>>>(cand, means, N, D, d, p0, red);
     rc = launch_status();
     if (rc) return rc;
-    cur ^= 1;
-    double cont = 0.0;
-    cudaError_t e = cudaMemcpyAsync(&cont, scal + S_CONT, sizeof(double), cudaMemcpyDeviceToHost, st);
+    unsigned long long hred[3];
+    e = cudaMemcpyAsync(hred, red, sizeof(hred), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_status(e);
-    if (g_prof.on) prof_collect();
-    if (cont == 0.0) break;
+    double dy, ay;
+    memcpy(&dy, &hred[0], sizeof(double));
+    memcpy(&ay, &hred[1], sizeof(double));
+    if (hred[2] != 0) break;  // non-finite float32 iterate: keep the last float64 one
+    ++it32;
+    e = cudaMemcpyAsync(means, cand, sizeof(double) * NM, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    const double rel = ay > 0.0 ? dy / ay : dy;
+    best = rel < best ? rel : best;
+    if (rel < rtol_f32) break;       // converged as far as float32 goes
+    worse = rel >= prev ? worse + 1 : 0;
+    if (worse >= 8) break;           // float32 stopped helping
+    prev = rel;
   }
-  if (bufs[cur] != means) {
-    cudaError_t e = cudaMemcpyAsync(means, bufs[cur], es * D * (n_steps + 1), cudaMemcpyDeviceToDevice, st);
+  // a float32 phase that never came near convergence (an ill-conditioned
+  // smoother in float32) is discarded: the polish starts from the input
+  if (it32 > 0 && !(best < 100.0 * rtol_f32)) {
+    cudaError_t e = cudaMemcpyAsync(means, keep, sizeof(double) * NM, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    it32 = 0;
+  }
+  // float64 polish: the reference loop from the last accepted trajectory
+  Loop l64{ops64, &m.p64, w, field, params, p0, p1, x0_mean, x0_chol, F, QL, means, chols, sizeof(double),
+           maxiters, calibrate != 0, 1e-6, 1e-9};
+  rc = ieks_loop(l64, st);
+  if (rc) return rc;
+  if (calibrate) ops64->scale_inplace(chols, (int64_t)D * D * N, w + m.p64.scale, st);
+  if (info) {
+    k_copy_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(w + m.p64.scalars), info, 1);
+    const double it = (double)it32;
+    cudaError_t e = cudaMemcpyAsync(info + POF_I_COUNT, &it, sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_status(e);
   }
-  if (calibrate) ops->scale_inplace(chols, (int64_t)D * D * (n_steps + 1), w + p.scale, st);
-  if (info) k_copy_scalars<<<1, 32, 0, st>>>(scal, info, 1);
   return launch_status();
 }
 

@@ -42,9 +42,11 @@ static __global__ void k_finalize_smoother(const double* __restrict__ partials, 
 }
 
 // Loop control of pof/solver.py:36-57 after one more ieks_step:
-// crit (pof/convergence_criteria.py:4-13) with rtol = 1e-6, atol = 1e-9 on
-// the objective and isclose(rtol = 1e-13, atol = 1e-8) on every mean.
-static __global__ void k_ieks_control(double* __restrict__ scalars, int64_t maxiters) {
+// crit (pof/convergence_criteria.py:4-13): stop on NaN, on
+// isclose(obj_old, obj, rtol, atol) or when every mean is
+// isclose(old, new, mrtol, matol); the reference's values are rtol = 1e-6,
+// atol = 1e-9, mrtol = 1e-13, matol = 1e-8.
+static __global__ void k_ieks_control(double* __restrict__ scalars, int64_t maxiters, double rtol, double atol) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const double k = scalars[S_ITER] + 1.0;
   scalars[S_ITER] = k;
@@ -53,7 +55,7 @@ static __global__ void k_ieks_control(double* __restrict__ scalars, int64_t maxi
   const bool nan = isnan(obj) || isnan(nll);
   bool objc;
   if (isfinite(oo) && isfinite(obj))
-    objc = fabs(oo - obj) <= 1e-9 + 1e-6 * fabs(obj);
+    objc = fabs(oo - obj) <= atol + rtol * fabs(obj);
   else
     objc = (oo == obj);
   const bool meansc = scalars[S_NOTCLOSE] == 0.0;
@@ -116,12 +118,28 @@ inline void launch_team(void (*kern)(KArgs...), int64_t nteams, cudaStream_t st,
 template <typename T, int D, int DY>
 struct Driver {
   static constexpr int kBlock = 64;
-  static constexpr int TS = TeamSize<D>::v;
+  static constexpr int TSW = TeamSize<D>::v;                     // wide teams
+  static constexpr int TSN = TSW / 2 >= 4 ? TSW / 2 : 4;          // narrow teams
   static constexpr bool kTeamL0 = D >= 6;  // pof_plan.h l0_lanes
   using FWS = FiltTeamWs<T, D>;
   using SWS = SmoTeamWs<T, D>;
   using L0WS = L0TeamWs<T, D, DY>;
   using SL0WS = SmoL0TeamWs<T, D>;
+
+  static void filter(const Plan& p, char* ws, const StepModel& sm, const T* x0m, const T* x0L, T* means, T* chols,
+                     cudaStream_t st) {
+    if (p.team == TSN && TSN != TSW)
+      filter_ts<TSN, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
+    else
+      filter_ts<TSW, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
+  }
+  static void smoother(const Plan& p, char* ws, const T* F, const T* QL, int64_t ft_stride, T* means, T* chols,
+                       bool calibrate, const T* means_old, cudaStream_t st) {
+    if (p.team == TSN && TSN != TSW)
+      smoother_ts<TSN, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);
+    else
+      smoother_ts<TSW, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);
+  }
 
   struct Bufs {
     char* ws;
@@ -134,8 +152,9 @@ struct Driver {
 
   // Filter (phases 1-3) then finalize.  Leaves filtered states in means/chols
   // and the smoother elements in the workspace.
-  static void filter(const Plan& p, char* ws, const StepModel& sm, const T* x0m, const T* x0L, T* means, T* chols,
-                     cudaStream_t st) {
+  template <int TS, int TU>
+  static void filter_ts(const Plan& p, char* ws, const StepModel& sm, const T* x0m, const T* x0L, T* means,
+                        T* chols, cudaStream_t st) {
     Bufs b{ws, &p};
     const int64_t n = p.n;
     const int64_t n1 = p.cnt[1];
@@ -150,17 +169,17 @@ struct Driver {
     }
     for (int l = 1; l < p.nlev; ++l) {
       ProfScope ps(PK_FILT_REDUCE, st);
-      launch_team<FWS, TS>(k_filt_reduce_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
+      launch_team<FWS, TU>(k_filt_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
                            p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
     }
     {
       ProfScope ps(PK_FILT_TOP, st);
-      launch_team<FWS, TS>(k_filt_top_team<T, D, TS>, 1, st, (const T*)b.template at<T>(p.felem[p.nlev]),
+      launch_team<FWS, TU>(k_filt_top_team<T, D, TU>, 1, st, (const T*)b.template at<T>(p.felem[p.nlev]),
                            p.cnt[p.nlev], x0m, x0L, b.template at<T>(p.fstate[p.nlev]));
     }
     for (int l = p.nlev - 1; l >= 1; --l) {
       ProfScope ps(PK_FILT_DOWN, st);
-      launch_team<FWS, TS>(k_filt_down_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
+      launch_team<FWS, TU>(k_filt_down_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
                            p.cnt[l], p.Cg, (const T*)b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
                            b.template at<T>(p.fstate[l]));
     }
@@ -184,8 +203,9 @@ struct Driver {
 
   // Smoother from the elements left by filter() (or by k_smo_elements) and
   // the terminal state in means/chols[n].
-  static void smoother(const Plan& p, char* ws, const T* F, const T* QL, int64_t ft_stride, T* means, T* chols,
-                       bool calibrate, const T* means_old, cudaStream_t st) {
+  template <int TS, int TU>
+  static void smoother_ts(const Plan& p, char* ws, const T* F, const T* QL, int64_t ft_stride, T* means, T* chols,
+                          bool calibrate, const T* means_old, cudaStream_t st) {
     Bufs b{ws, &p};
     const int64_t n = p.n;
     const int64_t n1 = p.cnt[1];
@@ -200,18 +220,18 @@ struct Driver {
     }
     for (int l = 1; l < p.nlev; ++l) {
       ProfScope ps(PK_SMO_REDUCE, st);
-      launch_team<SWS, TS>(k_smo_reduce_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
+      launch_team<SWS, TU>(k_smo_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
                            p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
     }
     {
       ProfScope ps(PK_SMO_TOP, st);
-      launch_team<SWS, TS>(k_smo_top_team<T, D, TS>, 1, st, (const T*)b.template at<T>(p.gelem[p.nlev]),
+      launch_team<SWS, TU>(k_smo_top_team<T, D, TU>, 1, st, (const T*)b.template at<T>(p.gelem[p.nlev]),
                            p.cnt[p.nlev], (const T*)(means + n * D), (const T*)(chols + n * D * D),
                            b.template at<T>(p.gend[p.nlev]));
     }
     for (int l = p.nlev - 1; l >= 1; --l) {
       ProfScope ps(PK_SMO_DOWN, st);
-      launch_team<SWS, TS>(k_smo_down_team<T, D, TS>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
+      launch_team<SWS, TU>(k_smo_down_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
                            p.cnt[l], p.Cg, (const T*)b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
                            b.template at<T>(p.gend[l]));
     }
@@ -221,11 +241,11 @@ struct Driver {
       if constexpr (kTeamL0)
         launch_team<SL0WS, TS>(k_smo_l0_down_team<T, D, TS>, n1, st, n, p.C0, F, QL, ft_stride,
                                (const T*)b.template at<T>(p.selem), (const T*)b.template at<T>(p.gend[1]), n1,
-                               means, chols, scl, means_old, b.template at<double>(p.partials));
+                               means, chols, scl, means_old, p.mrtol, p.matol, b.template at<double>(p.partials));
       else
         k_smo_l0_down<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
             n, p.C0, F, QL, ft_stride, b.template at<T>(p.selem), b.template at<T>(p.gend[1]), n1, means, chols,
-            scl, means_old, b.template at<double>(p.partials));
+            scl, means_old, p.mrtol, p.matol, b.template at<double>(p.partials));
     }
     {
       ProfScope ps(PK_SMO_FINALIZE, st);

@@ -38,6 +38,22 @@ __host__ __device__ inline int field_dim(int id) {
   }
 }
 
+__host__ __device__ inline int field_nparams(int id) {
+  switch (id) {
+    case FIELD_LOGISTIC:
+    case FIELD_VANDERPOL:
+    case FIELD_THREEBODY:
+    case FIELD_HENONHEILES: return 1;
+    case FIELD_FHN_CLASSIC:
+    case FIELD_ROBER:
+    case FIELD_RIGID_BODY: return 3;
+    case FIELD_LOTKAVOLTERRA:
+    case FIELD_FITZHUGHNAGUMO:
+    case FIELD_SEIR: return 4;
+    default: return 0;
+  }
+}
+
 // f(y) and J = df/dy (row-major DY x DY) of field `id` with parameters p.
 template <typename T, int DY>
 __device__ __forceinline__ void field_eval(int id, const T* __restrict__ p, const T* __restrict__ y, T* f, T* J) {

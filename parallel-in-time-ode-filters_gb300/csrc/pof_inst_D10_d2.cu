@@ -1,10 +1,10 @@
-// float64 kernels for D = 10, d = 2 (one translation unit per shape so the
+// float64 and float32 kernels for D = 10, d = 2 (one translation unit per shape so the
 // build compiles shapes in parallel).
 #include "pof_table.cuh"
 
 namespace pof {
 template <>
 const Ops* ops_shape<10, 2>(int dtype) {
-  return dtype == 0 ? OpsImpl<double, 10, 2>::get() : nullptr;
+  return dtype == 0 ? OpsImpl<double, 10, 2>::get() : OpsImpl<float, 10, 2>::get();
 }
 }  // namespace pof

@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(64) k_smo_l0_down(int64_t n, int C0, const T* 
                                                     const T* __restrict__ selems, const T* __restrict__ ends1,
                                                     int64_t n1, T* __restrict__ means, T* __restrict__ chols,
                                                     const T* __restrict__ scale, const T* __restrict__ means_old,
-                                                    double* __restrict__ partials) {
+                                                    double c_mrtol, double c_matol, double* __restrict__ partials) {
   using SL = StateLayout<D>;
   using GL = SmoLayout<D>;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(64) k_smo_l0_down(int64_t n, int C0, const T* 
       const double a = (double)means_old[k * D + i], b = (double)mk[i];
       bool ok;
       if (isfinite(a) && isfinite(b))
-        ok = fabs(a - b) <= 1e-8 + 1e-13 * fabs(b);
+        ok = fabs(a - b) <= c_matol + c_mrtol * fabs(b);
       else
         ok = (a == b);
       notclose += ok ? 0.0 : 1.0;

@@ -78,25 +78,32 @@ __device__ __forceinline__ void t_mv(const Team<TS>& tm, const T* A, const T* x,
 // lane.  Zeroes X's tails at the end.
 template <typename T, int TS, int M, int MB, int NC, int LD, int LDY>
 __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y) {
-  static_assert(M + MB <= 2 * TS || true, "");
+  const int src = (threadIdx.x & 31) / TS * TS;  // lane 0 of this team within the warp
 #pragma unroll 1
   for (int j = 0; j < M; ++j) {
     T* xj = X + j * LD;
     tm.sync();
-    // ||x[j, j+1:]||^2 across lanes (columns), alpha from column j
+    // ||x[j, j+1:]||^2: column partials, reduced across the team
     T part = T(0);
     for (int k = j + 1 + tm.r; k < NC; k += TS) part = fma(xj[k], xj[k], part);
     const T xn2 = tm.sum(part);
-    const T alpha = xj[j];
-    const bool zero = (xn2 == T(0));
-    const T nrm = sqrt(fma(alpha, alpha, xn2));
-    const T beta = zero ? alpha : (alpha >= T(0) ? -nrm : nrm);
-    const T tau = zero ? T(0) : (beta - alpha) / beta;
-    const T scal = zero ? T(0) : T(1) / (alpha - beta);
+    // the reflector's scalars on one lane (a square root and two divisions
+    // are long FP64 sequences), then broadcast
+    T tau = T(0), scal = T(0), beta = T(0);
+    if (tm.r == 0) {
+      const T alpha = xj[j];
+      const bool zero = (xn2 == T(0));
+      const T nrm = sqrt(fma(alpha, alpha, xn2));
+      beta = zero ? alpha : (alpha >= T(0) ? -nrm : nrm);
+      tau = zero ? T(0) : (beta - alpha) / beta;
+      scal = zero ? T(0) : T(1) / (alpha - beta);
+    }
+    tau = __shfl_sync(tm.mask, tau, src);
+    scal = __shfl_sync(tm.mask, scal, src);
     tm.sync();
     for (int k = j + 1 + tm.r; k < NC; k += TS) xj[k] *= scal;
-    tm.sync();
     if (tm.r == 0) xj[j] = beta;
+    tm.sync();
     // rows below j (X rows j+1..M-1, then Y rows 0..MB-1): one row per lane
     for (int rr = tm.r; rr < (M - j - 1) + MB; rr += TS) {
       T* xi = (rr < M - j - 1) ? X + (j + 1 + rr) * LD : Y + (rr - (M - j - 1)) * LDY;
@@ -115,16 +122,42 @@ __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y) {
   tm.sync();
 }
 
+// 1 / L_ii for i = 0..M-1, computed in parallel (lane i) and read by every
+// lane through a shuffle: each division is done once per team, not once per
+// right-hand side.
+template <typename T, int TS, int M, int LDL>
+__device__ __forceinline__ T t_recip_diag(const Team<TS>& tm, const T* L) {
+  static_assert(M <= TS, "t_recip_diag needs M <= TS");
+  return (tm.r < M) ? T(1) / L[tm.r * LDL + tm.r] : T(0);
+}
+
 // B(M x NR) <- L^{-1} B (lower L): one right-hand-side column per lane.
 template <typename T, int TS, int M, int NR, int LDL, int LDB>
 __device__ __forceinline__ void t_trsm_l(const Team<TS>& tm, const T* L, T* B) {
-  for (int j = tm.r; j < NR; j += TS) {
+  if constexpr (M <= TS) {
+    const int src = (threadIdx.x & 31) / TS * TS;
+    const T rd = t_recip_diag<T, TS, M, LDL>(tm, L);
+    T rdi[M];
 #pragma unroll
-    for (int i = 0; i < M; ++i) {
-      T s = B[i * LDB + j];
+    for (int i = 0; i < M; ++i) rdi[i] = __shfl_sync(tm.mask, rd, src + i);
+    for (int j = tm.r; j < NR; j += TS) {
 #pragma unroll
-      for (int k = 0; k < i; ++k) s = fma(-L[i * LDL + k], B[k * LDB + j], s);
-      B[i * LDB + j] = s / L[i * LDL + i];
+      for (int i = 0; i < M; ++i) {
+        T s = B[i * LDB + j];
+#pragma unroll
+        for (int k = 0; k < i; ++k) s = fma(-L[i * LDL + k], B[k * LDB + j], s);
+        B[i * LDB + j] = s * rdi[i];
+      }
+    }
+  } else {
+    for (int j = tm.r; j < NR; j += TS) {
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        T s = B[i * LDB + j];
+#pragma unroll
+        for (int k = 0; k < i; ++k) s = fma(-L[i * LDL + k], B[k * LDB + j], s);
+        B[i * LDB + j] = s / L[i * LDL + i];
+      }
     }
   }
 }
@@ -132,13 +165,30 @@ __device__ __forceinline__ void t_trsm_l(const Team<TS>& tm, const T* L, T* B) {
 // B(M x NR) <- L^{-T} B
 template <typename T, int TS, int M, int NR, int LDL, int LDB>
 __device__ __forceinline__ void t_trsm_lt(const Team<TS>& tm, const T* L, T* B) {
-  for (int j = tm.r; j < NR; j += TS) {
+  if constexpr (M <= TS) {
+    const int src = (threadIdx.x & 31) / TS * TS;
+    const T rd = t_recip_diag<T, TS, M, LDL>(tm, L);
+    T rdi[M];
 #pragma unroll
-    for (int i = M - 1; i >= 0; --i) {
-      T s = B[i * LDB + j];
+    for (int i = 0; i < M; ++i) rdi[i] = __shfl_sync(tm.mask, rd, src + i);
+    for (int j = tm.r; j < NR; j += TS) {
 #pragma unroll
-      for (int k = i + 1; k < M; ++k) s = fma(-L[k * LDL + i], B[k * LDB + j], s);
-      B[i * LDB + j] = s / L[i * LDL + i];
+      for (int i = M - 1; i >= 0; --i) {
+        T s = B[i * LDB + j];
+#pragma unroll
+        for (int k = i + 1; k < M; ++k) s = fma(-L[k * LDL + i], B[k * LDB + j], s);
+        B[i * LDB + j] = s * rdi[i];
+      }
+    }
+  } else {
+    for (int j = tm.r; j < NR; j += TS) {
+#pragma unroll
+      for (int i = M - 1; i >= 0; --i) {
+        T s = B[i * LDB + j];
+#pragma unroll
+        for (int k = i + 1; k < M; ++k) s = fma(-L[k * LDL + i], B[k * LDB + j], s);
+        B[i * LDB + j] = s / L[i * LDL + i];
+      }
     }
   }
 }

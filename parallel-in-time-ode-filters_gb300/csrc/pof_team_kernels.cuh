@@ -444,8 +444,8 @@ template <typename T, int D, int TS>
 __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, const T* __restrict__ QL,
                                    int64_t ft_stride, const T* __restrict__ selems, const T* __restrict__ ends1,
                                    int64_t n1, T* __restrict__ means, T* __restrict__ chols,
-                                   const T* __restrict__ scale, const T* __restrict__ means_old,
-                                   double* __restrict__ partials) {
+                                   const T* __restrict__ scale, const T* __restrict__ means_old, double c_mrtol,
+                                   double c_matol, double* __restrict__ partials) {
   using WS = SmoL0TeamWs<T, D>;
   POF_TEAM_PROLOGUE0(WS)
   if (t >= n1) return;
@@ -472,7 +472,7 @@ __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, c
       const double a = (double)means_old[k * D + i], b = (double)w.g1[i];
       bool ok;
       if (isfinite(a) && isfinite(b))
-        ok = fabs(a - b) <= 1e-8 + 1e-13 * fabs(b);
+        ok = fabs(a - b) <= c_matol + c_mrtol * fabs(b);
       else
         ok = (a == b);
       notclose += ok ? 0.0 : 1.0;

@@ -135,11 +135,14 @@ def kernel_flops(kind, n, D, d, C0, cnt):
 
 
 def l0_lanes(D):
-    """Lanes per level-0 chunk (csrc/pof_plan.h l0_lanes)."""
-    return (16 if 2 * D <= 16 else 32) if D >= 6 else 1
+    """Lanes per level-0 chunk (csrc/pof_plan.h: narrow teams from D = 6 on)."""
+    if D < 6:
+        return 1
+    wide = 8 if 2 * D <= 8 else (16 if 2 * D <= 16 else 32)
+    return max(wide // 2, 4)
 
 
-def plan_levels(n, D=4, C0=None, Cg=8, top=8):
+def plan_levels(n, D=4, C0=None, Cg=2, top=2):
     """The level sizes libpof uses (csrc/pof_plan.h make_plan)."""
     if C0 is None:
         lanes = l0_lanes(D)

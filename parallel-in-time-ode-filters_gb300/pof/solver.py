@@ -10,9 +10,11 @@ from .step import ieks_step
 from .utils import MVNSqrt, gmul_stack
 
 
-def _solve_builtin(setup, states, calibrate, maxiters):
+def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxiters_f32=10_000, rtol_f32=1e-5):
     """The whole IEKS loop in libpof (pof_ieks_solve): linearization, chunked
-    filter/smoother, calibration and the convergence test all on the device."""
+    filter/smoother, calibration and the convergence test all on the device.
+    precision="mixed": float32 iterations first, float64 polish after
+    (pof_ieks_solve_mixed)."""
     om = setup["om"]
     name, params = om.field
     x0 = setup["x0"]
@@ -27,14 +29,25 @@ def _solve_builtin(setup, states, calibrate, maxiters):
     info = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
     p = torch.tensor(params if params else (0.0,), dtype=torch.float64, device=dev)
     lib = _lib.lib()
-    wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
-    ws = _lib.workspace(wsb, dev)
     m0 = x0.mean.contiguous()
     L0 = x0.chol.contiguous()
-    rc = lib.pof_ieks_solve(_lib.POF_F64, n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]), _lib.ptr(m0),
-                            _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means), _lib.ptr(chols), int(maxiters),
-                            int(bool(calibrate)), _lib.ptr(info), _lib.ptr(ws), wsb, _lib.stream_handle())
-    _lib.check(rc, "pof_ieks_solve")
+    if precision == "mixed":
+        info = torch.zeros(_lib.I_COUNT + 1, dtype=torch.float64, device=dev)
+        wsb = lib.pof_ieks_mixed_workspace_bytes(n, D, d)
+        ws = _lib.workspace(wsb, dev)
+        rc = lib.pof_ieks_solve_mixed(n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]), _lib.ptr(m0),
+                                      _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means), _lib.ptr(chols),
+                                      int(maxiters_f32), float(rtol_f32), int(maxiters), int(bool(calibrate)),
+                                      _lib.ptr(info), _lib.ptr(ws), wsb, _lib.stream_handle())
+        _lib.check(rc, "pof_ieks_solve_mixed")
+    else:
+        wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+        ws = _lib.workspace(wsb, dev)
+        rc = lib.pof_ieks_solve(_lib.POF_F64, n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]),
+                                _lib.ptr(m0), _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means),
+                                _lib.ptr(chols), int(maxiters), int(bool(calibrate)), _lib.ptr(info), _lib.ptr(ws),
+                                wsb, _lib.stream_handle())
+        _lib.check(rc, "pof_ieks_solve")
     info_dict = {
         "iterations": info[_lib.I_ITERATIONS].to(torch.int64),
         "nll": info[_lib.I_NLL],
@@ -42,17 +55,26 @@ def _solve_builtin(setup, states, calibrate, maxiters):
         "sigma_squared": info[_lib.I_SSQ],
         "calibrated": bool(calibrate),
     }
+    if precision == "mixed":
+        info_dict["iterations_float32"] = info[_lib.I_COUNT].to(torch.int64)
     return MVNSqrt(means, chols), info_dict
 
 
-def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, sequential=False):
+def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, sequential=False,
+          precision="float64", maxiters_f32=10_000, rtol_f32=1e-5):
     """Parallel-in-time IEKS (pof/solver.py:11-73).
 
     Returns (MVNSqrt(means (N, d), chol_covs (N, d, D)), info) with
     info = {iterations, nll, obj, sigma_squared, calibrated}.  Built-in fields
     (pof.ivp) run the whole loop on the device; other torch vector fields are
     linearized with torch.func on the device and filtered/smoothed by libpof,
-    with the loop test read back each iteration."""
+    with the loop test read back each iteration.
+
+    precision="mixed" (built-in fields, an addition to the reference's
+    signature): float32 IEKS iterations until the objective's relative change
+    is below rtol_f32, then float64 iterations to the reference's criterion;
+    info["iterations"] counts the float64 ones, info["iterations_float32"]
+    the others."""
     setup = set_up_solver(f=f, y0=y0, ts=ts, order=order)
     dtm = setup["dtm"]
     om = setup["om"]
@@ -60,8 +82,10 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     states = get_initial_trajectory(setup, method=init)
 
     if om.field is not None and not sequential and _lib.shape_supported(x0.mean.shape[0], setup["iwp"].wiener_process_dimension):
-        states, info_dict = _solve_builtin(setup, states, calibrate, maxiters)
+        states, info_dict = _solve_builtin(setup, states, calibrate, maxiters, precision, maxiters_f32, rtol_f32)
         return gmul_stack(setup["E0"], states), info_dict
+    if precision != "float64":
+        raise NotImplementedError("precision=%r needs a built-in field (pof.ivp)" % (precision,))
 
     dev = x0.mean.device
     z = torch.zeros((), dtype=torch.float64, device=dev)

@@ -1,0 +1,51 @@
+"""Mixed precision (float32 IEKS iterations, float64 polish) against the
+float64 path and the float64 oracle.  The benchmark spec asks every form other
+than the plain float64 path to state its maximum relative error against the
+float64 oracle; the bound asserted here is 1e-6 on the means, in practice the
+polish converges to the float64 fixed point."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import ivp as oivp, solver as osolver
+from pof import ivp as pivp, solver as psolver
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("logistic", lambda: (pivp.logistic(r=3.0), oivp.logistic(r=3.0)), 2000, 3),
+    ("vdp0", lambda: (pivp.vanderpol(stiffness_constant=1.0), oivp.vanderpol(stiffness_constant=1.0)), 512, 3),
+    ("fhn", lambda: (pivp.fhn_classic(tmax=20.0), oivp.fhn_classic(tmax=20.0)), 2000, 3),
+    ("rigid", lambda: (pivp.rigid_body(), oivp.rigid_body()), 512, 2),
+]
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("name,mk,N,q", CASES)
+def test_mixed_matches_float64(name, mk, N, q):
+    p, o = mk()
+    ts = np.linspace(o.t0, o.tmax, N)
+    ref, rinfo = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant", maxiters=2000)
+    mix, minfo = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant", maxiters=2000, precision="mixed")
+    a = mix.mean.cpu().numpy()
+    b = ref.mean.cpu().numpy()
+    err = rel(a, b)
+    print(name, "float32 its", int(minfo["iterations_float32"]), "float64 its", int(minfo["iterations"]),
+          "plain its", int(rinfo["iterations"]), "max rel err", err)
+    assert err <= 1e-6
+    assert np.isfinite(float(minfo["obj"]))
+
+
+def test_mixed_against_oracle():
+    """logistic at N = 300 is a case where float32 is too coarse for the
+    smoother (errors of O(1) even at the solution): the float32 phase must be
+    dropped and the result still match the float64 oracle."""
+    p, o = pivp.logistic(r=3.0), oivp.logistic(r=3.0)
+    ts = np.linspace(0.0, 10.0, 300)
+    (om, _), _ = osolver.solve(o, ts, 3, init="constant", maxiters=1000)
+    mix, _ = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=3, init="constant", precision="mixed")
+    assert rel(mix.mean.cpu().numpy(), om) <= 1e-6
