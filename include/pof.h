@@ -175,7 +175,7 @@ size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
  * filter and smoother in float32 and converts the means back; it is kept if
  * finite.  The float32 phase ends when the largest change of the projected
  * trajectory y = E0 m falls below rtol_f32 relative to max |y|, when that
- * change failed to shrink eight times in a row, after a non-finite float32 iterate
+ * change failed to shrink three times in a row, after a non-finite float32 iterate
  * (discarded) or after maxiters_f32 iterations; a float32 phase whose
  * smallest change never came within 100 rtol_f32 is dropped (float32 is too
  * coarse for that problem) and the float64 loop starts from the input
@@ -232,6 +232,37 @@ void pof_profile_enable(int32_t on);
  * device array of `blocks` doubles that is (almost) never written. */
 int pof_fp64_probe(int64_t iters, int32_t blocks, int32_t threads, double* sink, void* stream);
 int pof_profile_read(double* ms_out, int64_t* count_out, int32_t nkinds, int32_t reset);
+
+/* ---------------------------------------------------------------------------
+ * Batched solves: B independent IVPs of one state shape (D, d) -- each with
+ * its own number of steps, step size h, built-in field and parameters --
+ * through one pipeline of launches per IEKS iteration, replayed from a CUDA
+ * graph.  No counterpart in the reference (it solves one IVP per call,
+ * pof/solver.py:11-73); per problem, the result is that of pof_ieks_solve's
+ * loop (same linearization, filter/smoother, calibration and criterion),
+ * computed by a chunked scan segmented at problem boundaries.  A problem's
+ * result depends only on its own inputs and on (C0, Cg): not on the other
+ * problems of the batch.  Converged problems stop iterating (they are
+ * dropped from the plan once they hold half of its steps).
+ *
+ * Host arrays: n_steps (B), fields (B, POF_FIELD_*), h (B).  Device arrays,
+ * of the dtype: params (B, 4) (first field_nparams used), x0_mean (B, D),
+ * x0_chol (B, D, D) (preconditioned coordinates, as in pof_ieks_solve),
+ * F, QL (D, D) (preconditioned IWP, the same for every h), means (G, D) with
+ * G = sum(n_steps) + B (problem b's N_b = n_steps[b] + 1 grid points follow
+ * those of problem b - 1; in: initial trajectories, out: results),
+ * chols (G, D, D) out; info (B, POF_I_COUNT) device doubles.  C0 (steps per
+ * level-0 chunk) and Cg (group size above) may be 0 for the defaults.
+ * Shapes compiled: (D, d) in {(3,1), (4,1), (5,1), (6,2), (8,2), (10,2)}.
+ * Waits on its own stream once per two iterations; ordered after the work
+ * already on `stream`, and work later put on `stream` waits for it. */
+size_t pof_batch_workspace_bytes(int32_t dtype, int64_t B, const int64_t* n_steps, int32_t D, int32_t d,
+                                 int32_t C0, int32_t Cg);
+int pof_ieks_solve_batch(int32_t dtype, int64_t B, const int64_t* n_steps, int32_t D, int32_t d,
+                         const int32_t* fields, const void* params, const double* h, const void* x0_mean,
+                         const void* x0_chol, const void* F, const void* QL, void* means, void* chols,
+                         int64_t maxiters, int32_t calibrate, int32_t C0, int32_t Cg, double* info, void* workspace,
+                         size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -14,9 +14,11 @@
 using namespace pof;
 
 namespace {
-
 thread_local std::string g_cuda_error;
+}  // namespace
 
+namespace pof {
+// Status of a CUDA runtime call; the message is kept for pof_last_cuda_error.
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return POF_OK;
   g_cuda_error = cudaGetErrorString(e);
@@ -24,6 +26,15 @@ int cuda_status(cudaError_t e) {
 }
 
 int launch_status() { return cuda_status(cudaGetLastError()); }
+
+char* aligned_ws(void* ws) {
+  uintptr_t a = reinterpret_cast<uintptr_t>(ws);
+  a = (a + 255) & ~uintptr_t(255);
+  return reinterpret_cast<char*>(a);
+}
+}  // namespace pof
+
+namespace {
 
 const Ops* find_ops(int dtype, int D, int DY) {
   if (dtype != POF_F64 && dtype != POF_F32) return nullptr;
@@ -55,12 +66,6 @@ int check_common(int dtype, int64_t n, int D, int DY, const Ops** ops) {
 // The filter's scalars are reported through the same block layout.
 void report_scalars(const Plan& p, char* ws, double* out, cudaStream_t st) {
   if (out) k_copy_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(ws + p.scalars), out, 0);
-}
-
-char* aligned_ws(void* ws) {
-  uintptr_t a = reinterpret_cast<uintptr_t>(ws);
-  a = (a + 255) & ~uintptr_t(255);
-  return reinterpret_cast<char*>(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -113,6 +118,7 @@ void prof_begin(int kind, cudaStream_t st) {
   cudaEventRecord(pp.b, st);
   g_prof.open.push_back(pp);
 }
+void prof_flush() { prof_collect(); }
 void prof_end(int kind, cudaStream_t st) {
   for (size_t i = g_prof.open.size(); i-- > 0;) {
     if (g_prof.open[i].kind == kind) {
@@ -280,16 +286,7 @@ int pof_smoothing(int32_t dtype, int64_t n_steps, int32_t D, const void* F, cons
 }
 
 static int nordsieck_p01(int D, int d, double h, double* p0, double* p1) {
-  const int q = D / d - 1;
-  if (q < 1 || D % d) return POF_ERR_ARG;
-  // P = diag(|h|^(q-i+1/2) / (q-i)!), i = 0..q  (pof/transitions.py:53-61)
-  double f0 = 1.0, f1 = 1.0;
-  for (int i = 2; i <= q; ++i) f0 *= i;
-  for (int i = 2; i <= q - 1; ++i) f1 *= i;
-  const double ah = fabs(h);
-  *p0 = pow(ah, q + 0.5) / f0;
-  *p1 = pow(ah, q - 0.5) / f1;
-  return POF_OK;
+  return nordsieck_scales(D, d, h, p0, p1) ? POF_OK : POF_ERR_ARG;
 }
 
 int pof_linearize(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field, const void* params,
@@ -607,7 +604,7 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
     best = rel < best ? rel : best;
     if (rel < rtol_f32) break;       // converged as far as float32 goes
     worse = rel >= prev ? worse + 1 : 0;
-    if (worse >= 8) break;           // float32 stopped helping
+    if (worse >= 3) break;           // float32 stopped helping
     prev = rel;
   }
   // a float32 phase that never came near convergence (an ill-conditioned

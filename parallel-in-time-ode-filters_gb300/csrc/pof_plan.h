@@ -3,6 +3,7 @@
 // always agree.
 #pragma once
 
+#include <math.h>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -54,6 +55,22 @@ inline int pick_c0(int64_t n, int lanes) {
 }
 
 inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Nordsieck scales of the state's derivative orders 0 and 1 at step h:
+// P = diag(|h|^(q-i+1/2) / (q-i)!), i = 0..q (pof/transitions.py:53-61);
+// p0 = P[0, 0], p1 = P[1, 1].  Returns false unless D = d (q + 1), q >= 1.
+inline bool nordsieck_scales(int D, int d, double h, double* p0, double* p1) {
+  if (d < 1 || D % d) return false;
+  const int q = D / d - 1;
+  if (q < 1) return false;
+  double f0 = 1.0, f1 = 1.0;
+  for (int i = 2; i <= q; ++i) f0 *= i;
+  for (int i = 2; i <= q - 1; ++i) f1 *= i;
+  const double ah = fabs(h);
+  *p0 = pow(ah, q + 0.5) / f0;
+  *p1 = pow(ah, q - 0.5) / f1;
+  return true;
+}
 
 // with_solver: also reserve the EK1 (H, c) buffers, a second means buffer
 // and a parameter slot used by the IEKS loop.

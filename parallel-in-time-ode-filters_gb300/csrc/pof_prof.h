@@ -30,5 +30,11 @@ enum ProfKind : int {
 bool prof_on();
 void prof_begin(int kind, cudaStream_t st);
 void prof_end(int kind, cudaStream_t st);
+void prof_flush();  // sum the finished event pairs (waits for them)
+
+// Status helpers shared by the C-ABI translation units (pof_capi.cu).
+int cuda_status(cudaError_t e);
+int launch_status();
+char* aligned_ws(void* ws);  // first 256-byte boundary at or after ws
 
 }  // namespace pof

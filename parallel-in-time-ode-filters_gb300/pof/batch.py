@@ -1,0 +1,216 @@
+"""Batched IEKS solves: many IVPs with built-in fields in one libpof call.
+
+No counterpart in the reference, whose ``pof.solver.solve`` takes one IVP
+(pof/solver.py:11-73).  ``solve_batch`` runs that solve for B problems at
+once -- each with its own field (of one dimension d), parameters, y0 and
+uniform grid -- through ``pof_ieks_solve_batch``: per problem the same
+set-up (convenience.py:13-45), the same initial trajectory and the same
+device-resident IEKS loop as ``pof.solver.solve``.  Each problem's result
+depends only on its own inputs, never on the rest of the batch.
+"""
+
+import math
+from typing import Any, NamedTuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from .transitions import IWP, preconditioned_discretize
+from .utils import default_device
+
+# Built-in fields with explicit parameters p (4 slots), the expressions of
+# pof/ivp.py: used for the Taylor-mode initial states of a whole batch at
+# once (torch.func.vmap over problems).
+_NPARAMS = {"logistic": 1, "lotkavolterra": 4, "vanderpol": 1, "fitzhughnagumo": 4, "fhn_classic": 3,
+            "rober": 3, "rigid_body": 3, "seir": 4, "threebody": 1, "henonheiles": 1}
+_DIM = {"logistic": 1, "lotkavolterra": 2, "vanderpol": 2, "fitzhughnagumo": 2, "fhn_classic": 2,
+        "rober": 3, "rigid_body": 3, "seir": 4, "threebody": 4, "henonheiles": 4}
+
+
+def _field(name):
+    if name == "logistic":
+        return lambda y, p: p[0] * y * (1 - y)
+    if name == "lotkavolterra":
+        return lambda Y, p: torch.stack([p[0] * Y[0] - p[1] * Y[0] * Y[1], -p[2] * Y[1] + p[3] * Y[0] * Y[1]])
+    if name == "vanderpol":
+        return lambda Y, p: torch.stack([Y[1], p[0] * ((1.0 - Y[0] ** 2) * Y[1] - Y[0])])
+    if name == "fitzhughnagumo":
+        return lambda Y, p: torch.stack([Y[0] - (Y[0] ** 3) / 3 - Y[1] + p[3], p[2] * (Y[0] + p[0] - p[1] * Y[1])])
+    if name == "fhn_classic":
+        return lambda Y, p: torch.stack([p[2] * (Y[0] - Y[0] ** 3 / 3 + Y[1]), -(Y[0] - p[0] + p[1] * Y[1]) / p[2]])
+    if name == "rober":
+        return lambda Y, p: torch.stack([-p[0] * Y[0] + p[2] * Y[1] * Y[2],
+                                         p[0] * Y[0] - p[1] * Y[1] ** 2 - p[2] * Y[1] * Y[2], p[1] * Y[1] ** 2])
+    if name == "rigid_body":
+        return lambda y, p: torch.stack([p[0] * y[1] * y[2], p[1] * y[0] * y[2], p[2] * y[0] * y[1]])
+    if name == "seir":
+        return lambda y, p: torch.stack([-p[1] * y[0] * y[2] / p[3], p[1] * y[0] * y[2] / p[3] - p[0] * y[1],
+                                         p[0] * y[1] - p[2] * y[2], p[2] * y[2]])
+    if name == "henonheiles":
+        return lambda y, p: torch.stack([y[2], y[3], -y[0] - 2 * p[0] * y[0] * y[1],
+                                         -y[1] - p[0] * (y[0] ** 2 - y[1] ** 2)])
+    if name == "threebody":
+        def f(y, p):
+            mu = p[0]
+            mp = 1.0 - mu
+            D1 = torch.sqrt((y[0] + mu) ** 2 + y[1] ** 2) ** 3.0
+            D2 = torch.sqrt((y[0] - mp) ** 2 + y[1] ** 2) ** 3.0
+            du0p = y[0] + 2 * y[3] - mp * (y[0] + mu) / D1 - mu * (y[0] - mp) / D2
+            du1p = y[1] - 2 * y[2] - mp * y[1] / D1 - mu * y[1] / D2
+            return torch.stack([y[2], y[3], du0p, du1p])
+        return f
+    raise ValueError("no built-in field %r" % (name,))
+
+
+def _taylor(g, y0, p, q):
+    """(q+1, d) derivatives y^(k)(0) of y' = g(y, p), y(0) = y0 (nested jvp,
+    as pof.initialization.taylor_derivatives)."""
+    derivs = [y0]
+    for k in range(1, q + 1):
+        coeffs = [dj / math.factorial(j) for j, dj in enumerate(derivs)]
+
+        def traj(t, coeffs=coeffs):
+            y = coeffs[0] + 0 * t
+            for j in range(1, len(coeffs)):
+                y = y + coeffs[j] * t**j
+            return g(y, p)
+
+        h = traj
+        for _ in range(k - 1):
+            h = (lambda hh: (lambda t: torch.func.jvp(hh, (t,), (torch.ones_like(t),))[1]))(h)
+        derivs.append(h(torch.zeros((), dtype=y0.dtype, device=y0.device)))
+    return torch.stack(derivs)
+
+
+def _nordsieck(q, hs):
+    """(B, q+1) diagonals of P(h) and P(h)^-1 (pof/transitions.py:53-61), each
+    entry computed as in pof.transitions._nordsieck_1d_np."""
+    powers = np.arange(q, -1, -1)
+    scales = np.array([math.factorial(int(p)) for p in powers], dtype=np.float64)
+    powers = powers + 0.5
+    ah = np.abs(np.asarray(hs, dtype=np.float64))[:, None]
+    return (ah ** powers) / scales, (ah ** (-powers)) * scales
+
+
+class BatchResult(NamedTuple):
+    """Concatenated results of a batch: problem b owns rows
+    offsets[b]:offsets[b+1] of mean (G, d) and chol (G, d, D)."""
+
+    mean: Any
+    chol: Any
+    offsets: Any
+    info: Any
+
+    def problem(self, b):
+        s, e = int(self.offsets[b]), int(self.offsets[b + 1])
+        info = {k: v[b] for k, v in self.info.items() if k != "calibrated"}
+        info["calibrated"] = self.info["calibrated"]
+        return (self.mean[s:e], self.chol[s:e]), info
+
+
+def prepare_batch(problems, order, device=None, init="constant"):
+    """Device inputs of pof_ieks_solve_batch for problems = [(field name,
+    params, y0, ts), ...] (uniform grids ts; the step is ts[1] - ts[0] as in
+    pof.convenience.set_up_solver).  Returns a dict of tensors and host
+    arrays."""
+    if init != "constant":
+        raise NotImplementedError("solve_batch supports init='constant'")
+    dev = device or default_device()
+    B = len(problems)
+    names = [p[0] for p in problems]
+    d = _DIM[names[0]]
+    if any(_DIM[nm] != d for nm in names):
+        raise ValueError("every problem of a batch needs the same dimension d")
+    q = int(order)
+    D = d * (q + 1)
+    n_steps = np.array([len(p[3]) - 1 for p in problems], dtype=np.int64)
+    if (n_steps < 1).any():
+        raise ValueError("every problem needs at least two grid points")
+    hs = np.array([float(p[3][1]) - float(p[3][0]) for p in problems], dtype=np.float64)
+    fields = np.array([_lib.FIELDS[nm] for nm in names], dtype=np.int32)
+    params = torch.zeros((B, 4), dtype=torch.float64)
+    for b, p in enumerate(problems):
+        pv = tuple(float(x) for x in p[1])
+        if len(pv) != _NPARAMS[p[0]]:
+            raise ValueError("field %s takes %d parameters" % (p[0], _NPARAMS[p[0]]))
+        params[b, : len(pv)] = torch.tensor(pv, dtype=torch.float64)
+    y0 = torch.stack([torch.as_tensor(p[2], dtype=torch.float64).reshape(d) for p in problems])
+    # Taylor-mode x0 and the constant-init row [y0, f(y0), 0, ...] per field group
+    derivs = torch.zeros((B, q + 1, d), dtype=torch.float64)
+    for nm in sorted(set(names)):
+        idx = torch.tensor([b for b in range(B) if names[b] == nm], dtype=torch.long)
+        g = _field(nm)
+        derivs[idx] = torch.func.vmap(lambda yy, pp: _taylor(g, yy, pp, q))(y0[idx], params[idx])
+    P, PI = _nordsieck(q, hs)  # (B, q+1)
+    PI_t = torch.as_tensor(PI, dtype=torch.float64)
+    x0m = (derivs.transpose(1, 2) * PI_t[:, None, :]).reshape(B, D)  # dimension-major, times P^-1
+    row = torch.zeros((B, d, q + 1), dtype=torch.float64)
+    row[:, :, 0] = y0
+    row[:, :, 1] = derivs[:, 1, :]
+    row = (row * PI_t[:, None, :]).reshape(B, D)
+    counts = torch.as_tensor(n_steps + 1)
+    means0 = torch.repeat_interleave(row, counts, dim=0)
+    iwp = IWP(num_derivatives=q, wiener_process_dimension=d)
+    F, QL = preconditioned_discretize(iwp, device=dev)
+    offsets = np.concatenate([[0], np.cumsum(n_steps + 1)]).astype(np.int64)
+    return {
+        "B": B, "D": D, "d": d, "q": q, "n_steps": n_steps, "fields": fields, "h": hs,
+        "params": params.to(dev), "x0m": x0m.to(dev).contiguous(),
+        "x0L": torch.zeros((B, D, D), dtype=torch.float64, device=dev), "F": F.contiguous(),
+        "QL": QL.contiguous(), "means0": means0.to(dev).contiguous(), "p0": torch.as_tensor(P[:, 0]),
+        "offsets": offsets,
+    }
+
+
+def run_batch(prep, means, chols, info, maxiters=10_000, calibrate=True, C0=0, Cg=0, dtype_code=_lib.POF_F64,
+              workspace=None):
+    """pof_ieks_solve_batch on prepared inputs; means (G, D) holds the initial
+    trajectories on entry and the results on return.  Returns the workspace
+    (reusable for the same batch)."""
+    lib = _lib.lib()
+    B, D, d = prep["B"], prep["D"], prep["d"]
+    ns = np.ascontiguousarray(prep["n_steps"], dtype=np.int64)
+    fl = np.ascontiguousarray(prep["fields"], dtype=np.int32)
+    hs = np.ascontiguousarray(prep["h"], dtype=np.float64)
+    vp = lambda a: a.ctypes.data_as(_lib.ctypes.c_void_p)  # noqa: E731
+    wsb = lib.pof_batch_workspace_bytes(dtype_code, B, vp(ns), D, d, int(C0), int(Cg))
+    if wsb == 0:
+        raise _lib.PofError("pof_batch_workspace_bytes refused the batch (shape (%d, %d) or sizes)" % (D, d))
+    if workspace is None or workspace.numel() < wsb:
+        workspace = _lib.workspace(wsb, means.device)
+    rc = lib.pof_ieks_solve_batch(dtype_code, B, vp(ns), D, d, vp(fl), _lib.ptr(prep["params"]), vp(hs),
+                                  _lib.ptr(prep["x0m"]), _lib.ptr(prep["x0L"]), _lib.ptr(prep["F"]),
+                                  _lib.ptr(prep["QL"]), _lib.ptr(means), _lib.ptr(chols), int(maxiters),
+                                  int(bool(calibrate)), int(C0), int(Cg), _lib.ptr(info), _lib.ptr(workspace),
+                                  int(workspace.numel()), _lib.stream_handle())
+    _lib.check(rc, "pof_ieks_solve_batch")
+    return workspace
+
+
+def project(prep, means, chols):
+    """(E0 P) applied per problem: ys.mean (G, d) and ys.chol (G, d, D), as
+    pof.solver.solve returns (gmul_stack(E0 P, states))."""
+    q1 = prep["q"] + 1
+    counts = torch.as_tensor(prep["n_steps"] + 1, device=means.device)
+    p0 = torch.repeat_interleave(prep["p0"].to(means.device), counts)
+    idx = torch.arange(prep["d"], device=means.device) * q1
+    return means[:, idx] * p0[:, None], chols[:, idx, :] * p0[:, None, None]
+
+
+def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_000, C0=0, Cg=0):
+    """Solve every (field name, params, y0, ts) of ``problems`` with the
+    parallel IEKS of pof.solver.solve (built-in fields, constant init).
+    Returns a BatchResult; ``result.problem(b)`` gives problem b's
+    ((means (N_b, d), chol_covs (N_b, d, D)), info) as pof.solver.solve."""
+    dev = default_device()
+    prep = prepare_batch(problems, order, device=dev, init=init)
+    means = prep["means0"].clone()
+    G, D = means.shape
+    chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
+    run_batch(prep, means, chols, info, maxiters=maxiters, calibrate=calibrate, C0=C0, Cg=Cg)
+    ym, yc = project(prep, means, chols)
+    info_d = {"iterations": info[:, _lib.I_ITERATIONS].to(torch.int64), "nll": info[:, _lib.I_NLL],
+              "obj": info[:, _lib.I_OBJ], "sigma_squared": info[:, _lib.I_SSQ], "calibrated": bool(calibrate)}
+    return BatchResult(ym, yc, prep["offsets"], info_d)

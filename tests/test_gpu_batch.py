@@ -1,0 +1,161 @@
+"""Batched solves (pof_ieks_solve_batch) against the float64 oracle, problem
+by problem, and the batch invariants: a problem's result does not depend on
+the other problems of the batch, on their order, on re-planning or on the
+CUDA-graph replay."""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import ivp as oivp, solver as osolver
+from oracle.scan import sequential_scan
+from pof import batch as pbatch, ivp as pivp, solver as psolver
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def covrel(a, b):
+    A = a @ np.swapaxes(a, -1, -2)
+    B = b @ np.swapaxes(b, -1, -2)
+    return rel(A, B)
+
+
+def close(x, ref, alt):
+    return abs(float(x) - ref) <= max(TOL * abs(ref), 10.0 * abs(ref - alt), 1e-300)
+
+
+def oracle_ivp(name, params, y0, t0, t1):
+    if name == "logistic":
+        return oivp.logistic(t0=t0, tmax=t1, y0=y0, r=params[0])
+    if name == "lotkavolterra":
+        return oivp.lotkavolterra(t0=t0, tmax=t1, y0=y0, p=params)
+    if name == "vanderpol":
+        return oivp.vanderpol(t0=t0, tmax=t1, y0=y0, stiffness_constant=params[0])
+    if name == "fhn_classic":
+        a, b, c = params
+        return oivp.fhn_classic(t0=t0, tmax=t1, y0=y0, a=a, b=b, c=c)
+    if name == "fitzhughnagumo":
+        return oivp.fitzhughnagumo(t0=t0, tmax=t1, y0=y0, p=params)
+    raise ValueError(name)
+
+
+# (field, params, y0, t0, t1, N); one batch per dimension, fields mixed
+BATCH_D1 = [
+    ("logistic", (3.0,), [0.01], 0.0, 10.0, 200),
+    ("logistic", (2.5,), [0.02], 0.0, 10.0, 64),
+    ("logistic", (3.5,), [0.015], 0.0, 8.0, 333),
+    ("logistic", (1.0,), [0.01], 0.0, 10.0, 17),
+]
+BATCH_D2 = [
+    ("lotkavolterra", (1.5, 1.0, 3.0, 1.0), [1.0, 1.0], 0.0, 7.0, 150),
+    ("vanderpol", (1.0,), [2.0, 0.0], 0.0, 6.3, 128),
+    ("fitzhughnagumo", (0.7, 0.8, 0.08, 0.5), [1.0, 1.0], 0.0, 20.0, 90),
+    ("lotkavolterra", (1.3, 0.9, 2.8, 1.1), [1.2, 0.8], 0.0, 5.0, 61),
+    ("vanderpol", (1.2,), [1.9, 0.1], 0.0, 5.0, 257),
+    ("fhn_classic", (0.2, 0.2, 3.0), [-1.0, 1.0], 0.0, 5.0, 120),
+]
+
+
+def problems(spec):
+    return [(nm, p, y0, np.linspace(t0, t1, N)) for (nm, p, y0, t0, t1, N) in spec]
+
+
+@pytest.mark.parametrize("spec,q", [(BATCH_D1, 3), (BATCH_D2, 3), (BATCH_D2, 2), (BATCH_D1, 4)])
+def test_batch_matches_oracle(spec, q):
+    """Every problem of a mixed batch: the oracle's IEKS iteration count,
+    means within 1e-10 (or 10x the spread between the oracle's tree and
+    sequential orders), covariances per unit sigma^2 likewise, NLL and
+    objective likewise."""
+    res = pbatch.solve_batch(problems(spec), order=q, maxiters=1000)
+    for b, (nm, p, y0, t0, t1, N) in enumerate(spec):
+        o = oracle_ivp(nm, p, y0, t0, t1)
+        ts = np.linspace(t0, t1, N)
+        (om, oL), oinfo = osolver.solve(o, ts, q, init="constant", maxiters=1000)
+        (sm, sL), sinfo = osolver.solve(o, ts, q, init="constant", maxiters=1000, scan=sequential_scan)
+        (gm, gL), ginfo = res.problem(b)
+        gm, gL = gm.cpu().numpy(), gL.cpu().numpy()
+        assert int(ginfo["iterations"]) == oinfo["iterations"], (b, nm)
+        assert rel(gm, om) <= max(TOL, 10 * rel(sm, om)), (b, nm)
+        gs, os_, ss_ = float(ginfo["sigma_squared"]), oinfo["sigma_squared"], sinfo["sigma_squared"]
+        assert covrel(gL / gs, oL / os_) <= max(TOL, 10 * covrel(sL / ss_, oL / os_)), (b, nm)
+        if len(y0) == 1:
+            assert close(gs, os_, ss_), (b, nm)
+        assert close(ginfo["obj"], oinfo["obj"], sinfo["obj"]), (b, nm)
+        assert close(ginfo["nll"], oinfo["nll"], sinfo["nll"]), (b, nm)
+
+
+def _run(spec, q, C0=8, Cg=2):
+    return pbatch.solve_batch(problems(spec), order=q, maxiters=1000, C0=C0, Cg=Cg)
+
+
+def _same(ra, a, rb, b):
+    (ma, La), ia = ra.problem(a)
+    (mb, Lb), ib = rb.problem(b)
+    assert torch.equal(ma, mb) and torch.equal(La, Lb)
+    for k in ("iterations", "nll", "obj", "sigma_squared"):
+        assert float(ia[k]) == float(ib[k]), k
+
+
+def test_batch_result_independent_of_the_mix():
+    """Bit-identical results for a problem solved alone, in the batch, and in
+    the batch in reverse order (fixed C0, Cg)."""
+    full = _run(BATCH_D2, 3)
+    rev = _run(BATCH_D2[::-1], 3)
+    B = len(BATCH_D2)
+    for b in range(B):
+        alone = _run([BATCH_D2[b]], 3)
+        _same(full, b, alone, 0)
+        _same(full, b, rev, B - 1 - b)
+
+
+def test_batch_graph_and_direct_launches_agree():
+    a = _run(BATCH_D1, 3)
+    os.environ["POF_BATCH_NO_GRAPH"] = "1"
+    try:
+        b = _run(BATCH_D1, 3)
+    finally:
+        del os.environ["POF_BATCH_NO_GRAPH"]
+    for i in range(len(BATCH_D1)):
+        _same(a, i, b, i)
+
+
+def test_batch_matches_plain_solve():
+    """Each problem against pof.solver.solve (one IVP per call): same
+    iteration count, means within the oracle-spread tolerance."""
+    spec = BATCH_D1
+    res = pbatch.solve_batch(problems(spec), order=3, maxiters=1000)
+    for b, (nm, p, y0, t0, t1, N) in enumerate(spec):
+        ivp = pivp.logistic(t0=t0, tmax=t1, y0=y0, r=p[0])
+        ts = np.linspace(t0, t1, N)
+        out, info = psolver.solve(f=ivp.f, y0=ivp.y0, ts=ts, order=3, init="constant", maxiters=1000)
+        (gm, _), ginfo = res.problem(b)
+        o = oracle_ivp(nm, p, y0, t0, t1)
+        (om, _), _ = osolver.solve(o, ts, 3, init="constant", maxiters=1000)
+        (sm, _), _ = osolver.solve(o, ts, 3, init="constant", maxiters=1000, scan=sequential_scan)
+        assert int(ginfo["iterations"]) == int(info["iterations"])
+        assert rel(gm.cpu().numpy(), out.mean.cpu().numpy()) <= max(TOL, 20 * rel(sm, om))
+
+
+def test_batch_chunk_shapes():
+    """Chunk lengths 1, 3, 64 and group sizes 2, 5 (ragged problems whose
+    step counts are not multiples of either) give the oracle's answer."""
+    spec = BATCH_D1
+    ref = None
+    for C0, Cg in [(1, 2), (3, 5), (64, 2), (3, 2)]:
+        res = _run(spec, 3, C0=C0, Cg=Cg)
+        if ref is None:
+            ref = res
+            continue
+        for b in range(len(spec)):
+            (ma, _), ia = ref.problem(b)
+            (mb, _), ib = res.problem(b)
+            assert int(ia["iterations"]) == int(ib["iterations"])
+            assert rel(mb.cpu().numpy(), ma.cpu().numpy()) <= 1e-9
