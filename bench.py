@@ -295,6 +295,11 @@ def run_gpu(args, workload):
         solve_resident()
     torch.cuda.synchronize()
     iterations = int(info[_lib.I_ITERATIONS].item())
+    if args.solves_only:  # the launches of W + K solves and nothing else (ncu captures)
+        for _ in range(args.steps):
+            solve_resident()
+        torch.cuda.synchronize()
+        return
 
     def barrier():
         torch.cuda.synchronize()
@@ -440,18 +445,278 @@ def run_gpu(args, workload):
     jprint(out)
 
 
+# ---------------------------------------------------------------------------
+# Batched uneven solves: many FitzHugh-Nagumo IVPs in one batched solve
+# ---------------------------------------------------------------------------
+
+BATCH_WORKLOADS = {
+    # name: (instances, seed, q, maxiters).  About one instance in six cycles
+    # without meeting the reference's criterion (mostly N in [512, 2048]) and
+    # runs to maxiters + 1: the capped forms bound a solve's length.
+    "fhn_batch4096": (4096, 0, 3, MAXITERS),
+    "fhn_batch4096_it100": (4096, 0, 3, 100),
+    "fhn_batch512_it300": (512, 0, 3, 300),
+}
+
+
+def fhn_batch_problems(B, seed):
+    """B FitzHugh-Nagumo IVPs: (a, b, c) each uniform within +-20 % of
+    (0.2, 0.2, 3), y0 ~ N((-1, 1), 0.1^2 I), t in [0, 100], N log-uniform
+    in [256, 8192] (seeded)."""
+    rng = np.random.default_rng(seed)
+    abc = np.array([0.2, 0.2, 3.0]) * rng.uniform(0.8, 1.2, size=(B, 3))
+    y0 = np.array([-1.0, 1.0]) + 0.1 * rng.standard_normal((B, 2))
+    N = np.floor(np.exp(rng.uniform(np.log(256), np.log(8192), size=B))).astype(int)
+    return [("fhn_classic", tuple(abc[b]), y0[b], np.linspace(0.0, 100.0, N[b])) for b in range(B)]
+
+
+def run_gpu_batch(args, workload):
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from pof import _build, _flops, _lib, batch as pbatch
+
+    _build.build(verbose=False)
+    lib = _lib.lib()
+    B, seed, q, maxiters = BATCH_WORKLOADS[workload]
+    problems = fhn_batch_problems(B, seed + rank)
+    dev = torch.device("cuda", local)
+    prep = pbatch.prepare_batch(problems, q, device=dev)
+    n_steps = prep["n_steps"]
+    total_steps = int(n_steps.sum())
+    D, d = prep["D"], prep["d"]
+    means0 = prep["means0"]
+    G = means0.shape[0]
+    means = torch.empty_like(means0)
+    chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros((B, _lib.I_COUNT), dtype=torch.float64, device=dev)
+    ws = None
+
+    def solve(precision="float64", info32=None):
+        nonlocal ws
+        means.copy_(means0)
+        ws = pbatch.run_batch(prep, means, chols, info, maxiters=maxiters, workspace=ws, precision=precision,
+                              info_f32=info32)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        out = []
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return out
+
+    for _ in range(args.warmup):
+        solve()
+    if args.solves_only:  # the launches of W + K batched solves and nothing else (ncu captures)
+        for _ in range(args.steps):
+            solve()
+        torch.cuda.synchronize()
+        return
+    barrier()
+    with ClockSampler(local) as clk:
+        times = timed(solve, args.steps)  # inputs (G x D means, ~0.5 GB) exceed L2
+        barrier()
+    ms = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    its = info[:, _lib.I_ITERATIONS].cpu().numpy()
+    step_iters = int((n_steps * its).sum())
+    value = world * total_steps / (ms * 1e-3)
+    ref_means = means.clone()
+
+    # mixed precision: float32 iterations, float64 polish, per problem
+    mixed = None
+    if not args.no_mixed:
+        info32 = torch.zeros(B, dtype=torch.float64, device=dev)
+        ws = None
+        for _ in range(args.warmup):
+            solve("mixed", info32)
+        mt = timed(lambda: solve("mixed", info32), args.steps)
+        mms = float(np.mean(mt))
+        E0P = _project_err(prep, means, ref_means)
+        it32 = info32.cpu().numpy()
+        it64 = info[:, _lib.I_ITERATIONS].cpu().numpy()
+        mixed = {"value": world * total_steps / (mms * 1e-3), "unit": "IVP*steps/s", "ms_per_step": mms,
+                 "iterations_float32_total": int(it32.sum()), "iterations_float64_total": int(it64.sum()),
+                 "max_rel_err_vs_float64": E0P, "speedup_vs_float64_batched": ms / mms}
+        ws = None
+
+    # plain one-solve-per-launch float64 path on a stratified sample
+    order = np.argsort(n_steps)
+    sample = [int(order[int(i)]) for i in np.linspace(0, B - 1, 8)]
+    plain_s = 0.0
+    plain_steps = 0
+    for b in sample:
+        n = int(n_steps[b])
+        m = means0[prep["offsets"][b]:prep["offsets"][b + 1]].clone()
+        c = torch.empty((n + 1, D, D), dtype=torch.float64, device=dev)
+        inf = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+        wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+        pws = _lib.workspace(wsb, dev)
+        x0m = prep["x0m"][b].contiguous()
+        x0L = prep["x0L"][b].contiguous()
+
+        def one():
+            m.copy_(means0[prep["offsets"][b]:prep["offsets"][b + 1]])
+            rc = lib.pof_ieks_solve(_lib.POF_F64, n, D, d, int(prep["fields"][b]), _lib.ptr(prep["params"][b]),
+                                    float(prep["h"][b]), _lib.ptr(x0m), _lib.ptr(x0L), _lib.ptr(prep["F"]),
+                                    _lib.ptr(prep["QL"]), _lib.ptr(m), _lib.ptr(c), maxiters, 1, _lib.ptr(inf),
+                                    _lib.ptr(pws), wsb, _lib.stream_handle())
+            _lib.check(rc, "pof_ieks_solve")
+
+        one()
+        tt = timed(one, 1)[0]
+        plain_s += tt * 1e-3
+        plain_steps += n
+    plain_value = plain_steps / plain_s
+
+    # per-kernel times of one batched solve (profiler on, not timed)
+    _lib.profile_enable(True)
+    _lib.profile_read(reset=True)
+    solve()
+    torch.cuda.synchronize()
+    prof = _lib.profile_read(reset=True)
+    _lib.profile_enable(False)
+    per_step = {"filt_l0_down": _flops.kf_step(D, d, True) + _flops.objective_term(D),
+                "filt_l0_reduce": _flops.cond_fold_step(D, d),
+                "smo_l0_down": _flops.smooth_apply(D) + _flops.objective_term(D) + D * D}
+    kern = {k: v for k, v in prof.items() if v[1] > 0 and k in per_step}
+    dom = max(kern, key=lambda k: kern[k][0])
+    dom_ms = kern[dom][0]
+    dom_launches = kern[dom][1]
+    achieved = per_step[dom] * step_iters / (dom_ms * 1e-3) / 1e9
+    peak = fp64_peak(torch, lib, _lib)
+
+    # end to end through the public API with host inputs and host results
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = pbatch.solve_batch(problems, order=q, maxiters=maxiters)
+        ym = res.mean.cpu().numpy()
+        yc = res.chol.cpu().numpy()
+        el = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_times.append(el)
+    h2d = sum(len(p[3]) * 8 + 16 + 24 for p in problems)
+    d2h = ym.nbytes + yc.nbytes
+    e2e_s = float(np.mean(e2e_times))
+
+    if rank != 0:
+        return
+    out = {
+        "metric": "IVP*steps/s (batched parallel IEKS solve, float64)",
+        "value": value,
+        "unit": "IVP*steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload, "instances": B, "seed": seed, "ivp": "fhn_classic",
+                   "params": "a, b, c uniform within +-20% of (0.2, 0.2, 3)", "y0": "N((-1, 1), 0.1^2 I)",
+                   "t1": 100.0, "N": "log-uniform in [256, 8192]", "q": q, "D": D, "init": "constant",
+                   "maxiters": maxiters, "total_steps": total_steps, "step_iterations": step_iters,
+                   "iterations_percentiles": {str(p): float(np.percentile(its, p)) for p in (0, 50, 90, 99, 100)},
+                   "l2": "inputs (%.2f GB of iterates) exceed L2" % (G * D * 8 / 1e9)},
+        "plain_float64_one_solve_per_launch": {"value": plain_value, "unit": "IVP*steps/s",
+                                               "sample": "8 instances stratified by N, pof_ieks_solve each",
+                                               "speedup_batched_vs_plain": value / plain_value},
+        "e2e": {"value": world * total_steps / e2e_s, "unit": "IVP*steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                "path": "pof.batch.solve_batch(problem list with numpy y0 / ts) -> means/chols .cpu()"},
+        "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured on this GPU by pof_fp64_probe (FP64 FMA chains)",
+                     "flops_total": per_step[dom] * step_iters, "ms_total": dom_ms, "launches": dom_launches},
+        "kernels": {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in prof.items() if v[1]},
+        "gpu_launches": int(sum(c for _, c in prof.values()) * args.steps),
+        "clocks": clk.summary(),
+    }
+    if mixed is not None:
+        out["mixed_precision"] = mixed
+        out["plain_float64_one_solve_per_launch"]["speedup_mixed_batched_vs_plain"] = mixed["value"] / plain_value
+    if not args.no_cpu_baseline:
+        cb = cpu_sample_batch(problems, q, its)
+        out["cpu_baseline"] = cb
+    jprint(out)
+
+
+def _project_err(prep, a, b):
+    """max |y_a - y_b| / max |y_b| over the solution components y = E0 P m."""
+    import torch
+
+    counts = torch.as_tensor(prep["n_steps"] + 1, device=a.device)
+    p0 = torch.repeat_interleave(prep["p0"].to(a.device), counts)[:, None]
+    idx = torch.arange(prep["d"], device=a.device) * (prep["q"] + 1)
+    ya, yb = a[:, idx] * p0, b[:, idx] * p0
+    return float(((ya - yb).abs().max() / yb.abs().max()).item())
+
+
+def cpu_sample_batch(problems, q, its, budget_s=20.0):
+    """The oracle's cost per step and IEKS iteration on one instance of the
+    batch (a contiguous sub-grid, as cpu_sample), extrapolated to every
+    instance's steps x iterations."""
+    from oracle import ivp as oivp, solver as osolver
+
+    nm, p, y0, ts = problems[0]
+    ivp = oivp.fhn_classic(tmax=float(ts[-1]), y0=list(y0), a=p[0], b=p[1], c=p[2])
+    M = 256
+    while True:
+        st = osolver.set_up_solver(ivp, ts[: M + 1], q)
+        states = osolver.get_initial_trajectory(st, "constant")
+        t0 = time.perf_counter()
+        osolver.ieks_step(st, states)
+        el = time.perf_counter() - t0
+        if el > budget_s / 4 or M >= len(ts) - 1:
+            break
+        M = min(M * 4, len(ts) - 1)
+    per = el / M
+    total = sum((len(pp[3]) - 1) * int(i) for pp, i in zip(problems, its))
+    steps = sum(len(pp[3]) - 1 for pp in problems)
+    solve_s = per * total
+    return {"value": steps / solve_s, "unit": "IVP*steps/s", "cores": 1, "kind": "port",
+            "sample": "one IEKS iteration of the oracle on %d steps of instance 0; solve time extrapolated as cost "
+                      "per step-iteration x sum over instances of steps x the GPU's iteration count" % M}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--solves-only", action="store_true",
+                    help="run the W + K solves of the workload and exit (for profiler captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args, args.workload)
+    elif args.workload in BATCH_WORKLOADS:
+        run_gpu_batch(args, args.workload)
     else:
         run_gpu(args, args.workload)
 

@@ -264,6 +264,21 @@ int pof_ieks_solve_batch(int32_t dtype, int64_t B, const int64_t* n_steps, int32
                          int64_t maxiters, int32_t calibrate, int32_t C0, int32_t Cg, double* info, void* workspace,
                          size_t workspace_bytes, void* stream);
 
+/* pof_ieks_solve_mixed for a batch (no reference counterpart): per problem,
+ * float32 IEKS iterations (float64 linearization at the float64 iterate,
+ * float32 filter/smoother, the change judged in float64) under
+ * pof_ieks_solve_mixed's stopping and discard rules, then the float64 loop
+ * of pof_ieks_solve_batch from the kept iterate.  Arrays as in
+ * pof_ieks_solve_batch, all float64; info_f32 (B) device doubles receives
+ * the number of kept float32 iterations of each problem (may be NULL). */
+size_t pof_batch_mixed_workspace_bytes(int64_t B, const int64_t* n_steps, int32_t D, int32_t d, int32_t C0,
+                                       int32_t Cg);
+int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int32_t d, const int32_t* fields,
+                               const double* params, const double* h, const double* x0_mean, const double* x0_chol,
+                               const double* F, const double* QL, double* means, double* chols, int64_t maxiters_f32,
+                               double rtol_f32, int64_t maxiters, int32_t calibrate, int32_t C0, int32_t Cg,
+                               double* info, double* info_f32, void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

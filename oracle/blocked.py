@@ -150,9 +150,35 @@ def _filter_states_at_starts(elems, Cs, m0, L0):
     return states
 
 
-def filter_blocked(x0, dtm, dom, C0=4, Cs=(4,)):
+def _filter_states_segmented(elems, Cg, m0, L0):
+    """States before each element for the batched schedule: groups of Cg
+    elements fold until one element remains, whose start state is x0; the
+    down-sweep propagates through every group (no element is special)."""
+    n = elems[0].shape[0]
+    if n == 1:
+        return [(m0, L0)]
+    chunks = _chunks(n, Cg)
+    totals = [_fold_general(tuple(x[s:t] for x in elems)) for s, t in chunks]
+    totals = tuple(np.stack([tt[j] for tt in totals]) for j in range(5))
+    starts = _filter_states_segmented(totals, Cg, m0, L0)
+    states = []
+    for (s, t), st in zip(chunks, starts):
+        cur = st
+        states.append(cur)
+        for i in range(s, t - 1):
+            cur = _propagate_state(cur[0], cur[1], tuple(x[i] for x in elems))
+            states.append(cur)
+    return states
+
+
+def filter_blocked(x0, dtm, dom, C0=4, Cs=(4,), segmented=False):
     """Filtered marginals with the chunked schedule; returns
-    ((means, chols), nll, obj, ssq, chunk_states)."""
+    ((means, chols), nll, obj, ssq, chunk_states).
+
+    segmented=True restates the batched solve's schedule for one problem
+    (csrc/pof_batch.cuh): chunk 0 is a conditional fold like the others, the
+    levels above fold groups of Cs[0] until one element remains, and x0 is
+    the state before it."""
     F, QL = dtm
     H, c, R = dom
     n, d, D = H.shape
@@ -161,7 +187,7 @@ def filter_blocked(x0, dtm, dom, C0=4, Cs=(4,)):
     # phase 1: chunk totals
     totals = []
     for j, (s, t) in enumerate(chunks):
-        if j == 0:
+        if j == 0 and not segmented:
             m, L = m0, L0
             for k in range(s, t):
                 m, L, _, _, _ = kf_step(F[k], QL[k], H[k], c[k], R[k], m, L)
@@ -170,7 +196,10 @@ def filter_blocked(x0, dtm, dom, C0=4, Cs=(4,)):
             totals.append(conditional_fold(F[s:t], QL[s:t], H[s:t], c[s:t], R[s:t]))
     totals = tuple(np.stack([tt[j] for tt in totals]) for j in range(5))
     # phase 2: state at every chunk start
-    starts = _filter_states_at_starts(totals, list(Cs), m0, L0)
+    if segmented:
+        starts = _filter_states_segmented(totals, Cs[0], m0, L0)
+    else:
+        starts = _filter_states_at_starts(totals, list(Cs), m0, L0)
     # phase 3: KF inside every chunk
     means = [m0]
     chols = [L0]
@@ -251,8 +280,28 @@ def _smoother_states_at_ends(elems, Cs, mT, LT):
     return ends
 
 
-def smoother_blocked(dtm, filt, C0=4, Cs=(4,)):
-    """Smoothed marginals with the chunked schedule; returns ((means, chols), obj)."""
+def _smoother_states_segmented(elems, Cg, mT, LT):
+    """Smoothed state after each element for the batched schedule: groups of
+    Cg fold until one element remains, which ends at the terminal state."""
+    n = elems[0].shape[0]
+    if n == 1:
+        return [(mT, LT)]
+    chunks = _chunks(n, Cg)
+    totals = [_fold_smoother(tuple(x[s:t] for x in elems)) for s, t in chunks]
+    totals = tuple(np.stack([tt[j] for tt in totals]) for j in range(3))
+    cends = _smoother_states_segmented(totals, Cg, mT, LT)
+    ends = [None] * n
+    for (s, t), ce in zip(chunks, cends):
+        cur = ce
+        for i in range(t - 1, s - 1, -1):
+            ends[i] = cur
+            cur = _apply_composite(tuple(x[i] for x in elems), *cur)
+    return ends
+
+
+def smoother_blocked(dtm, filt, C0=4, Cs=(4,), segmented=False):
+    """Smoothed marginals with the chunked schedule; returns ((means, chols), obj).
+    segmented=True: the batched solve's hierarchy (see filter_blocked)."""
     F, QL = dtm
     fm, fL = filt
     N, D = fm.shape
@@ -265,7 +314,10 @@ def smoother_blocked(dtm, filt, C0=4, Cs=(4,)):
     chunks = _chunks(n, C0)
     totals = [_fold_smoother((g[s:t], E[s:t], Dk[s:t])) for s, t in chunks]
     totals = tuple(np.stack([tt[j] for tt in totals]) for j in range(3))
-    ends = _smoother_states_at_ends(totals, list(Cs), fm[-1], fL[-1])
+    if segmented:
+        ends = _smoother_states_segmented(totals, Cs[0], fm[-1], fL[-1])
+    else:
+        ends = _smoother_states_at_ends(totals, list(Cs), fm[-1], fL[-1])
     means = np.zeros((N, D))
     chols = np.zeros((N, D, D))
     means[-1], chols[-1] = fm[-1], fL[-1]
@@ -282,8 +334,18 @@ def smoother_blocked(dtm, filt, C0=4, Cs=(4,)):
     return (means, chols), sum(obj_c)
 
 
-def linear_filtsmooth_blocked(x0, dtm, dom, C0=4, Cs=(4,)):
+def linear_filtsmooth_blocked(x0, dtm, dom, C0=4, Cs=(4,), segmented=False):
     """``pof/parallel_filtsmooth/__init__.py:5-10`` with the chunked schedule."""
-    out, nll, _, ssq, _ = filter_blocked(x0, dtm, dom, C0=C0, Cs=Cs)
-    out, obj = smoother_blocked(dtm, out, C0=C0, Cs=Cs)
+    out, nll, _, ssq, _ = filter_blocked(x0, dtm, dom, C0=C0, Cs=Cs, segmented=segmented)
+    out, obj = smoother_blocked(dtm, out, C0=C0, Cs=Cs, segmented=segmented)
     return out, nll, obj, ssq
+
+
+def segmented_filtsmooth(C0, Cg):
+    """linear_filtsmooth with the batched solve's schedule, for
+    oracle.solver.solve(..., filtsmooth=...)."""
+
+    def fs(x0, dtm, dom):
+        return linear_filtsmooth_blocked(x0, dtm, dom, C0=C0, Cs=(Cg,), segmented=True)
+
+    return fs

@@ -153,11 +153,14 @@ def crit(obj, obj_old, nll, nll_old, means, means_old, *, rtol=1e-6, atol=1e-9):
     return bool(isnan or obj_converged or means_converged)
 
 
-def ieks_step(setup, states, calibrate=True, sequential=False, scan=associative_scan):
-    """``step.py:33-45``."""
+def ieks_step(setup, states, calibrate=True, sequential=False, scan=associative_scan, filtsmooth_fn=None):
+    """``step.py:33-45``.  filtsmooth_fn(x0, dtm, dom) replaces the parallel
+    filter/smoother (another bracketing of the same scans)."""
     dtm = (setup.F, setup.QL)
     dom = linearize_at_previous_states(setup, states[0])
-    if not sequential:
+    if filtsmooth_fn is not None:
+        out, nll, obj, ssq = filtsmooth_fn(setup.x0, dtm, dom)
+    elif not sequential:
         out, nll, obj, ssq = filtsmooth.linear_filtsmooth(setup.x0, dtm, dom, scan=scan)
     else:
         out, nll, obj, ssq = filtsmooth.sequential_linear_filtsmooth(setup.x0, dtm, dom)
@@ -167,7 +170,7 @@ def ieks_step(setup, states, calibrate=True, sequential=False, scan=associative_
 
 
 def solve(ivp, ts, order, init="prior", calibrate=True, maxiters=10_000, sequential=False,
-          scan=associative_scan, return_full=False, callback=None):
+          scan=associative_scan, return_full=False, callback=None, filtsmooth_fn=None):
     """``solver.py:11-73``: returns ((means (N,d), chols (N,d,D)), info)."""
     setup = set_up_solver(ivp, ts, order)
     states = get_initial_trajectory(setup, method=init)
@@ -183,7 +186,8 @@ def solve(ivp, ts, order, init="prior", calibrate=True, maxiters=10_000, sequent
             break
         # body (solver.py:47-55)
         states_old, nll_old, obj_old = states, nll, obj
-        states, nll, obj, ssq = ieks_step(setup, states_old, sequential=sequential, scan=scan)
+        states, nll, obj, ssq = ieks_step(setup, states_old, sequential=sequential, scan=scan,
+                                          filtsmooth_fn=filtsmooth_fn)
         k += 1
         if callback is not None:
             callback(k, states, nll, obj, ssq)

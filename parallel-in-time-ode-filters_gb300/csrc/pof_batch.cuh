@@ -489,6 +489,194 @@ __global__ void kb_finish(const int64_t* __restrict__ so, const double* __restri
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision (float32 iterations, float64 polish) for a batch: the
+// per-problem form of pof_ieks_solve_mixed's float32 phase.
+// ---------------------------------------------------------------------------
+
+// EK1 linearization in float64 at the float64 iterate (kb_linearize's
+// arithmetic), each row of (H, c) scaled to unit norm and rounded to float32
+// (a noiseless observation row can be scaled freely; k_rows_to_f32).
+template <int D, int DY>
+__global__ void kb_lin_mixed(BView v, const double* __restrict__ params, const double* __restrict__ means,
+                             float* __restrict__ H, float* __restrict__ c) {
+  constexpr int Q1 = D / DY;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = i / v.C0;
+  if (t >= v.n1) return;
+  const int b = v.cp[t];
+  if (v.frozen[b]) return;
+  const int64_t s = v.cs[t] + i % v.C0;
+  if (s >= v.ce[t]) return;
+  const double p0 = v.p01[2 * b], p1 = v.p01[2 * b + 1];
+  const double* m = means + (s + b + 1) * D;
+  double y[DY], f[DY], J[DY * DY];
+#pragma unroll
+  for (int k = 0; k < DY; ++k) y[k] = p0 * m[k * Q1];
+  field_eval<double, DY>(v.fld[b], params + 4 * b, y, f, J);
+#pragma unroll
+  for (int r = 0; r < DY; ++r) {
+    double h[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) h[k] = 0.0;
+#pragma unroll
+    for (int j = 0; j < DY; ++j) h[j * Q1] = -(J[r * DY + j] * p0);
+    h[r * Q1 + 1] += p1;
+    const double res = p1 * m[r * Q1 + 1] - f[r];
+    double hm = 0.0, ss = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) hm = fma(h[k], m[k], hm);
+#pragma unroll
+    for (int k = 0; k < D; ++k) ss = fma(h[k], h[k], ss);
+    const double inv = ss > 0.0 ? 1.0 / sqrt(ss) : 1.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) H[(s * DY + r) * D + k] = (float)(h[k] * inv);
+    c[s * DY + r] = (float)((res - hm) * inv);
+  }
+}
+
+template <int D, int DY>
+void batch_lin_mixed(const BView& v, const double* params, const double* means, float* H, float* c, cudaStream_t st) {
+  ProfScope ps(PK_LINEARIZE, st);
+  kb_lin_mixed<D, DY><<<grid_for(v.n1 * v.C0, 128), 128, 0, st>>>(v, params, means, H, c);
+}
+
+// Per-problem state of the float32 phase (doubles): iterations kept, best
+// and previous relative change, consecutive non-shrinking count, this
+// iteration's max |dy|, max |y|, non-finite flag, accept flag.
+enum Mixed32 : int { M_IT = 0, M_BEST, M_PREV, M_WORSE, M_DY, M_AY, M_BAD, M_ACCEPT, M_COUNT = 8 };
+
+// max |y_new - y_old| and max |y_old| over the problem's projected states
+// y = p0 m[i (q+1)] (the float32 candidate against the float64 iterate) and
+// a non-finite flag; one block per active problem (k_ychange per problem).
+template <int D, int DY>
+__global__ void kb_ychange(BView v, const float* __restrict__ mnew, const double* __restrict__ mold,
+                           double* __restrict__ mst) {
+  constexpr int Q1 = D / DY;
+  const int64_t k = blockIdx.x;
+  const int b = v.ap[k];
+  if (v.frozen[b]) return;
+  const double p0 = v.p01[2 * b];
+  const int64_t g0 = v.so[b] + b, g1 = v.so[b + 1] + b + 1;
+  double dy = 0.0, ay = 0.0;
+  int bad = 0;
+  for (int64_t idx = g0 * DY + threadIdx.x; idx < g1 * DY; idx += blockDim.x) {
+    const int64_t g = idx / DY;
+    const int i = (int)(idx % DY);
+    const double a = (double)mnew[g * D + i * Q1], o = mold[g * D + i * Q1];
+    bad |= !isfinite(a);
+    dy = fmax(dy, fabs(p0 * (a - o)));
+    ay = fmax(ay, fabs(p0 * o));
+  }
+  __shared__ double sdy[32], say[32];
+  __shared__ int sbad[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    dy = fmax(dy, __shfl_xor_sync(0xffffffffu, dy, o));
+    ay = fmax(ay, __shfl_xor_sync(0xffffffffu, ay, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sdy[w] = dy;
+    say[w] = ay;
+    sbad[w] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 1; j < nw; ++j) {
+      dy = fmax(dy, sdy[j]);
+      ay = fmax(ay, say[j]);
+      bad |= sbad[j];
+    }
+    double* m = mst + (int64_t)M_COUNT * b;
+    m[M_DY] = dy;
+    m[M_AY] = ay;
+    m[M_BAD] = bad ? 1.0 : 0.0;
+  }
+}
+
+// The float32 phase's stopping rules per problem (pof_ieks_solve_mixed):
+// a non-finite candidate is dropped and ends the phase; otherwise it is
+// kept; the phase ends when the relative change is below rtol_f32, after
+// three changes in a row that did not shrink, or after maxiters_f32 kept
+// iterations.  done32 marks the problems whose phase has ended.
+static __global__ void kb_ctl32(BView v, double* __restrict__ mst, int32_t* __restrict__ done32, int64_t maxiters_f32,
+                                double rtol_f32, int32_t* __restrict__ nactive) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= v.Ba) return;
+  const int b = v.ap[k];
+  if (done32[b]) return;
+  double* m = mst + (int64_t)M_COUNT * b;
+  if (m[M_BAD] != 0.0) {
+    m[M_ACCEPT] = 0.0;
+    done32[b] = 1;
+    return;
+  }
+  m[M_ACCEPT] = 1.0;
+  m[M_IT] += 1.0;
+  const double rel = m[M_AY] > 0.0 ? m[M_DY] / m[M_AY] : m[M_DY];
+  m[M_BEST] = rel < m[M_BEST] ? rel : m[M_BEST];
+  bool stop = rel < rtol_f32;
+  m[M_WORSE] = rel >= m[M_PREV] ? m[M_WORSE] + 1.0 : 0.0;
+  stop = stop || m[M_WORSE] >= 3.0 || m[M_IT] >= (double)maxiters_f32;
+  m[M_PREV] = rel;
+  if (stop)
+    done32[b] = 1;
+  else
+    atomicAdd(nactive, 1);
+}
+
+// Kept candidates become the float64 iterate; one block per active problem.
+template <int D>
+__global__ void kb_accept(BView v, const float* __restrict__ mnew, double* __restrict__ means,
+                          const double* __restrict__ mst) {
+  const int b = v.ap[blockIdx.x];
+  if (mst[(int64_t)M_COUNT * b + M_ACCEPT] == 0.0) return;
+  const int64_t g0 = v.so[b] + b, g1 = v.so[b + 1] + b + 1;
+  for (int64_t i = g0 * D + threadIdx.x; i < g1 * D; i += blockDim.x) means[i] = (double)mnew[i];
+}
+
+// End of the float32 phase: a problem whose best relative change never came
+// within 100 rtol_f32 (float32 too coarse for it) goes back to its input
+// trajectory, with no float32 iterations counted; one block per problem.
+template <int D>
+__global__ void kb_revert(const int64_t* __restrict__ so, double* __restrict__ mst, double rtol_f32,
+                          const double* __restrict__ keep, double* __restrict__ means) {
+  const int b = blockIdx.x;
+  double* m = mst + (int64_t)M_COUNT * b;
+  if (!(m[M_IT] > 0.0) || m[M_BEST] < 100.0 * rtol_f32) return;
+  const int64_t g0 = so[b] + b, g1 = so[b + 1] + b + 1;
+  for (int64_t i = g0 * D + threadIdx.x; i < g1 * D; i += blockDim.x) means[i] = keep[i];
+  __syncthreads();
+  if (threadIdx.x == 0) m[M_IT] = 0.0;
+}
+
+template <int D, int DY>
+void batch_ychange(const BView& v, const float* mnew, const double* mold, double* mst, cudaStream_t st) {
+  kb_ychange<D, DY><<<(unsigned)v.Ba, 256, 0, st>>>(v, mnew, mold, mst);
+}
+template <int D>
+void batch_accept(const BView& v, const float* mnew, double* means, const double* mst, cudaStream_t st) {
+  kb_accept<D><<<(unsigned)v.Ba, 256, 0, st>>>(v, mnew, means, mst);
+}
+template <int D>
+void batch_revert(int64_t B, const int64_t* so, double* mst, double rtol_f32, const double* keep, double* means,
+                  cudaStream_t st) {
+  kb_revert<D><<<(unsigned)B, 256, 0, st>>>(so, mst, rtol_f32, keep, means);
+}
+
+static __global__ void kb_init_mixed(double* __restrict__ mst, int64_t B) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= B * M_COUNT) return;
+  const int f = (int)(i % M_COUNT);
+  mst[i] = (f == M_BEST || f == M_PREV) ? 1e300 : 0.0;
+}
+
+static __global__ void kb_d2f(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
 // Type-erased arguments of one batched iteration (pointers of the plan's
 // element type T).
 struct BatchRaw {
@@ -529,21 +717,41 @@ struct BatchDriver {
     return reinterpret_cast<U*>(base + off);
   }
 
+  // One IEKS iteration: linearize at mold, filter and smooth into mnew,
+  // then the convergence test of every problem against mold.
   static void iteration(const BatchRaw& a, const void* mold, void* mnew, cudaStream_t st) {
+    cudaMemsetAsync(a.nactive, 0, sizeof(int32_t), st);
+    {
+      ProfScope ps(PK_LINEARIZE, st);
+      kb_linearize<T, D, DY><<<grid_for(a.v.n1 * a.v.C0, 128), 128, 0, st>>>(
+          a.v, static_cast<const T*>(a.params), static_cast<const T*>(mold), static_cast<T*>(a.H),
+          static_cast<T*>(a.c));
+    }
+    filtsmooth(a, mold, mnew, st);
+    {
+      ProfScope ps(PK_CONTROL, st);
+      kb_control<<<grid_for(a.v.Ba * 32, 128), 128, 0, st>>>(a.v, at<double>(a.lw, a.L->partials), a.pscal,
+                                                            a.frozen, a.maxiters, a.rtol, a.atol, a.nactive);
+    }
+  }
+
+  // Filter and smoother of the linear model in a.H, a.c (per-problem
+  // sigma^2 / NLL / objective sums into a.pscal; not-close counts against
+  // mold when given).
+  static void filtsmooth(const BatchRaw& a, const void* mold, void* mnew, cudaStream_t st) {
     if (a.team == TSN && TSN != TSW)
-      iteration_ts<TSN>(a, static_cast<const T*>(mold), static_cast<T*>(mnew), st);
+      filtsmooth_ts<TSN>(a, static_cast<const T*>(mold), static_cast<T*>(mnew), st);
     else
-      iteration_ts<TSW>(a, static_cast<const T*>(mold), static_cast<T*>(mnew), st);
+      filtsmooth_ts<TSW>(a, static_cast<const T*>(mold), static_cast<T*>(mnew), st);
   }
 
   template <int TS>
-  static void iteration_ts(const BatchRaw& a, const T* mold, T* mnew, cudaStream_t st) {
+  static void filtsmooth_ts(const BatchRaw& a, const T* mold, T* mnew, cudaStream_t st) {
     constexpr int TU = TSW;
     const BatchLevels& L = *a.L;
     const BView& v = a.v;
     char* lw = a.lw;
     const int64_t n1 = v.n1;
-    const T* params = static_cast<const T*>(a.params);
     const T* x0m = static_cast<const T*>(a.x0m);
     const T* x0L = static_cast<const T*>(a.x0L);
     const T* F = static_cast<const T*>(a.F);
@@ -553,11 +761,6 @@ struct BatchDriver {
     T* selem = static_cast<T*>(a.selem);
     T* chols = static_cast<T*>(a.chols);
     const int32_t* frozen = a.frozen;
-    cudaMemsetAsync(a.nactive, 0, sizeof(int32_t), st);
-    {
-      ProfScope ps(PK_LINEARIZE, st);
-      kb_linearize<T, D, DY><<<grid_for(n1 * v.C0, 128), 128, 0, st>>>(v, params, mold, H, c);
-    }
     {
       ProfScope ps(PK_FILT_L0_REDUCE, st);
       launch_team<L0WS, TS>(kb_filt_l0_reduce<T, D, DY, TS>, n1, st, v, F, QL, (const T*)H, (const T*)c,
@@ -616,11 +819,6 @@ struct BatchDriver {
                              a.calibrate ? (const double*)a.pscale : nullptr, mold, a.mrtol, a.matol,
                              at<double>(lw, L.partials));
     }
-    {
-      ProfScope ps(PK_CONTROL, st);
-      kb_control<<<grid_for(v.Ba * 32, 128), 128, 0, st>>>(v, at<double>(lw, L.partials), a.pscal, a.frozen,
-                                                          a.maxiters, a.rtol, a.atol, a.nactive);
-    }
   }
 
   static void finish(int64_t B, const int64_t* so, const double* pscal, const double* pscale, bool calibrate,
@@ -632,15 +830,24 @@ struct BatchDriver {
 
 struct BatchOps {
   void (*iteration)(const BatchRaw&, const void*, void*, cudaStream_t);
+  void (*filtsmooth)(const BatchRaw&, const void*, void*, cudaStream_t);
   void (*finish)(int64_t, const int64_t*, const double*, const double*, bool, void*, const void*, void*, double*,
                  cudaStream_t);
+  // float32 phase of the mixed-precision batch (float32 table only):
+  // float64 linearization at the float64 iterate into float32 rows
+  void (*lin_mixed)(const BView&, const double*, const double*, float*, float*, cudaStream_t);
+  void (*ychange)(const BView&, const float*, const double*, double*, cudaStream_t);
+  void (*accept)(const BView&, const float*, double*, const double*, cudaStream_t);
+  void (*revert)(int64_t, const int64_t*, double*, double, const double*, double*, cudaStream_t);
   int tsn, tsw;  // level-0 team sizes available (narrow, wide)
 };
 
 template <typename T, int D, int DY>
 const BatchOps* batch_ops_impl() {
-  static const BatchOps ops{&BatchDriver<T, D, DY>::iteration, &BatchDriver<T, D, DY>::finish,
-                            BatchDriver<T, D, DY>::TSN, BatchDriver<T, D, DY>::TSW};
+  static const BatchOps ops{&BatchDriver<T, D, DY>::iteration, &BatchDriver<T, D, DY>::filtsmooth,
+                            &BatchDriver<T, D, DY>::finish, &batch_lin_mixed<D, DY>, &batch_ychange<D, DY>,
+                            &batch_accept<D>, &batch_revert<D>, BatchDriver<T, D, DY>::TSN,
+                            BatchDriver<T, D, DY>::TSW};
   return &ops;
 }
 

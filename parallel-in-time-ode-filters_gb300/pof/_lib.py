@@ -93,6 +93,12 @@ _SIGS = {
         [_i32, _i64, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _i32, _dp, _vp,
          _sz, _vp],
     ),
+    "pof_batch_mixed_workspace_bytes": (_sz, [_i64, _vp, _i32, _i32, _i32, _i32]),
+    "pof_ieks_solve_batch_mixed": (
+        _c.c_int,
+        [_i64, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _f64, _i64, _i32, _i32, _i32, _dp,
+         _dp, _vp, _sz, _vp],
+    ),
 }
 
 PROFILE_KINDS = [

@@ -163,28 +163,57 @@ def prepare_batch(problems, order, device=None, init="constant"):
     }
 
 
-def run_batch(prep, means, chols, info, maxiters=10_000, calibrate=True, C0=0, Cg=0, dtype_code=_lib.POF_F64,
-              workspace=None):
-    """pof_ieks_solve_batch on prepared inputs; means (G, D) holds the initial
-    trajectories on entry and the results on return.  Returns the workspace
-    (reusable for the same batch)."""
-    lib = _lib.lib()
-    B, D, d = prep["B"], prep["D"], prep["d"]
+def _host(prep):
     ns = np.ascontiguousarray(prep["n_steps"], dtype=np.int64)
     fl = np.ascontiguousarray(prep["fields"], dtype=np.int32)
     hs = np.ascontiguousarray(prep["h"], dtype=np.float64)
-    vp = lambda a: a.ctypes.data_as(_lib.ctypes.c_void_p)  # noqa: E731
-    wsb = lib.pof_batch_workspace_bytes(dtype_code, B, vp(ns), D, d, int(C0), int(Cg))
+    return ns, fl, hs
+
+
+def _vp(a):
+    return a.ctypes.data_as(_lib.ctypes.c_void_p)
+
+
+def workspace_bytes(prep, precision="float64", C0=0, Cg=0):
+    lib = _lib.lib()
+    ns, _, _ = _host(prep)
+    if precision == "mixed":
+        wsb = lib.pof_batch_mixed_workspace_bytes(prep["B"], _vp(ns), prep["D"], prep["d"], int(C0), int(Cg))
+    else:
+        wsb = lib.pof_batch_workspace_bytes(_lib.POF_F64, prep["B"], _vp(ns), prep["D"], prep["d"], int(C0), int(Cg))
     if wsb == 0:
-        raise _lib.PofError("pof_batch_workspace_bytes refused the batch (shape (%d, %d) or sizes)" % (D, d))
+        raise _lib.PofError("the batch workspace query refused the batch (shape (%d, %d) or sizes)"
+                            % (prep["D"], prep["d"]))
+    return wsb
+
+
+def run_batch(prep, means, chols, info, maxiters=10_000, calibrate=True, C0=0, Cg=0, workspace=None,
+              precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, info_f32=None):
+    """pof_ieks_solve_batch (precision="float64") or
+    pof_ieks_solve_batch_mixed ("mixed") on prepared inputs; means (G, D)
+    holds the initial trajectories on entry and the results on return.
+    Returns the workspace (reusable for the same batch)."""
+    lib = _lib.lib()
+    B, D, d = prep["B"], prep["D"], prep["d"]
+    ns, fl, hs = _host(prep)
+    wsb = workspace_bytes(prep, precision, C0, Cg)
     if workspace is None or workspace.numel() < wsb:
         workspace = _lib.workspace(wsb, means.device)
-    rc = lib.pof_ieks_solve_batch(dtype_code, B, vp(ns), D, d, vp(fl), _lib.ptr(prep["params"]), vp(hs),
-                                  _lib.ptr(prep["x0m"]), _lib.ptr(prep["x0L"]), _lib.ptr(prep["F"]),
-                                  _lib.ptr(prep["QL"]), _lib.ptr(means), _lib.ptr(chols), int(maxiters),
-                                  int(bool(calibrate)), int(C0), int(Cg), _lib.ptr(info), _lib.ptr(workspace),
-                                  int(workspace.numel()), _lib.stream_handle())
-    _lib.check(rc, "pof_ieks_solve_batch")
+    common = (_lib.ptr(prep["params"]), _vp(hs), _lib.ptr(prep["x0m"]), _lib.ptr(prep["x0L"]), _lib.ptr(prep["F"]),
+              _lib.ptr(prep["QL"]), _lib.ptr(means), _lib.ptr(chols))
+    if precision == "mixed":
+        rc = lib.pof_ieks_solve_batch_mixed(B, _vp(ns), D, d, _vp(fl), *common, int(maxiters_f32), float(rtol_f32),
+                                            int(maxiters), int(bool(calibrate)), int(C0), int(Cg), _lib.ptr(info),
+                                            _lib.ptr(info_f32), _lib.ptr(workspace), int(workspace.numel()),
+                                            _lib.stream_handle())
+        _lib.check(rc, "pof_ieks_solve_batch_mixed")
+    elif precision == "float64":
+        rc = lib.pof_ieks_solve_batch(_lib.POF_F64, B, _vp(ns), D, d, _vp(fl), *common, int(maxiters),
+                                      int(bool(calibrate)), int(C0), int(Cg), _lib.ptr(info), _lib.ptr(workspace),
+                                      int(workspace.numel()), _lib.stream_handle())
+        _lib.check(rc, "pof_ieks_solve_batch")
+    else:
+        raise ValueError("precision must be 'float64' or 'mixed'")
     return workspace
 
 
@@ -198,10 +227,13 @@ def project(prep, means, chols):
     return means[:, idx] * p0[:, None], chols[:, idx, :] * p0[:, None, None]
 
 
-def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_000, C0=0, Cg=0):
+def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_000, C0=0, Cg=0,
+                precision="float64", maxiters_f32=10_000, rtol_f32=1e-5):
     """Solve every (field name, params, y0, ts) of ``problems`` with the
     parallel IEKS of pof.solver.solve (built-in fields, constant init).
-    Returns a BatchResult; ``result.problem(b)`` gives problem b's
+    precision="mixed": float32 iterations first, float64 polish after, per
+    problem (as pof.solver.solve's precision="mixed").  Returns a
+    BatchResult; ``result.problem(b)`` gives problem b's
     ((means (N_b, d), chol_covs (N_b, d, D)), info) as pof.solver.solve."""
     dev = default_device()
     prep = prepare_batch(problems, order, device=dev, init=init)
@@ -209,8 +241,12 @@ def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_00
     G, D = means.shape
     chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
     info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
-    run_batch(prep, means, chols, info, maxiters=maxiters, calibrate=calibrate, C0=C0, Cg=Cg)
+    info32 = torch.zeros(prep["B"], dtype=torch.float64, device=dev) if precision == "mixed" else None
+    run_batch(prep, means, chols, info, maxiters=maxiters, calibrate=calibrate, C0=C0, Cg=Cg, precision=precision,
+              maxiters_f32=maxiters_f32, rtol_f32=rtol_f32, info_f32=info32)
     ym, yc = project(prep, means, chols)
     info_d = {"iterations": info[:, _lib.I_ITERATIONS].to(torch.int64), "nll": info[:, _lib.I_NLL],
               "obj": info[:, _lib.I_OBJ], "sigma_squared": info[:, _lib.I_SSQ], "calibrated": bool(calibrate)}
+    if info32 is not None:
+        info_d["iterations_float32"] = info32.to(torch.int64)
     return BatchResult(ym, yc, prep["offsets"], info_d)
