@@ -56,6 +56,10 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "fhn_q3_N65536"
 MAXITERS = 10_000  # the reference's default (pof/solver.py:12)
 
+# DRAM bytes (read + write) per launch of a workload's dominant kernel from
+# one ncu capture (profiles/k_filt_l0_down_team_fhn_q3_N65536.md)
+NCU_TRAFFIC = {("fhn_q3_N65536", "filt_l0_down"): 56.600832e6 + 91.651840e6}
+
 
 def jprint(obj):
     print(json.dumps(obj), flush=True)
@@ -425,7 +429,7 @@ def run_gpu(args, workload):
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
                 "path": "pof.solver.solve(numpy y0, ts) -> means/chols .cpu()"},
         "roofline": {"bound": "fp64", "kernel": dom_kind, "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": NCU_TRAFFIC.get((workload, dom_kind)),
                      "peak_source": "measured on this GPU by pof_fp64_probe (FP64 FMA chains); "
                                     "MEASURED_PEAKS.json has no FP64 figure",
                      "flops_per_launch": dom_flops, "ms_per_launch": dom_ms_per_launch},
@@ -701,13 +705,160 @@ def cpu_sample_batch(problems, q, its, budget_s=20.0):
                       "per step-iteration x sum over instances of steps x the GPU's iteration count" % M}
 
 
+# ---------------------------------------------------------------------------
+# Served request stream: continuous batching against one-request-at-a-time
+# ---------------------------------------------------------------------------
+
+SERVE_WORKLOADS = {
+    # name: (requests per rate, arrival rates (requests/s), seed, maxiters)
+    "serve_stream": (96, (8.0, 32.0), 0, 300),
+}
+
+_SERVE_FIELDS = {
+    # field: (parameters, y0, t1) before the +-20 % jitter of the parameters
+    "logistic": ((3.0,), [0.01], 10.0),
+    "fhn_classic": ((0.2, 0.2, 3.0), [-1.0, 1.0], 100.0),
+    "lotkavolterra": ((1.5, 1.0, 3.0, 1.0), [1.0, 1.0], 10.0),
+    "vanderpol": ((10.0,), [2.0, 0.0], 6.3),
+}
+
+
+def serve_requests(R, seed):
+    """R requests: field uniform over logistic (d = 1), FitzHugh-Nagumo,
+    Lotka-Volterra, Van der Pol mu = 10 (d = 2); parameters jittered
+    uniformly within +-20 %; N log-uniform in [2^8, 2^16]; q in {2, 3, 4};
+    objective tolerance in {1e-4, 1e-6}."""
+    rng = np.random.default_rng(seed)
+    names = sorted(_SERVE_FIELDS)
+    out = []
+    for _ in range(R):
+        nm = names[rng.integers(len(names))]
+        p, y0, t1 = _SERVE_FIELDS[nm]
+        p = tuple(float(x) * rng.uniform(0.8, 1.2) for x in p)
+        N = int(np.floor(np.exp(rng.uniform(np.log(2 ** 8), np.log(2 ** 16)))))
+        q = int(rng.integers(2, 5))
+        tol = 1e-4 if rng.uniform() < 0.5 else 1e-6
+        out.append((nm, p, y0, np.linspace(0.0, t1, N), q, tol))
+    return out
+
+
+def run_serve(args, workload):
+    """Poisson arrivals at each rate; the continuous-batching server in real
+    time against the plain path (one pof_ieks_solve per request, first come
+    first served, the same arrival times)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from pof import _build, _lib, batch as pbatch, serve
+
+    _build.build(verbose=False)
+    lib = _lib.lib()
+    R, rates, seed, maxiters = SERVE_WORKLOADS[workload]
+    reqs = serve_requests(R, seed + rank)
+    steps_total = sum(len(r[3]) - 1 for r in reqs)
+    dev = torch.device("cuda", local)
+
+    # plain path: each request's solve time, one at a time
+    plain_t = []
+    for (nm, p, y0, ts, q, tol) in reqs:
+        prep = pbatch.prepare_batch([(nm, p, y0, ts)], q, device=dev)
+        n, D, d = int(prep["n_steps"][0]), prep["D"], prep["d"]
+        m = prep["means0"].clone()
+        c = torch.empty((n + 1, D, D), dtype=torch.float64, device=dev)
+        inf = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+        wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+        ws = _lib.workspace(wsb, dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.copy_(prep["means0"])
+        _lib.check(lib.pof_ieks_solve(_lib.POF_F64, n, D, d, int(prep["fields"][0]), _lib.ptr(prep["params"][0]),
+                                      float(prep["h"][0]), _lib.ptr(prep["x0m"][0]), _lib.ptr(prep["x0L"][0]),
+                                      _lib.ptr(prep["F"]), _lib.ptr(prep["QL"]), _lib.ptr(m), _lib.ptr(c),
+                                      maxiters, 1, _lib.ptr(inf), _lib.ptr(ws), wsb, _lib.stream_handle()),
+                   "pof_ieks_solve")
+        torch.cuda.synchronize()
+        plain_t.append(time.perf_counter() - t0)
+        del ws, m, c
+    # warm the server's engines (first use builds them)
+    srv = serve.Server(max_requests=256, max_points=1 << 21, device=dev)
+    for r in reqs[:6]:
+        nm, p, y0, ts, q, tol = r
+        srv.submit(nm, p, y0, ts[: min(len(ts), 300)], q, rtol=tol, maxiters=maxiters)
+    while srv.busy():
+        srv.tick()
+
+    lines = []
+    rng = np.random.default_rng(seed + 1000)
+    for rate in rates:
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=R))
+        # plain: first come first served on the measured solve times
+        fin = 0.0
+        lat_plain = []
+        for a, t in zip(arrivals, plain_t):
+            start = max(a, fin)
+            fin = start + t
+            lat_plain.append(fin - a)
+        makespan_plain = fin - arrivals[0]
+        # served, in real time
+        srv.results.clear()
+        t_start = time.perf_counter()
+        rid_of = {}
+        k = 0
+        while k < R or srv.busy():
+            now = time.perf_counter() - t_start
+            while k < R and arrivals[k] <= now:
+                nm, p, y0, ts, q, tol = reqs[k]
+                rid_of[srv.submit(nm, p, y0, ts, q, rtol=tol, maxiters=maxiters, t_arrival=t_start + arrivals[k])] = k
+                k += 1
+            if srv.busy():
+                srv.tick()
+            elif k < R:
+                time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t_start))))
+        lat = [srv.t_done[rid] - srv.t_submit[rid] for rid in rid_of]
+        makespan = max(srv.t_done[rid] for rid in rid_of) - (t_start + arrivals[0])
+        lines.append({
+            "rate_per_s": rate,
+            "served": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                       "throughput": steps_total / makespan, "makespan_s": makespan},
+            "plain_fifo": {"p50_s": float(np.percentile(lat_plain, 50)), "p99_s": float(np.percentile(lat_plain, 99)),
+                           "throughput": steps_total / makespan_plain, "makespan_s": makespan_plain},
+        })
+    srv.close()
+    if rank != 0:
+        return
+    best = max(lines, key=lambda x: x["served"]["throughput"])
+    jprint({
+        "metric": "IVP*steps/s and p50/p99 latency, served request stream (continuous batching, float64)",
+        "value": best["served"]["throughput"],
+        "unit": "IVP*steps/s",
+        "n_gpus": world,
+        "steps": R,
+        "warmup": 6,
+        "ms_per_step": None,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload, "requests_per_rate": R, "seed": seed, "maxiters": maxiters,
+                   "fields": "logistic, fhn_classic, lotkavolterra, vanderpol mu=10 (+-20 % parameters)",
+                   "N": "log-uniform in [2^8, 2^16]", "q": [2, 3, 4], "tolerances": [1e-4, 1e-6],
+                   "total_steps": steps_total,
+                   "omitted": "reaction-diffusion d = 128 (needs the dense D >= 128 combine, not built)"},
+        "rates": lines,
+        "plain_solve_s_total": float(sum(plain_t)),
+    })
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(SERVE_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--solves-only", action="store_true",
@@ -717,6 +868,8 @@ def main():
         run_reference(args, args.workload)
     elif args.workload in BATCH_WORKLOADS:
         run_gpu_batch(args, args.workload)
+    elif args.workload in SERVE_WORKLOADS:
+        run_serve(args, args.workload)
     else:
         run_gpu(args, args.workload)
 

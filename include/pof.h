@@ -44,7 +44,8 @@ enum {
   POF_ERR_WORKSPACE = -3, /* workspace smaller than *_workspace_bytes */
   POF_ERR_CUDA = -4,      /* a CUDA runtime call failed (see pof_last_cuda_error) */
   POF_ERR_FIELD = -5,     /* unknown built-in field or d mismatch */
-  POF_ERR_DTYPE = -6      /* dtype not POF_F64 / POF_F32 */
+  POF_ERR_DTYPE = -6,     /* dtype not POF_F64 / POF_F32 */
+  POF_ERR_BUSY = -7       /* no free request slot or memory right now (pof_server_submit) */
 };
 
 enum { POF_F64 = 0, POF_F32 = 1 };
@@ -278,6 +279,49 @@ int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int
                                const double* F, const double* QL, double* means, double* chols, int64_t maxiters_f32,
                                double rtol_f32, int64_t maxiters, int32_t calibrate, int32_t C0, int32_t Cg,
                                double* info, double* info_f32, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Continuous-batching engine (no reference counterpart): IEKS solves of one
+ * state shape (D, d) are admitted while others iterate.  Each tick runs one
+ * IEKS iteration (pof_ieks_solve's loop body, per request: own field,
+ * parameters, step, maxiters and objective rtol of crit) over every
+ * admitted, unfinished request with the batched segmented scan; finished
+ * requests leave the plan and their memory is reused.  A request's chunk
+ * length depends on its own step count only, so its result is bit-identical
+ * alone and in any mix.  The engine owns a CUDA stream (pof_server_stream);
+ * its calls are for one host thread.
+ *
+ * Memory: the caller's workspace, sized by pof_server_workspace_bytes for
+ * up to max_requests requests holding up to max_points grid points in total
+ * and level_bytes of scan levels (the admission budget: a request that does
+ * not fit is refused with POF_ERR_BUSY and can be submitted again later). */
+typedef struct pof_server pof_server;
+size_t pof_server_workspace_bytes(int32_t D, int32_t d, int64_t max_requests, int64_t max_points,
+                                  size_t level_bytes);
+/* F, QL: device (D, D) preconditioned IWP (the same for every step size). */
+int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_points, size_t level_bytes,
+                      const double* F, const double* QL, int32_t calibrate, void* workspace, size_t workspace_bytes,
+                      pof_server** out);
+int pof_server_destroy(pof_server* s);
+/* Admit a request (host arrays): field, params (4), step h, x0 (D) and its
+ * chol (D, D, NULL = 0) in preconditioned coordinates, the initial
+ * trajectory's row (D, repeated over the N = n_steps + 1 grid points:
+ * "constant" init), maxiters and the objective rtol of crit.  Returns the
+ * request's slot (>= 0) or a negative status (POF_ERR_BUSY: retry later). */
+int64_t pof_server_submit(pof_server* s, int64_t n_steps, int32_t field, const double* params, double h,
+                          const double* x0_mean, const double* x0_chol, const double* init_row, int64_t maxiters,
+                          double rtol);
+/* Enqueue `iterations` ticks; pof_server_sync waits for them and moves the
+ * requests that stopped to the finished list (n_running: still iterating). */
+int pof_server_launch(pof_server* s, int64_t iterations);
+int pof_server_sync(pof_server* s, int64_t* n_running);
+int pof_server_step(pof_server* s, int64_t iterations, int64_t* n_running);
+/* Up to cap slots that finished since the last poll. */
+int64_t pof_server_poll(pof_server* s, int64_t* slots_out, int64_t cap);
+/* Copy a finished request's result -- means (N, D), calibrated chols
+ * (N, D, D), info (POF_I_COUNT) into device arrays -- and free its slot. */
+int pof_server_fetch(pof_server* s, int64_t slot, double* means, double* chols, double* info);
+void* pof_server_stream(pof_server* s);
 
 #ifdef __cplusplus
 }

@@ -170,7 +170,7 @@ def ieks_step(setup, states, calibrate=True, sequential=False, scan=associative_
 
 
 def solve(ivp, ts, order, init="prior", calibrate=True, maxiters=10_000, sequential=False,
-          scan=associative_scan, return_full=False, callback=None, filtsmooth_fn=None):
+          scan=associative_scan, return_full=False, callback=None, filtsmooth_fn=None, rtol=1e-6):
     """``solver.py:11-73``: returns ((means (N,d), chols (N,d,D)), info)."""
     setup = set_up_solver(ivp, ts, order)
     states = get_initial_trajectory(setup, method=init)
@@ -181,7 +181,7 @@ def solve(ivp, ts, order, init="prior", calibrate=True, maxiters=10_000, sequent
         # cond (solver.py:36-45)
         first = k < 1
         not_max = k <= maxiters
-        conv = crit(obj, obj_old, nll, nll_old, states[0], states_old[0])
+        conv = crit(obj, obj_old, nll, nll_old, states[0], states_old[0], rtol=rtol)
         if not (first or ((not conv) and not_max)):
             break
         # body (solver.py:47-55)

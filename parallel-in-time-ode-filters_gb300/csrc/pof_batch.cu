@@ -69,7 +69,7 @@ struct BatchCtx {
   BatchShape sh;
   BatchPersist P;
   BatchLevels L;
-  std::vector<int64_t> so;
+  std::vector<int64_t> gb;  // first grid point of each problem
   std::vector<int32_t> active;
   std::vector<unsigned char> tab;
   char* w = nullptr;   // persistent part
@@ -83,13 +83,18 @@ struct BatchCtx {
     if (rc) return rc;
     B = B_;
     n_steps = ns;
-    P = batch_persist(B, ns, D, d, dtype == POF_F32 ? 4 : 8);
-    sh = batch_shape(dtype, D, d, C0, Cg, P.n, ops);
-    so.assign(B + 1, 0);
-    for (int64_t b = 0; b < B; ++b) so[b + 1] = so[b] + ns[b];
+    gb.assign(B, 0);
+    int64_t G = 0, steps = 0;
+    for (int64_t b = 0; b < B; ++b) {
+      gb[b] = G;
+      G += ns[b] + 1;
+      steps += ns[b];
+    }
+    P = batch_persist(B, G, D, d, dtype == POF_F32 ? 4 : 8);
+    sh = batch_shape(dtype, D, d, C0, Cg, steps, ops);
     active.resize(B);
     for (int64_t b = 0; b < B; ++b) active[b] = (int32_t)b;
-    L = batch_levels(sh, active, ns, so.data(), &tab);
+    L = batch_levels(sh, active, ns, gb.data(), nullptr, &tab);
     if (L.cnt[L.nlev] != L.Ba) return POF_ERR_ARG;  // a problem too long for kMaxLevels levels
     return POF_OK;
   }
@@ -101,7 +106,8 @@ struct BatchCtx {
     w = base;
     lw = base + align_up(P.total);
     std::vector<unsigned char> ptab(P.host_tab_bytes, 0);
-    memcpy(ptab.data() + (P.so - P.host_tab), so.data(), sizeof(int64_t) * (B + 1));
+    memcpy(ptab.data() + (P.gb - P.host_tab), gb.data(), sizeof(int64_t) * B);
+    memcpy(ptab.data() + (P.ns - P.host_tab), n_steps, sizeof(int64_t) * B);
     memcpy(ptab.data() + (P.fld - P.host_tab), fields, sizeof(int32_t) * B);
     double* p01 = reinterpret_cast<double*>(ptab.data() + (P.p01 - P.host_tab));
     for (int64_t b = 0; b < B; ++b)
@@ -135,8 +141,11 @@ struct BatchCtx {
     if (!rc) rc = cuda_status(cudaStreamSynchronize(st));
     a.L = &L;
     BView& v = a.v;
-    v.so = reinterpret_cast<const int64_t*>(w + P.so);
+    v.gb = reinterpret_cast<const int64_t*>(w + P.gb);
+    v.ns = reinterpret_cast<const int64_t*>(w + P.ns);
     v.fld = reinterpret_cast<const int32_t*>(w + P.fld);
+    v.rtol = nullptr;
+    v.maxit = nullptr;
     v.p01 = reinterpret_cast<const double*>(w + P.p01);
     v.frozen = a.frozen;
     v.ap = reinterpret_cast<const int32_t*>(lw + L.ap);
@@ -144,7 +153,7 @@ struct BatchCtx {
     v.cs = reinterpret_cast<const int64_t*>(lw + L.cs);
     v.ce = reinterpret_cast<const int64_t*>(lw + L.ce);
     v.cp = reinterpret_cast<const int32_t*>(lw + L.cp);
-    v.n = P.n;
+    v.n = P.G;
     v.n1 = L.cnt[1];
     v.Ba = L.Ba;
     v.C0 = L.C0max;
@@ -168,7 +177,7 @@ struct BatchCtx {
       }
     if (still.empty() || 2 * steps >= L.steps) return POF_OK;
     active.swap(still);
-    L = batch_levels(sh, active, n_steps, so.data(), &tab);
+    L = batch_levels(sh, active, n_steps, gb.data(), nullptr, &tab);
     *replanned = true;
     return set_plan(st);
   }
@@ -317,7 +326,7 @@ int pof_ieks_solve_batch(int32_t dtype, int64_t B, const int64_t* n_steps, int32
   void* bufs[2] = {means, c.w + c.P.means2};
   rc = loop_f64(c, bufs, maxiters, st);
   if (rc) return rc;
-  c.ops->finish(B, c.a.v.so, c.a.pscal, c.a.pscale, c.a.calibrate, means, bufs[1], chols, info, st);
+  c.ops->finish(B, c.a.v.gb, c.a.v.ns, c.a.pscal, c.a.pscale, c.a.calibrate, means, bufs[1], chols, info, st);
   return launch_status();
 }
 
@@ -410,7 +419,7 @@ int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int
       if (!rc && replanned && use_graph) rc = c32.capture(st, body);
     }
     if (rc) return rc;
-    c32.ops->revert(B, c32.a.v.so, mst, rtol_f32, keep, means, st);
+    c32.ops->revert(B, c32.a.v.gb, c32.a.v.ns, mst, rtol_f32, keep, means, st);
   }
 
   // float64 polish: the reference loop per problem from the kept iterates
@@ -425,7 +434,8 @@ int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int
   void* bufs[2] = {means, c64.w + c64.P.means2};
   rc = loop_f64(c64, bufs, maxiters, st);
   if (rc) return rc;
-  c64.ops->finish(B, c64.a.v.so, c64.a.pscal, c64.a.pscale, c64.a.calibrate, means, bufs[1], chols, info, st);
+  c64.ops->finish(B, c64.a.v.gb, c64.a.v.ns, c64.a.pscal, c64.a.pscale, c64.a.calibrate, means, bufs[1], chols, info,
+                  st);
   if (info_f32) {
     rc = cuda_status(cudaMemcpy2DAsync(info_f32, sizeof(double), mst + M_IT, sizeof(double) * M_COUNT, sizeof(double),
                                        B, cudaMemcpyDeviceToDevice, st));

@@ -12,7 +12,8 @@ namespace pof {
 
 // Device view of the tables of a plan (persistent + level part).
 struct BView {
-  const int64_t* so;      // (B + 1)
+  const int64_t* gb;      // (B) first grid point of each problem (= index of its first step)
+  const int64_t* ns;      // (B) steps of each problem
   const int32_t* fld;     // (B)
   const double* p01;      // (B, 2)
   const int32_t* frozen;  // (B)
@@ -21,7 +22,9 @@ struct BView {
   const int64_t* cs;      // (n1)
   const int64_t* ce;      // (n1)
   const int32_t* cp;      // (n1)
-  int64_t n;              // global steps (SoA stride of the smoother elements)
+  const double* rtol;     // (B) objective rtol of crit per problem, or null (a shared value)
+  const int64_t* maxit;   // (B) maxiters per problem, or null (a shared value)
+  int64_t n;              // grid points of the index space (SoA stride of the smoother elements)
   int64_t n1;             // level-0 chunks
   int64_t Ba;             // problems of the plan
   int C0;                 // longest chunk
@@ -51,7 +54,7 @@ __global__ void kb_linearize(BView v, const T* __restrict__ params, const T* __r
   const int64_t s = v.cs[t] + i % v.C0;
   if (s >= v.ce[t]) return;
   const T p0 = (T)v.p01[2 * b], p1 = (T)v.p01[2 * b + 1];
-  const T* m = means + (s + b + 1) * D;
+  const T* m = means + (s + 1) * D;
   T y[DY], f[DY], J[DY * DY];
 #pragma unroll
   for (int k = 0; k < DY; ++k) y[k] = p0 * m[k * Q1];
@@ -193,8 +196,8 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
   t_load_state<T, TS, D>(tm, states1, v.n1, t, w.m, w.L);
   tm.sync();
   t_inv_lower<T, TS, D>(tm, w.QL, ws_.QLi);
-  if (s0 == v.so[b]) {  // first chunk of the problem: its grid point 0 holds x0
-    const int64_t g = s0 + b;
+  if (s0 == v.gb[b]) {  // first chunk of the problem: its grid point 0 holds x0
+    const int64_t g = s0;
     for (int f = tm.r; f < D + D * D; f += TS) {
       if (f < D)
         means[g * D + f] = w.m[f];
@@ -221,7 +224,7 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
         val = w.Y[((f - GL::DM) / D) * L2 + D + (f - GL::DM) % D];
       selems[f * n + s] = val;
     }
-    const int64_t g = s + b + 1;
+    const int64_t g = s + 1;
     for (int f = tm.r; f < D + D * D; f += TS) {
       if (f < D)
         means[g * D + f] = w.m[f];
@@ -288,7 +291,7 @@ __global__ void kb_smo_top(BView v, const T* __restrict__ means, const T* __rest
   if (t >= v.Ba) return;
   const int b = v.ap[t];
   if (v.frozen[b]) return;
-  const int64_t g = v.so[b + 1] + b;
+  const int64_t g = v.gb[b] + v.ns[b];
   for (int f = tm.r; f < D + D * D; f += TS) {
     const T val = (f < D) ? means[g * D + f] : chols[g * D * D + f - D];
     ends[f * v.Ba + t] = val;
@@ -358,8 +361,8 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
       notclose += ok ? 0.0 : 1.0;
     }
   };
-  if (s1 == v.so[b + 1]) {  // last chunk: the terminal grid point
-    const int64_t g = s1 + b;
+  if (s1 == v.gb[b] + v.ns[b]) {  // last chunk: the terminal grid point
+    const int64_t g = s1;
     close_count(g);
     if (scale)
       for (int f = tm.r; f < D * D; f += TS) chols[g * D * D + f] = w.D1[(f / D) * L1 + f % D] * sc;
@@ -370,7 +373,7 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
     tm.sync();
     t_smooth_apply<T, TS, D>(tm, w);
     sobj += (double)t_objective<T, TS, D>(tm, ws_.F, ws_.QLi, w.g1, ws_.mnext, ws_.r);
-    const int64_t g = k + b;
+    const int64_t g = k;
     close_count(g);
     for (int f = tm.r; f < D + D * D; f += TS) {
       if (f < D)
@@ -414,7 +417,7 @@ static __global__ void kb_fin_filter(BView v, const double* __restrict__ partial
   const double nll = warp_chunk_sum(partials + P_NLL * v.n1, c0, c1, lane);
   const double fobj = warp_chunk_sum(partials + P_FOBJ * v.n1, c0, c1, lane);
   if (lane == 0) {
-    const double nb = (double)(v.so[b + 1] - v.so[b]);
+    const double nb = (double)v.ns[b];
     const double s = ssq / nb / (double)DY;
     double* sc = pscal + (int64_t)kBatchScalars * b;
     sc[S_SSQ] = s;
@@ -447,6 +450,8 @@ static __global__ void kb_control(BView v, const double* __restrict__ partials, 
   sc[S_ITER] = it;
   const double obj = sobj, nll = sc[S_NLL], oo = sc[S_OBJ_OLD];
   const bool nan = isnan(obj) || isnan(nll);
+  if (v.rtol) rtol = v.rtol[b];
+  if (v.maxit) maxiters = v.maxit[b];
   bool objc;
   if (isfinite(oo) && isfinite(obj))
     objc = fabs(oo - obj) <= atol + rtol * fabs(obj);
@@ -468,12 +473,13 @@ static __global__ void kb_control(BView v, const double* __restrict__ partials, 
 // iterations), the final calibration of the returned chol
 // (pof/solver.py:66-69), and info[b] = (iterations, nll, obj, sigma^2).
 template <typename T>
-__global__ void kb_finish(const int64_t* __restrict__ so, const double* __restrict__ pscal,
-                          const double* __restrict__ pscale, int D, int calibrate, T* __restrict__ means,
-                          const T* __restrict__ means2, T* __restrict__ chols, double* __restrict__ info) {
+__global__ void kb_finish(const int64_t* __restrict__ gb, const int64_t* __restrict__ ns,
+                          const double* __restrict__ pscal, const double* __restrict__ pscale, int D, int calibrate,
+                          T* __restrict__ means, const T* __restrict__ means2, T* __restrict__ chols,
+                          double* __restrict__ info) {
   const int b = blockIdx.x;
   const double* sc = pscal + (int64_t)kBatchScalars * b;
-  const int64_t g0 = so[b] + b, g1 = so[b + 1] + b + 1;
+  const int64_t g0 = gb[b], g1 = gb[b] + ns[b] + 1;
   const long long it = (long long)sc[S_ITER];
   if (it & 1)
     for (int64_t i = g0 * D + threadIdx.x; i < g1 * D; i += blockDim.x) means[i] = means2[i];
@@ -509,7 +515,7 @@ __global__ void kb_lin_mixed(BView v, const double* __restrict__ params, const d
   const int64_t s = v.cs[t] + i % v.C0;
   if (s >= v.ce[t]) return;
   const double p0 = v.p01[2 * b], p1 = v.p01[2 * b + 1];
-  const double* m = means + (s + b + 1) * D;
+  const double* m = means + (s + 1) * D;
   double y[DY], f[DY], J[DY * DY];
 #pragma unroll
   for (int k = 0; k < DY; ++k) y[k] = p0 * m[k * Q1];
@@ -557,7 +563,7 @@ __global__ void kb_ychange(BView v, const float* __restrict__ mnew, const double
   const int b = v.ap[k];
   if (v.frozen[b]) return;
   const double p0 = v.p01[2 * b];
-  const int64_t g0 = v.so[b] + b, g1 = v.so[b + 1] + b + 1;
+  const int64_t g0 = v.gb[b], g1 = v.gb[b] + v.ns[b] + 1;
   double dy = 0.0, ay = 0.0;
   int bad = 0;
   for (int64_t idx = g0 * DY + threadIdx.x; idx < g1 * DY; idx += blockDim.x) {
@@ -632,7 +638,7 @@ __global__ void kb_accept(BView v, const float* __restrict__ mnew, double* __res
                           const double* __restrict__ mst) {
   const int b = v.ap[blockIdx.x];
   if (mst[(int64_t)M_COUNT * b + M_ACCEPT] == 0.0) return;
-  const int64_t g0 = v.so[b] + b, g1 = v.so[b + 1] + b + 1;
+  const int64_t g0 = v.gb[b], g1 = v.gb[b] + v.ns[b] + 1;
   for (int64_t i = g0 * D + threadIdx.x; i < g1 * D; i += blockDim.x) means[i] = (double)mnew[i];
 }
 
@@ -640,12 +646,12 @@ __global__ void kb_accept(BView v, const float* __restrict__ mnew, double* __res
 // within 100 rtol_f32 (float32 too coarse for it) goes back to its input
 // trajectory, with no float32 iterations counted; one block per problem.
 template <int D>
-__global__ void kb_revert(const int64_t* __restrict__ so, double* __restrict__ mst, double rtol_f32,
-                          const double* __restrict__ keep, double* __restrict__ means) {
+__global__ void kb_revert(const int64_t* __restrict__ gb, const int64_t* __restrict__ ns, double* __restrict__ mst,
+                          double rtol_f32, const double* __restrict__ keep, double* __restrict__ means) {
   const int b = blockIdx.x;
   double* m = mst + (int64_t)M_COUNT * b;
   if (!(m[M_IT] > 0.0) || m[M_BEST] < 100.0 * rtol_f32) return;
-  const int64_t g0 = so[b] + b, g1 = so[b + 1] + b + 1;
+  const int64_t g0 = gb[b], g1 = gb[b] + ns[b] + 1;
   for (int64_t i = g0 * D + threadIdx.x; i < g1 * D; i += blockDim.x) means[i] = keep[i];
   __syncthreads();
   if (threadIdx.x == 0) m[M_IT] = 0.0;
@@ -660,9 +666,9 @@ void batch_accept(const BView& v, const float* mnew, double* means, const double
   kb_accept<D><<<(unsigned)v.Ba, 256, 0, st>>>(v, mnew, means, mst);
 }
 template <int D>
-void batch_revert(int64_t B, const int64_t* so, double* mst, double rtol_f32, const double* keep, double* means,
-                  cudaStream_t st) {
-  kb_revert<D><<<(unsigned)B, 256, 0, st>>>(so, mst, rtol_f32, keep, means);
+void batch_revert(int64_t B, const int64_t* gb, const int64_t* ns, double* mst, double rtol_f32, const double* keep,
+                  double* means, cudaStream_t st) {
+  kb_revert<D><<<(unsigned)B, 256, 0, st>>>(gb, ns, mst, rtol_f32, keep, means);
 }
 
 static __global__ void kb_init_mixed(double* __restrict__ mst, int64_t B) {
@@ -821,9 +827,9 @@ struct BatchDriver {
     }
   }
 
-  static void finish(int64_t B, const int64_t* so, const double* pscal, const double* pscale, bool calibrate,
-                     void* means, const void* means2, void* chols, double* info, cudaStream_t st) {
-    kb_finish<T><<<(unsigned)B, 256, 0, st>>>(so, pscal, pscale, D, calibrate ? 1 : 0, static_cast<T*>(means),
+  static void finish(int64_t B, const int64_t* gb, const int64_t* ns, const double* pscal, const double* pscale,
+                     bool calibrate, void* means, const void* means2, void* chols, double* info, cudaStream_t st) {
+    kb_finish<T><<<(unsigned)B, 256, 0, st>>>(gb, ns, pscal, pscale, D, calibrate ? 1 : 0, static_cast<T*>(means),
                                               static_cast<const T*>(means2), static_cast<T*>(chols), info);
   }
 };
@@ -831,14 +837,14 @@ struct BatchDriver {
 struct BatchOps {
   void (*iteration)(const BatchRaw&, const void*, void*, cudaStream_t);
   void (*filtsmooth)(const BatchRaw&, const void*, void*, cudaStream_t);
-  void (*finish)(int64_t, const int64_t*, const double*, const double*, bool, void*, const void*, void*, double*,
-                 cudaStream_t);
+  void (*finish)(int64_t, const int64_t*, const int64_t*, const double*, const double*, bool, void*, const void*,
+                 void*, double*, cudaStream_t);
   // float32 phase of the mixed-precision batch (float32 table only):
   // float64 linearization at the float64 iterate into float32 rows
   void (*lin_mixed)(const BView&, const double*, const double*, float*, float*, cudaStream_t);
   void (*ychange)(const BView&, const float*, const double*, double*, cudaStream_t);
   void (*accept)(const BView&, const float*, double*, const double*, cudaStream_t);
-  void (*revert)(int64_t, const int64_t*, double*, double, const double*, double*, cudaStream_t);
+  void (*revert)(int64_t, const int64_t*, const int64_t*, double*, double, const double*, double*, cudaStream_t);
   int tsn, tsw;  // level-0 team sizes available (narrow, wide)
 };
 

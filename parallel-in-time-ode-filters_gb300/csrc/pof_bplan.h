@@ -2,9 +2,10 @@
 // shape (D, d), each with its own number of steps, step size, field and
 // parameters, solved by one pipeline of launches.  Host-only.
 //
-// Problem b owns the global steps [so[b], so[b+1]) and the grid points
-// [so[b] + b, so[b+1] + b] of the concatenated trajectory (grid index of the
-// state after global step s of problem b: s + b + 1).  The chunked scan of
+// Problem b owns the grid points [gb[b], gb[b] + ns[b]] of the concatenated
+// trajectories and the steps [gb[b], gb[b] + ns[b]): step s maps grid point
+// s to s + 1 (one index space for steps and grid points; the last index of
+// each problem's range is a grid point with no step).  The chunked scan of
 // the one-problem path is applied per problem: level-0 chunks and the groups
 // of every level above never span two problems, and a problem's tree ends in
 // a single element per problem at the top level, where its x0 (filter) and
@@ -39,18 +40,19 @@ struct BatchShape {
 
 // Persistent part, fixed for the life of a batch.
 struct BatchPersist {
-  int64_t B = 0, n = 0, G = 0;  // problems, global steps, grid points
-  size_t so = 0;                // (B + 1) int64 first global step of each problem
+  int64_t B = 0, n = 0, G = 0;  // problems, steps, grid points (the index space)
+  size_t gb = 0;                // (B) int64 first grid point of each problem
+  size_t ns = 0;                // (B) int64 steps of each problem
   size_t fld = 0;               // (B) int32 field id
   size_t p01 = 0;               // (B, 2) double Nordsieck scales
   size_t pscal = 0;             // (B, kBatchScalars) double
   size_t pscale = 0;            // (B) double sqrt(sigma^2) of the latest filter
   size_t frozen = 0;            // (B) int32
   size_t nactive = 0;           // int32 (+ pad)
-  size_t H = 0, c = 0;          // (n, d, D), (n, d)
-  size_t selem = 0;             // smoother elements, SoA with stride n
+  size_t H = 0, c = 0;          // (G, d, D), (G, d) indexed by step
+  size_t selem = 0;             // smoother elements, SoA with stride G
   size_t means2 = 0;            // (G, D) second iterate buffer
-  size_t host_tab = 0, host_tab_bytes = 0;  // so | fld | p01 (one upload)
+  size_t host_tab = 0, host_tab_bytes = 0;  // gb | ns | fld | p01 (one upload)
   size_t total = 0;
 };
 
@@ -72,13 +74,13 @@ struct BatchLevels {
   size_t total = 0;
 };
 
-inline BatchPersist batch_persist(int64_t B, const int64_t* n_steps, int D, int DY, int esz) {
+// Persistent part of a batch whose index space has G grid points (at least
+// sum(n_steps) + B; more when problems sit in an arena with free space).
+inline BatchPersist batch_persist(int64_t B, int64_t G, int D, int DY, int esz) {
   BatchPersist p;
   p.B = B;
-  int64_t n = 0;
-  for (int64_t b = 0; b < B; ++b) n += n_steps[b];
-  p.n = n;
-  p.G = n + B;
+  p.n = G - B;
+  p.G = G;
   const int64_t NG = D + 2LL * D * D;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -88,7 +90,8 @@ inline BatchPersist batch_persist(int64_t B, const int64_t* n_steps, int D, int 
   };
   // the host-built tables first, contiguous, so they go up in one copy
   p.host_tab = off;
-  p.so = take(sizeof(int64_t) * (B + 1));
+  p.gb = take(sizeof(int64_t) * B);
+  p.ns = take(sizeof(int64_t) * B);
   p.fld = take(sizeof(int32_t) * B);
   p.p01 = take(sizeof(double) * 2 * B);
   p.host_tab_bytes = off - p.host_tab;
@@ -96,10 +99,10 @@ inline BatchPersist batch_persist(int64_t B, const int64_t* n_steps, int D, int 
   p.pscale = take(sizeof(double) * B);
   p.frozen = take(sizeof(int32_t) * B);
   p.nactive = take(16);
-  p.H = take((size_t)esz * DY * D * n);
-  p.c = take((size_t)esz * DY * n);
-  p.selem = take((size_t)esz * NG * n);
-  p.means2 = take((size_t)esz * D * p.G);
+  p.H = take((size_t)esz * DY * D * G);
+  p.c = take((size_t)esz * DY * G);
+  p.selem = take((size_t)esz * NG * G);
+  p.means2 = take((size_t)esz * D * G);
   p.total = off;
   return p;
 }
@@ -114,27 +117,32 @@ inline int batch_pick_c0(int64_t total_steps, int lanes) {
   return c;
 }
 
-// Level tables of the plan over `active` (problem ids, in order).  When
-// `tab` is non-null it receives the tables' bytes (tab_bytes), laid out as
-// in the workspace from the start of the level part.
+// Level tables of the plan over `active` (problem ids, in order); problem b
+// has n_steps[b] steps from index gb[b], in chunks of c0[b] steps (sh.C0
+// for every problem when c0 is null).  When `tab` is non-null it receives
+// the tables' bytes (tab_bytes), laid out as in the workspace from the
+// start of the level part.
 inline BatchLevels batch_levels(const BatchShape& sh, const std::vector<int32_t>& active, const int64_t* n_steps,
-                                const int64_t* so, std::vector<unsigned char>* tab) {
+                                const int64_t* gb, const int32_t* c0, std::vector<unsigned char>* tab) {
   BatchLevels L;
   const int64_t Ba = (int64_t)active.size();
   L.Ba = Ba;
-  const int C0 = sh.C0;
   const int Cg = sh.Cg > 1 ? sh.Cg : 2;
+  auto chunk = [&](int32_t b) -> int64_t { return c0 ? c0[b] : sh.C0; };
   // per-problem element counts per level
   std::vector<int64_t> cur(Ba);
   int64_t n1 = 0, steps = 0;
+  int c0max = 1;
   for (int64_t k = 0; k < Ba; ++k) {
     const int64_t nb = n_steps[active[k]];
-    cur[k] = (nb + C0 - 1) / C0;
+    const int64_t C = chunk(active[k]);
+    cur[k] = (nb + C - 1) / C;
     n1 += cur[k];
     steps += nb;
+    c0max = C > c0max ? (int)C : c0max;
   }
   L.steps = steps;
-  L.C0max = C0;
+  L.C0max = c0max;
   L.cnt[1] = n1;
   int l = 1;
   std::vector<std::vector<int64_t>> per_level;  // counts per problem, per level
@@ -190,11 +198,12 @@ inline BatchLevels batch_levels(const BatchShape& sh, const std::vector<int32_t>
     int64_t c = 0;
     for (int64_t k = 0; k < Ba; ++k) {
       const int32_t b = active[k];
+      const int64_t C = chunk(b), s1 = gb[b] + n_steps[b];
       ap[k] = b;
       pc[k] = c;
-      for (int64_t s = so[b]; s < so[b + 1]; s += C0, ++c) {
+      for (int64_t s = gb[b]; s < s1; s += C, ++c) {
         cs[c] = s;
-        ce[c] = (s + C0 < so[b + 1]) ? s + C0 : so[b + 1];
+        ce[c] = (s + C < s1) ? s + C : s1;
         cp[c] = b;
       }
     }

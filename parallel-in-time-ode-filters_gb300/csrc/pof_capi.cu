@@ -182,6 +182,7 @@ const char* pof_status_string(int status) {
     case POF_ERR_CUDA: return "CUDA runtime error";
     case POF_ERR_FIELD: return "unknown built-in field or dimension mismatch";
     case POF_ERR_DTYPE: return "unsupported dtype";
+    case POF_ERR_BUSY: return "no free request slot or memory (retry later)";
     default: return "unknown status";
   }
 }

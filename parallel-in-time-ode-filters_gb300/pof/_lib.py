@@ -93,6 +93,16 @@ _SIGS = {
         [_i32, _i64, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _i32, _dp, _vp,
          _sz, _vp],
     ),
+    "pof_server_workspace_bytes": (_sz, [_i32, _i32, _i64, _i64, _sz]),
+    "pof_server_create": (_c.c_int, [_i32, _i32, _i64, _i64, _sz, _vp, _vp, _i32, _vp, _sz, _vp]),
+    "pof_server_destroy": (_c.c_int, [_vp]),
+    "pof_server_submit": (_i64, [_vp, _i64, _i32, _vp, _f64, _vp, _vp, _vp, _i64, _f64]),
+    "pof_server_launch": (_c.c_int, [_vp, _i64]),
+    "pof_server_sync": (_c.c_int, [_vp, _vp]),
+    "pof_server_step": (_c.c_int, [_vp, _i64, _vp]),
+    "pof_server_poll": (_i64, [_vp, _vp, _i64]),
+    "pof_server_fetch": (_c.c_int, [_vp, _i64, _vp, _vp, _dp]),
+    "pof_server_stream": (_vp, [_vp]),
     "pof_batch_mixed_workspace_bytes": (_sz, [_i64, _vp, _i32, _i32, _i32, _i32]),
     "pof_ieks_solve_batch_mixed": (
         _c.c_int,
@@ -140,6 +150,9 @@ def lib():
 
 def exported_symbols():
     return list(_SIGS)
+
+
+POF_ERR_BUSY = -7
 
 
 def check(rc, what=""):

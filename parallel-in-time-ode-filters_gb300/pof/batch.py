@@ -109,14 +109,10 @@ class BatchResult(NamedTuple):
         return (self.mean[s:e], self.chol[s:e]), info
 
 
-def prepare_batch(problems, order, device=None, init="constant"):
-    """Device inputs of pof_ieks_solve_batch for problems = [(field name,
-    params, y0, ts), ...] (uniform grids ts; the step is ts[1] - ts[0] as in
-    pof.convenience.set_up_solver).  Returns a dict of tensors and host
-    arrays."""
-    if init != "constant":
-        raise NotImplementedError("solve_batch supports init='constant'")
-    dev = device or default_device()
+def prepare_rows(problems, order):
+    """Per-problem set-up on the host (CPU tensors): x0 (B, D) (Taylor mode,
+    times P^-1), the constant-init row (B, D) [y0, f(y0), 0, ...] times
+    P^-1, steps, step sizes, field ids, parameters (B, 4), P[0, 0]."""
     B = len(problems)
     names = [p[0] for p in problems]
     d = _DIM[names[0]]
@@ -149,17 +145,30 @@ def prepare_batch(problems, order, device=None, init="constant"):
     row[:, :, 0] = y0
     row[:, :, 1] = derivs[:, 1, :]
     row = (row * PI_t[:, None, :]).reshape(B, D)
+    return {"B": B, "D": D, "d": d, "q": q, "n_steps": n_steps, "fields": fields, "h": hs, "params": params,
+            "x0m": x0m, "row": row, "p0": torch.as_tensor(P[:, 0])}
+
+
+def prepare_batch(problems, order, device=None, init="constant"):
+    """Device inputs of pof_ieks_solve_batch for problems = [(field name,
+    params, y0, ts), ...] (uniform grids ts; the step is ts[1] - ts[0] as in
+    pof.convenience.set_up_solver).  Returns a dict of tensors and host
+    arrays."""
+    if init != "constant":
+        raise NotImplementedError("solve_batch supports init='constant'")
+    dev = device or default_device()
+    r = prepare_rows(problems, order)
+    B, D, d, q, n_steps = r["B"], r["D"], r["d"], r["q"], r["n_steps"]
     counts = torch.as_tensor(n_steps + 1)
-    means0 = torch.repeat_interleave(row, counts, dim=0)
+    means0 = torch.repeat_interleave(r["row"], counts, dim=0)
     iwp = IWP(num_derivatives=q, wiener_process_dimension=d)
     F, QL = preconditioned_discretize(iwp, device=dev)
     offsets = np.concatenate([[0], np.cumsum(n_steps + 1)]).astype(np.int64)
     return {
-        "B": B, "D": D, "d": d, "q": q, "n_steps": n_steps, "fields": fields, "h": hs,
-        "params": params.to(dev), "x0m": x0m.to(dev).contiguous(),
+        "B": B, "D": D, "d": d, "q": q, "n_steps": n_steps, "fields": r["fields"], "h": r["h"],
+        "params": r["params"].to(dev), "x0m": r["x0m"].to(dev).contiguous(),
         "x0L": torch.zeros((B, D, D), dtype=torch.float64, device=dev), "F": F.contiguous(),
-        "QL": QL.contiguous(), "means0": means0.to(dev).contiguous(), "p0": torch.as_tensor(P[:, 0]),
-        "offsets": offsets,
+        "QL": QL.contiguous(), "means0": means0.to(dev).contiguous(), "p0": r["p0"], "offsets": offsets,
     }
 
 

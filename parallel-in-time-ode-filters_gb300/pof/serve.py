@@ -1,0 +1,214 @@
+"""Continuous-batching IEKS server (no counterpart in the reference, which
+solves one IVP per ``pof.solver.solve`` call, pof/solver.py:11-73).
+
+Requests -- (field name, params, y0, ts) with a built-in field, an order q,
+an objective tolerance and maxiters -- are queued on the host and admitted
+into one libpof engine per state shape (D, d) as request slots and memory
+free up.  Every tick runs one IEKS iteration of every admitted, unfinished
+request; requests that meet their criterion leave at once and their result
+is fetched.  Engines of different shapes run on their own CUDA streams, so
+their work overlaps on the device.  A request's result is bit-identical to
+the same request served alone (pof_server_* in include/pof.h).
+"""
+
+import ctypes
+import time
+from collections import deque
+from typing import Any, NamedTuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import batch as pbatch
+from .transitions import IWP, preconditioned_discretize
+from .utils import default_device
+
+
+class Request(NamedTuple):
+    rid: int
+    field: str
+    params: tuple
+    y0: Any
+    ts: Any
+    order: int
+    rtol: float
+    maxiters: int
+
+
+class Engine:
+    """One libpof engine: requests of state shape (D, d) = (d (q+1), d)."""
+
+    def __init__(self, d, q, max_requests, max_points, level_bytes=None, device=None, calibrate=True):
+        self.dev = device or default_device()
+        self.d, self.q = d, q
+        self.D = d * (q + 1)
+        lib = _lib.lib()
+        if level_bytes is None:  # scan levels for chunks of >= 4 steps (about 56 D^2 bytes per chunk, x 2)
+            level_bytes = 28 * self.D * self.D * max_points + (64 << 20)
+        wsb = lib.pof_server_workspace_bytes(self.D, d, max_requests, max_points, int(level_bytes))
+        if wsb == 0:
+            raise _lib.PofError("no batched kernels for (D, d) = (%d, %d)" % (self.D, d))
+        self.ws = _lib.workspace(wsb, self.dev)
+        F, QL = preconditioned_discretize(IWP(num_derivatives=q, wiener_process_dimension=d), device=self.dev)
+        self.F, self.QL = F.contiguous(), QL.contiguous()
+        h = ctypes.c_void_p()
+        _lib.check(lib.pof_server_create(self.D, d, max_requests, max_points, int(level_bytes), _lib.ptr(self.F),
+                                         _lib.ptr(self.QL), int(bool(calibrate)), _lib.ptr(self.ws), int(wsb),
+                                         ctypes.byref(h)), "pof_server_create")
+        self.h = h
+        self.slots = {}  # slot -> (request, p0)
+        self.running = 0
+
+    def close(self):
+        if self.h:
+            _lib.lib().pof_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, req, x0m, row, h, p0):
+        """Admit a prepared request; False when the engine is full."""
+        lib = _lib.lib()
+        prm = np.zeros(4, dtype=np.float64)
+        prm[: len(req.params)] = req.params
+        x0m = np.ascontiguousarray(x0m, dtype=np.float64)
+        row = np.ascontiguousarray(row, dtype=np.float64)
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        slot = lib.pof_server_submit(self.h, len(req.ts) - 1, _lib.FIELDS[req.field], vp(prm), float(h), vp(x0m),
+                                     None, vp(row), int(req.maxiters), float(req.rtol))
+        if slot == _lib.POF_ERR_BUSY:
+            return False
+        if slot < 0:
+            _lib.check(int(slot), "pof_server_submit")
+        self.slots[int(slot)] = (req, p0)
+        return True
+
+    def launch(self, k=1):
+        _lib.check(_lib.lib().pof_server_launch(self.h, int(k)), "pof_server_launch")
+
+    def sync(self):
+        n = ctypes.c_int64(0)
+        _lib.check(_lib.lib().pof_server_sync(self.h, ctypes.byref(n)), "pof_server_sync")
+        self.running = n.value
+        return self.running
+
+    def finished(self):
+        """[(request, (means, chols), info)] of the requests that finished since the last call."""
+        lib = _lib.lib()
+        out = []
+        buf = (ctypes.c_int64 * 256)()
+        while True:
+            n = lib.pof_server_poll(self.h, ctypes.cast(buf, ctypes.c_void_p), 256)
+            if n <= 0:
+                break
+            for i in range(n):
+                slot = int(buf[i])
+                req, p0 = self.slots.pop(slot)
+                N = len(req.ts)
+                m = torch.empty((N, self.D), dtype=torch.float64, device=self.dev)
+                L = torch.empty((N, self.D, self.D), dtype=torch.float64, device=self.dev)
+                info = torch.empty(_lib.I_COUNT, dtype=torch.float64, device=self.dev)
+                _lib.check(lib.pof_server_fetch(self.h, slot, _lib.ptr(m), _lib.ptr(L), _lib.ptr(info)),
+                           "pof_server_fetch")
+                idx = torch.arange(self.d, device=self.dev) * (self.q + 1)
+                ys = (m[:, idx] * p0, L[:, idx, :] * p0)
+                out.append((req, ys, info))
+            if n < 256:
+                break
+        return out
+
+
+class Server:
+    """Host side of continuous batching: a FIFO of requests, one Engine per
+    (d, q), admission each tick as memory allows."""
+
+    def __init__(self, max_requests=1024, max_points=1 << 21, device=None):
+        self.dev = device or default_device()
+        self.max_requests = max_requests
+        self.max_points = max_points
+        self.engines = {}
+        self.queue = deque()
+        self.results = {}
+        self.next_rid = 0
+        self.t_submit = {}
+        self.t_done = {}
+        self.prepared = {}
+
+    def engine(self, d, q):
+        key = (d, q)
+        if key not in self.engines:
+            self.engines[key] = Engine(d, q, self.max_requests, self.max_points, device=self.dev)
+        return self.engines[key]
+
+    def submit(self, field, params, y0, ts, order, rtol=1e-6, maxiters=10_000, t_arrival=None):
+        rid = self.next_rid
+        self.next_rid += 1
+        self.queue.append(Request(rid, field, tuple(float(p) for p in params), np.asarray(y0, dtype=np.float64),
+                                  np.asarray(ts, dtype=np.float64), int(order), float(rtol), int(maxiters)))
+        self.t_submit[rid] = time.perf_counter() if t_arrival is None else t_arrival
+        return rid
+
+    def _admit(self):
+        """Prepare and admit queued requests in arrival order while engines take them."""
+        if not self.queue:
+            return
+        reqs = list(self.queue)
+        groups = {}
+        for r in reqs:
+            if r.rid not in self.prepared:
+                groups.setdefault((pbatch._DIM[r.field], r.order), []).append(r)
+        for (d, q), rs in groups.items():
+            prep = pbatch.prepare_rows([(r.field, r.params, r.y0, r.ts) for r in rs], q)
+            for i, r in enumerate(rs):
+                self.prepared[r.rid] = (prep["x0m"][i].numpy(), prep["row"][i].numpy(), float(prep["h"][i]),
+                                        float(prep["p0"][i]))
+        prepared = self.prepared
+        kept = deque()
+        blocked = set()
+        for r in reqs:
+            key = (pbatch._DIM[r.field], r.order)
+            if key in blocked:
+                kept.append(r)
+                continue
+            x0m, row, h, p0 = prepared[r.rid]
+            if self.engine(*key).submit(r, x0m, row, h, p0):
+                del prepared[r.rid]
+            else:
+                blocked.add(key)  # keep FIFO order within a shape
+                kept.append(r)
+        self.queue = kept
+
+    def tick(self, k=1):
+        """Admit, run k iterations on every engine (overlapping), collect the
+        finished requests; returns their ids."""
+        self._admit()
+        live = [e for e in self.engines.values() if e.slots]
+        for e in live:
+            e.launch(k)
+        done = []
+        for e in live:
+            e.sync()
+            for req, ys, info in e.finished():
+                self.results[req.rid] = (ys, info)
+                self.t_done[req.rid] = time.perf_counter()
+                done.append(req.rid)
+        return done
+
+    def busy(self):
+        return bool(self.queue) or any(e.slots for e in self.engines.values())
+
+    def result(self, rid):
+        """((means (N, d), chol_covs (N, d, D)), info) as pof.solver.solve returns."""
+        ys, info = self.results[rid]
+        return ys, {"iterations": info[_lib.I_ITERATIONS].to(torch.int64), "nll": info[_lib.I_NLL],
+                    "obj": info[_lib.I_OBJ], "sigma_squared": info[_lib.I_SSQ], "calibrated": True}
+
+    def close(self):
+        for e in self.engines.values():
+            e.close()
+        self.engines = {}
