@@ -232,6 +232,11 @@ void pof_profile_enable(int32_t on);
  * `iters` fused multiply-adds (16 * iters flops per thread). `sink` is a
  * device array of `blocks` doubles that is (almost) never written. */
 int pof_fp64_probe(int64_t iters, int32_t blocks, int32_t threads, double* sink, void* stream);
+/* Diagnostics: the double reciprocal and reciprocal square root the kernels
+ * use for reflector scalars and diagonal solves (Newton-Raphson from a
+ * single-precision seed), applied to x (n device doubles; rsqrt_out = 0 for
+ * x <= 0). */
+int pof_recip_check(int64_t n, const double* x, double* rcp_out, double* rsqrt_out, void* stream);
 int pof_profile_read(double* ms_out, int64_t* count_out, int32_t nkinds, int32_t reset);
 
 /* ---------------------------------------------------------------------------

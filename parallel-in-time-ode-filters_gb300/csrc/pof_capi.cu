@@ -146,6 +146,21 @@ __global__ void k_fp64_probe(int64_t iters, double* sink) {
   if (s == 12345.678) sink[blockIdx.x] = s;  // keeps the chains alive
 }
 
+// rcp_nr / rsqrt_nr on an array (diagnostics: their accuracy against IEEE
+// division and square root is checked by the tests).
+__global__ void k_recip_check(int64_t n, const double* __restrict__ x, double* __restrict__ r, double* __restrict__ q) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  r[i] = rcp_nr(x[i]);
+  q[i] = x[i] > 0.0 ? rsqrt_nr(x[i]) : 0.0;
+}
+
+int pof_recip_check(int64_t n, const double* x, double* rcp_out, double* rsqrt_out, void* stream) {
+  if (n < 1 || !x || !rcp_out || !rsqrt_out) return POF_ERR_ARG;
+  k_recip_check<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(n, x, rcp_out, rsqrt_out);
+  return launch_status();
+}
+
 int pof_fp64_probe(int64_t iters, int32_t blocks, int32_t threads, double* sink, void* stream) {
   if (iters < 1 || blocks < 1 || threads < 1 || threads > 1024 || !sink) return POF_ERR_ARG;
   k_fp64_probe<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(iters, sink);

@@ -14,7 +14,89 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 namespace pof {
+
+// ---------------------------------------------------------------------------
+// Reciprocal and reciprocal square root of a double, for the scalars of the
+// Householder reflectors and the diagonal solves.
+//
+// GB300 runs FP64 at 1/64 of the FP32 rate and a warp instruction holds an
+// SM sub-partition's FP64 pipe for the same time however many of its lanes
+// are active, so the instruction sequences of IEEE double division and
+// square root -- computed once per reflector, often on one lane -- are a
+// large share of a small factorization's FP64 instructions.  These start
+// from a single-precision hardware approximation on an exponent-normalized
+// argument (FP32 pipe, integer exponent arithmetic) and take two
+// Newton-Raphson steps in double precision, each of which squares the
+// relative error (y <- y + y (1 - a y) for 1/a; y <- y + y (1 - a y^2) / 2
+// for 1/sqrt(a)): from the seed's ~2^-22 to below double rounding, so the
+// result is within a few units in the last place of the correctly rounded
+// value.  Arguments whose binary exponent is beyond +-1000 (zero,
+// subnormals, infinities, NaN included) take the IEEE operations.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rcp_nr(double a) {
+  const long long bits = __double_as_longlong(a);
+  const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+  if (e < -1000 || e > 1000) return 1.0 / a;
+  // m = a with exponent 0 (|m| in [1, 2), sign of a); 1/a = (1/m) 2^-e
+  const double m = __longlong_as_double((bits & ~(0x7ffLL << 52)) | (1023LL << 52));
+  double y = (double)__frcp_rn((float)m);
+  y = __longlong_as_double(__double_as_longlong(y) - ((long long)e << 52));
+  double r = fma(-a, y, 1.0);
+  y = fma(y, r, y);
+  r = fma(-a, y, 1.0);
+  return fma(y, r, y);
+}
+
+__device__ __forceinline__ double rsqrt_nr(double a) {
+  const long long bits = __double_as_longlong(a);
+  const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+  if (e < -1000 || e > 1000 || bits < 0) return 1.0 / sqrt(a);
+  // a = m 4^k with m in [1, 4); 1/sqrt(a) = (1/sqrt(m)) 2^-k
+  const int k = e >> 1;
+  const double m = __longlong_as_double((bits & ((1LL << 52) - 1)) | ((long long)(1023 + e - 2 * k) << 52));
+  double y = (double)rsqrtf((float)m);
+  y = __longlong_as_double(__double_as_longlong(y) - ((long long)k << 52));
+  double r = fma(-(a * y), y, 1.0);
+  y = fma(0.5 * y, r, y);
+  r = fma(-(a * y), y, 1.0);
+  return fma(0.5 * y, r, y);
+}
+
+template <typename T>
+__device__ __forceinline__ T rcp(T a) {
+  if constexpr (std::is_same<T, double>::value)
+    return rcp_nr(a);
+  else
+    return T(1) / a;
+}
+
+// Scalars of the Householder reflector that maps (alpha, x), ||x||^2 = xn2,
+// onto (beta, 0), with LAPACK dlarfg's conventions: beta = -sign(alpha)
+// ||(alpha, x)|| (sign(0) = +1), tau = (beta - alpha) / beta, the tail
+// scaled by scal = 1 / (alpha - beta); no reflection (beta = alpha,
+// tau = scal = 0) when x is exactly zero.
+template <typename T>
+__device__ __forceinline__ void householder(T alpha, T xn2, T& beta, T& tau, T& scal) {
+  const bool zero = (xn2 == T(0));
+  if constexpr (std::is_same<T, double>::value) {
+    const double a2 = fma(alpha, alpha, xn2);
+    const double g = rsqrt_nr(a2);  // 1 / ||(alpha, x)||
+    const double sgn = alpha >= 0.0 ? -1.0 : 1.0;
+    const double b = sgn * (a2 * g);
+    const double u = alpha - b;
+    beta = zero ? alpha : b;
+    tau = zero ? 0.0 : -u * (sgn * g);  // (beta - alpha) / beta, 1 / beta = sgn g
+    scal = zero ? 0.0 : rcp_nr(u);
+  } else {
+    const T nrm = sqrt(fma(alpha, alpha, xn2));
+    beta = zero ? alpha : (alpha >= T(0) ? -nrm : nrm);
+    tau = zero ? T(0) : (beta - alpha) / beta;
+    scal = zero ? T(0) : T(1) / (alpha - beta);
+  }
+}
 
 // C(MxN) = A(MxK) * B(KxN)
 template <typename T, int M, int K, int N, int LDA, int LDB, int LDC>
@@ -120,12 +202,8 @@ __device__ __forceinline__ void tria(T* X) {
     T xn2 = T(0);
 #pragma unroll
     for (int k = j + 1; k < NC; ++k) xn2 = fma(xj[k], xj[k], xn2);
-    const bool zero = (xn2 == T(0));
-    const T nrm = sqrt(fma(alpha, alpha, xn2));
-    const T beta = zero ? alpha : (alpha >= T(0) ? -nrm : nrm);
-    const T den = zero ? T(1) : (alpha - beta);
-    const T tau = zero ? T(0) : (beta - alpha) / beta;
-    const T scal = zero ? T(0) : T(1) / den;
+    T beta, tau, scal;
+    householder(alpha, xn2, beta, tau, scal);
 #pragma unroll
     for (int k = j + 1; k < NC; ++k) xj[k] *= scal;  // reflector v (v_j = 1)
     xj[j] = beta;
@@ -158,12 +236,8 @@ __device__ __forceinline__ void tria_top(T* X, T* Y) {
     T xn2 = T(0);
 #pragma unroll
     for (int k = j + 1; k < NC; ++k) xn2 = fma(xj[k], xj[k], xn2);
-    const bool zero = (xn2 == T(0));
-    const T nrm = sqrt(fma(alpha, alpha, xn2));
-    const T beta = zero ? alpha : (alpha >= T(0) ? -nrm : nrm);
-    const T den = zero ? T(1) : (alpha - beta);
-    const T tau = zero ? T(0) : (beta - alpha) / beta;
-    const T scal = zero ? T(0) : T(1) / den;
+    T beta, tau, scal;
+    householder(alpha, xn2, beta, tau, scal);
 #pragma unroll
     for (int k = j + 1; k < NC; ++k) xj[k] *= scal;
     xj[j] = beta;
@@ -202,7 +276,7 @@ __device__ __forceinline__ void trsv_l(const T* __restrict__ L, T* b) {
     T s = b[i];
 #pragma unroll
     for (int k = 0; k < i; ++k) s = fma(-L[i * LDL + k], b[k], s);
-    b[i] = s / L[i * LDL + i];
+    b[i] = s * rcp(L[i * LDL + i]);
   }
 }
 
@@ -214,7 +288,7 @@ __device__ __forceinline__ void trsv_lt(const T* __restrict__ L, T* b) {
     T s = b[i];
 #pragma unroll
     for (int k = i + 1; k < M; ++k) s = fma(-L[k * LDL + i], b[k], s);
-    b[i] = s / L[i * LDL + i];
+    b[i] = s * rcp(L[i * LDL + i]);
   }
 }
 
@@ -223,7 +297,7 @@ template <typename T, int M, int NR, int LDL, int LDB>
 __device__ __forceinline__ void trsm_l(const T* __restrict__ L, T* B) {
 #pragma unroll
   for (int i = 0; i < M; ++i) {
-    const T inv = T(1) / L[i * LDL + i];
+    const T inv = rcp(L[i * LDL + i]);
 #pragma unroll
     for (int j = 0; j < NR; ++j) {
       T s = B[i * LDB + j];
@@ -239,7 +313,7 @@ template <typename T, int M, int NR, int LDL, int LDB>
 __device__ __forceinline__ void trsm_lt(const T* __restrict__ L, T* B) {
 #pragma unroll
   for (int i = M - 1; i >= 0; --i) {
-    const T inv = T(1) / L[i * LDL + i];
+    const T inv = rcp(L[i * LDL + i]);
 #pragma unroll
     for (int j = 0; j < NR; ++j) {
       T s = B[i * LDB + j];

@@ -7,6 +7,7 @@ namespace pof {
 template <> const Ops* ops_shape<2, 1>(int dtype);
 template <> const Ops* ops_shape<3, 1>(int dtype);
 template <> const Ops* ops_shape<4, 1>(int dtype);
+template <> const Ops* ops_shape<5, 1>(int dtype);
 template <> const Ops* ops_shape<6, 1>(int dtype);
 template <> const Ops* ops_shape<4, 2>(int dtype);
 template <> const Ops* ops_shape<6, 2>(int dtype);
@@ -22,6 +23,7 @@ const Ops* find_shape(int dtype, int D, int DY) {
     case 21: return ops_shape<2, 1>(dtype);
     case 31: return ops_shape<3, 1>(dtype);
     case 41: return ops_shape<4, 1>(dtype);
+    case 51: return ops_shape<5, 1>(dtype);
     case 61: return ops_shape<6, 1>(dtype);
     case 42: return ops_shape<4, 2>(dtype);
     case 62: return ops_shape<6, 2>(dtype);

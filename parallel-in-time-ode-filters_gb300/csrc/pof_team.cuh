@@ -90,14 +90,7 @@ __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y) {
     // the reflector's scalars on one lane (a square root and two divisions
     // are long FP64 sequences), then broadcast
     T tau = T(0), scal = T(0), beta = T(0);
-    if (tm.r == 0) {
-      const T alpha = xj[j];
-      const bool zero = (xn2 == T(0));
-      const T nrm = sqrt(fma(alpha, alpha, xn2));
-      beta = zero ? alpha : (alpha >= T(0) ? -nrm : nrm);
-      tau = zero ? T(0) : (beta - alpha) / beta;
-      scal = zero ? T(0) : T(1) / (alpha - beta);
-    }
+    if (tm.r == 0) householder(xj[j], xn2, beta, tau, scal);
     tau = __shfl_sync(tm.mask, tau, src);
     scal = __shfl_sync(tm.mask, scal, src);
     tm.sync();
@@ -128,7 +121,7 @@ __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y) {
 template <typename T, int TS, int M, int LDL>
 __device__ __forceinline__ T t_recip_diag(const Team<TS>& tm, const T* L) {
   static_assert(M <= TS, "t_recip_diag needs M <= TS");
-  return (tm.r < M) ? T(1) / L[tm.r * LDL + tm.r] : T(0);
+  return (tm.r < M) ? rcp(L[tm.r * LDL + tm.r]) : T(0);
 }
 
 // B(M x NR) <- L^{-1} B (lower L): one right-hand-side column per lane.
@@ -156,7 +149,7 @@ __device__ __forceinline__ void t_trsm_l(const Team<TS>& tm, const T* L, T* B) {
         T s = B[i * LDB + j];
 #pragma unroll
         for (int k = 0; k < i; ++k) s = fma(-L[i * LDL + k], B[k * LDB + j], s);
-        B[i * LDB + j] = s / L[i * LDL + i];
+        B[i * LDB + j] = s * rcp(L[i * LDL + i]);
       }
     }
   }
@@ -187,7 +180,7 @@ __device__ __forceinline__ void t_trsm_lt(const Team<TS>& tm, const T* L, T* B) 
         T s = B[i * LDB + j];
 #pragma unroll
         for (int k = i + 1; k < M; ++k) s = fma(-L[k * LDL + i], B[k * LDB + j], s);
-        B[i * LDB + j] = s / L[i * LDL + i];
+        B[i * LDB + j] = s * rcp(L[i * LDL + i]);
       }
     }
   }
@@ -462,13 +455,14 @@ __device__ __forceinline__ void t_update(const Team<TS>& tm, StepTeamWs<T, D, DY
     }
     trsv_l<T, DY, LP>(w.P, wv);
     trsv_lt<T, DY, LP>(w.P, wq);
-    T ss = T(0), yy = T(0), ld = T(0);
+    T ss = T(0), yy = T(0);
 #pragma unroll
     for (int i = 0; i < DY; ++i) {
       ss = fma(wq[i], wq[i], ss);
       yy = fma(wv[i], wv[i], yy);
-      ld += log(fabs(w.P[i * LP + i]));
     }
+    // log |Psi11_ii| on lane i (the DY logarithms run side by side)
+    const T ld = tm.sum(tm.r < DY ? T(log(fabs(w.P[tm.r * LP + tm.r]))) : T(0));
     if (tm.r == 0) {
       w.sc[0] = ss;
       w.sc[1] = T(0.5) * yy + ld + T(DY) * Log2Pi<T>::half;

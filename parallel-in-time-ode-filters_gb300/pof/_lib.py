@@ -87,6 +87,7 @@ _SIGS = {
     "pof_profile_enable": (None, [_i32]),
     "pof_profile_read": (_c.c_int, [_vp, _vp, _i32, _i32]),
     "pof_fp64_probe": (_c.c_int, [_i64, _i32, _i32, _dp, _vp]),
+    "pof_recip_check": (_c.c_int, [_i64, _dp, _dp, _dp, _vp]),
     "pof_batch_workspace_bytes": (_sz, [_i32, _i64, _vp, _i32, _i32, _i32, _i32]),
     "pof_ieks_solve_batch": (
         _c.c_int,
