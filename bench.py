@@ -365,7 +365,7 @@ def run_gpu(args, workload):
         ref_means = means.clone()
         mws_b = lib.pof_ieks_mixed_workspace_bytes(n, D, d)
         mws = _lib.workspace(mws_b, dev)
-        minfo = torch.zeros(_lib.I_COUNT + 1, dtype=torch.float64, device=dev)
+        minfo = torch.zeros(_lib.I_COUNT + 2, dtype=torch.float64, device=dev)
 
         def solve_mixed():
             means.copy_(means0)
@@ -392,6 +392,7 @@ def run_gpu(args, workload):
         err = float(((ya - yb).abs().max() / yb.abs().max()).item())
         mixed = {"value": world * n / (mms * 1e-3), "unit": "IVP*steps/s", "ms_per_step": mms,
                  "iterations_float32": int(minfo[_lib.I_COUNT].item()),
+                 "best_change_float32": float(minfo[_lib.I_COUNT + 1].item()),
                  "iterations_float64": int(minfo[_lib.I_ITERATIONS].item()),
                  "max_rel_err_vs_float64": err, "speedup_vs_float64": ms / mms}
         del mws
@@ -575,14 +576,14 @@ def run_gpu_batch(args, workload):
     # mixed precision: float32 iterations, float64 polish, per problem
     mixed = None
     if not args.no_mixed:
-        info32 = torch.zeros(B, dtype=torch.float64, device=dev)
+        info32 = torch.zeros((B, 2), dtype=torch.float64, device=dev)
         ws = None
         for _ in range(args.warmup):
             solve("mixed", info32)
         mt = timed(lambda: solve("mixed", info32), args.steps)
         mms = float(np.mean(mt))
         E0P = _project_err(prep, means, ref_means)
-        it32 = info32.cpu().numpy()
+        it32 = info32[:, 0].cpu().numpy()
         it64 = info[:, _lib.I_ITERATIONS].cpu().numpy()
         mixed = {"value": world * total_steps / (mms * 1e-3), "unit": "IVP*steps/s", "ms_per_step": mms,
                  "iterations_float32_total": int(it32.sum()), "iterations_float64_total": int(it64.sum()),
@@ -878,6 +879,151 @@ def run_serve(args, workload):
     })
 
 
+# ---------------------------------------------------------------------------
+# Mixed precision with float64 polish on the problems of the mixed-precision
+# configuration: Lotka-Volterra and Van der Pol mu in {1, 10, 100}, N = 2^14,
+# q = 4 -- one solve per launch and batched, float64 and mixed
+# ---------------------------------------------------------------------------
+
+MIXED_WORKLOADS = {
+    # name: ([(field, params, y0, t1)], N, q, maxiters).  Lotka-Volterra at
+    # q = 4 on this grid does not converge in float64 (the iterates blow up
+    # and the loop runs to maxiters), hence the cap.
+    "mixed_lv_vdp": ([("lotkavolterra", (1.5, 1.0, 3.0, 1.0), [1.0, 1.0], 10.0),
+                      ("vanderpol", (1.0,), [2.0, 0.0], 6.3),
+                      ("vanderpol", (10.0,), [2.0, 0.0], 6.3),
+                      ("vanderpol", (100.0,), [2.0, 0.0], 6.3)], 2 ** 14, 4, 1000),
+}
+
+
+def run_mixed(args, workload):
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from pof import _build, _lib, batch as pbatch
+
+    _build.build(verbose=False)
+    lib = _lib.lib()
+    spec, N, q, maxiters = MIXED_WORKLOADS[workload]
+    dev = torch.device("cuda", local)
+    problems = [(nm, p, y0, np.linspace(0.0, t1, N)) for (nm, p, y0, t1) in spec]
+    prep = pbatch.prepare_batch(problems, q, device=dev)
+    B, D, d = prep["B"], prep["D"], prep["d"]
+    off = prep["offsets"]
+    steps = int(prep["n_steps"].sum())
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    results = {}
+    # one solve per launch, float64 and mixed
+    for prec in ("float64", "mixed"):
+        per = []
+        for b in range(B):
+            n = int(prep["n_steps"][b])
+            m = torch.empty((n + 1, D), dtype=torch.float64, device=dev)
+            c = torch.empty((n + 1, D, D), dtype=torch.float64, device=dev)
+            inf = torch.zeros(_lib.I_COUNT + 2, dtype=torch.float64, device=dev)
+            if prec == "float64":
+                wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+            else:
+                wsb = lib.pof_ieks_mixed_workspace_bytes(n, D, d)
+            ws = _lib.workspace(wsb, dev)
+            m0 = prep["means0"][off[b]:off[b + 1]]
+            args_c = (_lib.ptr(prep["params"][b]), float(prep["h"][b]), _lib.ptr(prep["x0m"][b]),
+                      _lib.ptr(prep["x0L"][b]), _lib.ptr(prep["F"]), _lib.ptr(prep["QL"]), _lib.ptr(m), _lib.ptr(c))
+
+            def one():
+                m.copy_(m0)
+                if prec == "float64":
+                    rc = lib.pof_ieks_solve(_lib.POF_F64, n, D, d, int(prep["fields"][b]), *args_c, maxiters, 1,
+                                            _lib.ptr(inf), _lib.ptr(ws), wsb, _lib.stream_handle())
+                else:
+                    rc = lib.pof_ieks_solve_mixed(n, D, d, int(prep["fields"][b]), *args_c, maxiters, 1e-5, maxiters,
+                                                  1, _lib.ptr(inf), _lib.ptr(ws), wsb, _lib.stream_handle())
+                _lib.check(rc, "solve")
+
+            ms = timed(one)
+            per.append({"ms": ms, "iterations": int(inf[_lib.I_ITERATIONS].item()),
+                        "iterations_float32": int(inf[_lib.I_COUNT].item()) if prec == "mixed" else 0,
+                        "best_change_float32": float(inf[_lib.I_COUNT + 1].item()) if prec == "mixed" else None,
+                        "y": m[:, ::q + 1].clone()})
+        results["plain_" + prec] = per
+    ref = [r["y"] for r in results["plain_float64"]]
+    # batched, float64 and mixed
+    means = torch.empty_like(prep["means0"])
+    G = means.shape[0]
+    chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros((B, _lib.I_COUNT), dtype=torch.float64, device=dev)
+    info32 = torch.zeros((B, 2), dtype=torch.float64, device=dev)
+    for prec in ("float64", "mixed"):
+        ws = [None]
+
+        def one():
+            means.copy_(prep["means0"])
+            ws[0] = pbatch.run_batch(prep, means, chols, info, maxiters=maxiters, workspace=ws[0], precision=prec,
+                                     maxiters_f32=maxiters, info_f32=info32)
+
+        ms = timed(one)
+        ys = [means[off[b]:off[b + 1], ::q + 1] for b in range(B)]
+        results["batched_" + prec] = {"ms": ms, "y": ys, "iterations": info[:, _lib.I_ITERATIONS].tolist(),
+                                      "iterations_float32": info32[:, 0].tolist() if prec == "mixed" else None,
+                                      "best_change_float32": info32[:, 1].tolist() if prec == "mixed" else None}
+
+    def err(y, r):
+        return float(((y - r).abs().max() / r.abs().max()).item())
+
+    names = ["%s%s" % (nm, p) for (nm, p, _, _) in spec]
+    out_probs = []
+    for b in range(B):
+        pf, pm = results["plain_float64"][b], results["plain_mixed"][b]
+        out_probs.append({
+            "problem": names[b], "N": N, "q": q,
+            "plain_float64": {"ms": pf["ms"], "iterations": pf["iterations"]},
+            "plain_mixed": {"ms": pm["ms"], "iterations_float64": pm["iterations"],
+                            "iterations_float32": pm["iterations_float32"],
+                            "best_change_float32": pm["best_change_float32"], "max_rel_err": err(pm["y"], ref[b])},
+            "batched_mixed_max_rel_err": err(results["batched_mixed"]["y"][b], ref[b]),
+            "batched_float64_max_rel_err": err(results["batched_float64"]["y"][b], ref[b]),
+        })
+    plain64_ms = sum(r["ms"] for r in results["plain_float64"])
+    plainmx_ms = sum(r["ms"] for r in results["plain_mixed"])
+    if rank != 0:
+        return
+    jprint({
+        "metric": "IVP*steps/s, mixed precision (float32 iterations + float64 polish) vs float64",
+        "value": steps / (results["batched_mixed"]["ms"] * 1e-3),
+        "unit": "IVP*steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": results["batched_mixed"]["ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": workload, "problems": names, "N": N, "q": q, "D": D, "maxiters": maxiters,
+                   "omitted": "the reaction-diffusion system (d = 128) of the configuration: needs the dense D >= 128 "
+                              "combine, not built"},
+        "plain_float64": {"value": steps / (plain64_ms * 1e-3), "ms": plain64_ms},
+        "plain_mixed": {"value": steps / (plainmx_ms * 1e-3), "ms": plainmx_ms},
+        "batched_float64": {"value": steps / (results["batched_float64"]["ms"] * 1e-3),
+                            "ms": results["batched_float64"]["ms"], "iterations": results["batched_float64"]["iterations"]},
+        "batched_mixed": {"value": steps / (results["batched_mixed"]["ms"] * 1e-3), "ms": results["batched_mixed"]["ms"],
+                          "iterations_float64": results["batched_mixed"]["iterations"],
+                          "iterations_float32": results["batched_mixed"]["iterations_float32"],
+                          "best_change_float32": results["batched_mixed"]["best_change_float32"]},
+        "speedup_batched_mixed_vs_plain_float64": plain64_ms / results["batched_mixed"]["ms"],
+        "problems": out_probs,
+    })
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -885,7 +1031,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(SERVE_WORKLOADS))
+                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(SERVE_WORKLOADS)
+                    + sorted(MIXED_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--solves-only", action="store_true",
@@ -897,6 +1044,8 @@ def main():
         run_gpu_batch(args, args.workload)
     elif args.workload in SERVE_WORKLOADS:
         run_serve(args, args.workload)
+    elif args.workload in MIXED_WORKLOADS:
+        run_mixed(args, args.workload)
     else:
         run_gpu(args, args.workload)
 

@@ -184,9 +184,10 @@ size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
  * pof_ieks_solve runs from the last kept trajectory with the reference's
  * criterion, so the result is a float64 IEKS fixed point.  No reference
  * counterpart (the reference is float64 throughout).  All arrays float64 as
- * in pof_ieks_solve; info has POF_I_COUNT + 1 entries, the last being the
+ * in pof_ieks_solve; info has POF_I_COUNT + 2 entries: [POF_I_COUNT] the
  * number of kept float32 iterations (POF_I_ITERATIONS counts the float64
- * ones).  Waits on `stream` once per iteration. */
+ * ones), [POF_I_COUNT + 1] the smallest relative change the float32 phase
+ * reached.  Waits on `stream` once per iteration. */
 int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, const double* params, double h,
                          const double* x0_mean, const double* x0_chol, const double* F, const double* QL,
                          double* means, double* chols, int64_t maxiters_f32, double rtol_f32, int64_t maxiters,
@@ -275,8 +276,9 @@ int pof_ieks_solve_batch(int32_t dtype, int64_t B, const int64_t* n_steps, int32
  * float32 filter/smoother, the change judged in float64) under
  * pof_ieks_solve_mixed's stopping and discard rules, then the float64 loop
  * of pof_ieks_solve_batch from the kept iterate.  Arrays as in
- * pof_ieks_solve_batch, all float64; info_f32 (B) device doubles receives
- * the number of kept float32 iterations of each problem (may be NULL). */
+ * pof_ieks_solve_batch, all float64; info_f32 (B, 2) device doubles
+ * receives, per problem, the number of kept float32 iterations and the
+ * smallest relative change the float32 phase reached (may be NULL). */
 size_t pof_batch_mixed_workspace_bytes(int64_t B, const int64_t* n_steps, int32_t D, int32_t d, int32_t C0,
                                        int32_t Cg);
 int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int32_t d, const int32_t* fields,

@@ -437,8 +437,9 @@ int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int
   c64.ops->finish(B, c64.a.v.gb, c64.a.v.ns, c64.a.pscal, c64.a.pscale, c64.a.calibrate, means, bufs[1], chols, info,
                   st);
   if (info_f32) {
-    rc = cuda_status(cudaMemcpy2DAsync(info_f32, sizeof(double), mst + M_IT, sizeof(double) * M_COUNT, sizeof(double),
-                                       B, cudaMemcpyDeviceToDevice, st));
+    static_assert(M_BEST == M_IT + 1, "info_f32 copies (iterations, best change) as one pair");
+    rc = cuda_status(cudaMemcpy2DAsync(info_f32, 2 * sizeof(double), mst + M_IT, sizeof(double) * M_COUNT,
+                                       2 * sizeof(double), B, cudaMemcpyDeviceToDevice, st));
     if (rc) return rc;
   }
   return launch_status();

@@ -107,11 +107,14 @@ inline BatchPersist batch_persist(int64_t B, int64_t G, int D, int DY, int esz) 
   return p;
 }
 
-// Chunk length rule when the caller gives none: enough chunks over the
-// whole batch to fill the GPU (about 4 per FP64-pipe lane group), chunks as
-// long as that allows, since the levels above level 0 cost more per step.
+// Chunk length rule when the caller gives none: about 8 x 8192 level-0
+// chunks over the whole batch for 8-lane teams (several waves of the ~3600
+// teams a GB300 holds at once, so the tail of the last wave is short),
+// chunks as long as that allows, since the levels above level 0 cost more
+// per step.  Measured on 512 FitzHugh-Nagumo problems (1.14 M steps): C0 =
+// 32 (36 k chunks) 14.1 s, 64 (18 k) 14.9 s, 128 (9 k) 18.1 s.
 inline int batch_pick_c0(int64_t total_steps, int lanes) {
-  const int64_t target = 4 * (65536 / (lanes > 0 ? lanes : 1));
+  const int64_t target = 8 * (65536 / (lanes > 0 ? lanes : 1));
   int c = 4;
   while (c < 256 && total_steps / c > target) c *= 2;
   return c;

@@ -638,8 +638,8 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
   if (calibrate) ops64->scale_inplace(chols, (int64_t)D * D * N, w + m.p64.scale, st);
   if (info) {
     k_copy_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(w + m.p64.scalars), info, 1);
-    const double it = (double)it32;
-    cudaError_t e = cudaMemcpyAsync(info + POF_I_COUNT, &it, sizeof(double), cudaMemcpyHostToDevice, st);
+    const double extra[2] = {(double)it32, best};
+    cudaError_t e = cudaMemcpyAsync(info + POF_I_COUNT, extra, sizeof(extra), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_status(e);
   }

@@ -250,12 +250,13 @@ def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_00
     G, D = means.shape
     chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
     info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
-    info32 = torch.zeros(prep["B"], dtype=torch.float64, device=dev) if precision == "mixed" else None
+    info32 = torch.zeros((prep["B"], 2), dtype=torch.float64, device=dev) if precision == "mixed" else None
     run_batch(prep, means, chols, info, maxiters=maxiters, calibrate=calibrate, C0=C0, Cg=Cg, precision=precision,
               maxiters_f32=maxiters_f32, rtol_f32=rtol_f32, info_f32=info32)
     ym, yc = project(prep, means, chols)
     info_d = {"iterations": info[:, _lib.I_ITERATIONS].to(torch.int64), "nll": info[:, _lib.I_NLL],
               "obj": info[:, _lib.I_OBJ], "sigma_squared": info[:, _lib.I_SSQ], "calibrated": bool(calibrate)}
     if info32 is not None:
-        info_d["iterations_float32"] = info32.to(torch.int64)
+        info_d["iterations_float32"] = info32[:, 0].to(torch.int64)
+        info_d["best_change_float32"] = info32[:, 1]
     return BatchResult(ym, yc, prep["offsets"], info_d)

@@ -32,7 +32,7 @@ def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxi
     m0 = x0.mean.contiguous()
     L0 = x0.chol.contiguous()
     if precision == "mixed":
-        info = torch.zeros(_lib.I_COUNT + 1, dtype=torch.float64, device=dev)
+        info = torch.zeros(_lib.I_COUNT + 2, dtype=torch.float64, device=dev)
         wsb = lib.pof_ieks_mixed_workspace_bytes(n, D, d)
         ws = _lib.workspace(wsb, dev)
         rc = lib.pof_ieks_solve_mixed(n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]), _lib.ptr(m0),
@@ -57,6 +57,7 @@ def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxi
     }
     if precision == "mixed":
         info_dict["iterations_float32"] = info[_lib.I_COUNT].to(torch.int64)
+        info_dict["best_change_float32"] = info[_lib.I_COUNT + 1]
     return MVNSqrt(means, chols), info_dict
 
 
