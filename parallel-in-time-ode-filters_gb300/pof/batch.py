@@ -226,6 +226,36 @@ def run_batch(prep, means, chols, info, maxiters=10_000, calibrate=True, C0=0, C
     return workspace
 
 
+def autotune(prep, C0s=(8, 16, 32, 64, 128), Cgs=(2, 4), iterations=3, repeats=2):
+    """Chunk length C0 and group size Cg for a prepared batch, by timing: each
+    candidate runs `iterations` IEKS iterations of the whole batch (maxiters
+    caps the solve; the work per iteration is what differs between
+    candidates), best of `repeats`, CUDA events on the current stream.
+    Returns (C0, Cg, {(C0, Cg): ms}).  A problem's result depends on (C0, Cg)
+    only through rounding; pass the same values again to reproduce it."""
+    dev = prep["x0m"].device
+    means = torch.empty_like(prep["means0"])
+    G, D = means.shape
+    chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
+    times = {}
+    ws = None
+    for C0 in C0s:
+        for Cg in Cgs:
+            best = float("inf")
+            for _ in range(repeats):
+                means.copy_(prep["means0"])
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                ws = run_batch(prep, means, chols, info, maxiters=iterations - 1, C0=C0, Cg=Cg, workspace=ws)
+                e1.record()
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            times[(C0, Cg)] = best
+    C0, Cg = min(times, key=times.get)
+    return C0, Cg, times
+
+
 def project(prep, means, chols):
     """(E0 P) applied per problem: ys.mean (G, d) and ys.chol (G, d, D), as
     pof.solver.solve returns (gmul_stack(E0 P, states))."""
@@ -241,11 +271,14 @@ def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_00
     """Solve every (field name, params, y0, ts) of ``problems`` with the
     parallel IEKS of pof.solver.solve (built-in fields, constant init).
     precision="mixed": float32 iterations first, float64 polish after, per
-    problem (as pof.solver.solve's precision="mixed").  Returns a
+    problem (as pof.solver.solve's precision="mixed").  C0="auto" picks the
+    chunk length and group size by timing (autotune).  Returns a
     BatchResult; ``result.problem(b)`` gives problem b's
     ((means (N_b, d), chol_covs (N_b, d, D)), info) as pof.solver.solve."""
     dev = default_device()
     prep = prepare_batch(problems, order, device=dev, init=init)
+    if C0 == "auto":
+        C0, Cg, _ = autotune(prep)
     means = prep["means0"].clone()
     G, D = means.shape
     chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)

@@ -214,3 +214,16 @@ def test_batch_mixed_independent_of_the_mix():
         alone = pbatch.solve_batch(problems([MIXED_D2[b]]), order=3, maxiters=1000, C0=8, precision="mixed")
         _same(full, b, alone, 0)
         assert int(full.info["iterations_float32"][b]) == int(alone.info["iterations_float32"][0])
+
+
+def test_autotune_picks_a_candidate_and_keeps_parity():
+    prep = pbatch.prepare_batch(problems(BATCH_D2), 3)
+    C0, Cg, times = pbatch.autotune(prep, C0s=(4, 16), Cgs=(2, 4), iterations=2, repeats=1)
+    assert (C0, Cg) in times and len(times) == 4 and all(t > 0 for t in times.values())
+    res = pbatch.solve_batch(problems(BATCH_D2), order=3, maxiters=1000, C0=C0, Cg=Cg)
+    ref = pbatch.solve_batch(problems(BATCH_D2), order=3, maxiters=1000, C0=4, Cg=2)
+    for b in range(len(BATCH_D2)):
+        (ma, _), ia = ref.problem(b)
+        (mb, _), ib = res.problem(b)
+        assert int(ia["iterations"]) == int(ib["iterations"])
+        assert rel(mb.cpu().numpy(), ma.cpu().numpy()) <= TOL

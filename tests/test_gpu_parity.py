@@ -172,6 +172,7 @@ SOLVES = [
     ("vdp0", lambda: (pivp.vanderpol(stiffness_constant=1.0), oivp.vanderpol(stiffness_constant=1.0)), 128, 3),
     ("rigid", lambda: (pivp.rigid_body(), oivp.rigid_body()), 128, 2),
     ("lv", lambda: (pivp.lotkavolterra(), oivp.lotkavolterra()), 256, 1),
+    ("logistic_q4", lambda: (pivp.logistic(), oivp.logistic()), 150, 4),
 ]
 
 
