@@ -176,7 +176,12 @@ size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
  * filter and smoother in float32 and converts the means back; it is kept if
  * finite.  The float32 phase ends when the largest change of the projected
  * trajectory y = E0 m falls below rtol_f32 relative to max |y|, when that
- * change failed to shrink three times in a row, after a non-finite float32 iterate
+ * change failed to shrink three times in a row once the smallest change so
+ * far is below settle_f32 (pass HUGE_VAL to count from the first iteration;
+ * a smaller value lets the first iterations from a crude initial trajectory
+ * be non-monotone -- more float32 iterations, fewer float64 ones, and on
+ * problems with several IEKS fixed points possibly another one than the
+ * float64 loop from the same start), after a non-finite float32 iterate
  * (discarded) or after maxiters_f32 iterations; a float32 phase whose
  * smallest change never came within 100 rtol_f32 is dropped (float32 is too
  * coarse for that problem) and the float64 loop starts from the input
@@ -190,7 +195,8 @@ size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
  * reached.  Waits on `stream` once per iteration. */
 int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, const double* params, double h,
                          const double* x0_mean, const double* x0_chol, const double* F, const double* QL,
-                         double* means, double* chols, int64_t maxiters_f32, double rtol_f32, int64_t maxiters,
+                         double* means, double* chols, int64_t maxiters_f32, double rtol_f32, double settle_f32,
+                         int64_t maxiters,
                          int32_t calibrate, double* info, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Scratch size of pof_linear_filtsmooth_noalloc (16 MiB per GPU). */
@@ -284,8 +290,9 @@ size_t pof_batch_mixed_workspace_bytes(int64_t B, const int64_t* n_steps, int32_
 int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int32_t d, const int32_t* fields,
                                const double* params, const double* h, const double* x0_mean, const double* x0_chol,
                                const double* F, const double* QL, double* means, double* chols, int64_t maxiters_f32,
-                               double rtol_f32, int64_t maxiters, int32_t calibrate, int32_t C0, int32_t Cg,
-                               double* info, double* info_f32, void* workspace, size_t workspace_bytes, void* stream);
+                               double rtol_f32, double settle_f32, int64_t maxiters, int32_t calibrate, int32_t C0,
+                               int32_t Cg, double* info, double* info_f32, void* workspace, size_t workspace_bytes,
+                               void* stream);
 
 /* ---------------------------------------------------------------------------
  * Continuous-batching engine (no reference counterpart): IEKS solves of one

@@ -340,8 +340,9 @@ size_t pof_batch_mixed_workspace_bytes(int64_t B, const int64_t* n_steps, int32_
 int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int32_t d, const int32_t* fields,
                                const double* params, const double* h, const double* x0_mean, const double* x0_chol,
                                const double* F, const double* QL, double* means, double* chols, int64_t maxiters_f32,
-                               double rtol_f32, int64_t maxiters, int32_t calibrate, int32_t C0, int32_t Cg,
-                               double* info, double* info_f32, void* workspace, size_t workspace_bytes, void* stream) {
+                               double rtol_f32, double settle_f32, int64_t maxiters, int32_t calibrate, int32_t C0,
+                               int32_t Cg, double* info, double* info_f32, void* workspace, size_t workspace_bytes,
+                               void* stream) {
   BatchCtx c64, c32;
   int rc = c64.init(POF_F64, B, n_steps, D, d, C0, Cg);
   if (!rc) rc = c32.init(POF_F32, B, n_steps, D, d, C0, Cg);
@@ -349,7 +350,7 @@ int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int
   rc = check_fields(B, d, fields, h);
   if (rc) return rc;
   if (!params || !x0_mean || !x0_chol || !F || !QL || !means || !chols || !workspace || maxiters < 0 ||
-      maxiters_f32 < 0 || !(rtol_f32 > 0))
+      maxiters_f32 < 0 || !(rtol_f32 > 0) || !(settle_f32 > 0))
     return POF_ERR_ARG;
   const MixedExtras ex = mixed_extras(c32);
   if (workspace_bytes < c64.bytes() + c32.bytes() + ex.total + 256) return POF_ERR_WORKSPACE;
@@ -400,7 +401,7 @@ int pof_ieks_solve_batch_mixed(int64_t B, const int64_t* n_steps, int32_t D, int
       c32.ops->lin_mixed(a.v, params, means, static_cast<float*>(a.H), static_cast<float*>(a.c), st);
       c32.ops->filtsmooth(a, nullptr, m32, st);
       c32.ops->ychange(a.v, m32, means, mst, st);
-      kb_ctl32<<<g256(a.v.Ba), 256, 0, st>>>(a.v, mst, a.frozen, maxiters_f32, rtol_f32, a.nactive);
+      kb_ctl32<<<g256(a.v.Ba), 256, 0, st>>>(a.v, mst, a.frozen, maxiters_f32, rtol_f32, settle_f32, a.nactive);
       c32.ops->accept(a.v, m32, means, mst, st);
     };
     rc = use_graph ? c32.capture(st, body) : POF_OK;

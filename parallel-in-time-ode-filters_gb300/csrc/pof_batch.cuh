@@ -38,6 +38,19 @@ struct BView {
   const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;     \
   Team<TS> tm;
 
+// Level-0 batch kernels: the block shares one copy of F, QL, QL^{-1} (the
+// preconditioned transition model is the same for every step and problem).
+#define POF_BL0_PROLOGUE(WS)                                                             \
+  constexpr int HB_ = FQHeader<T, D, false>::bytes;                                      \
+  using B_ = TeamBlockH<WS, TS, HB_>;                                                    \
+  extern __shared__ __align__(16) unsigned char smem_raw_[];                             \
+  const int team_in_block = threadIdx.x / TS;                                            \
+  WS& ws_ = reinterpret_cast<WS*>(smem_raw_ + HB_)[team_in_block];                      \
+  const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;                    \
+  Team<TS> tm;                                                                           \
+  FQ<T, D>& fq = *reinterpret_cast<FQ<T, D>*>(smem_raw_);                               \
+  load_fq_block<T, TS, D>(tm, fq, F, QL);
+
 // EK1 linearization (pof/step.py:12-22, observations.py:35-40) at the
 // previous iterate, one thread per step of an active chunk: the residual
 // E1 x - f(E0 x) of the step's problem (own field, parameters and Nordsieck
@@ -85,15 +98,13 @@ __global__ void kb_linearize(BView v, const T* __restrict__ params, const T* __r
 template <typename T, int D, int DY, int TS>
 __global__ void kb_filt_l0_reduce(BView v, const T* __restrict__ F, const T* __restrict__ QL,
                                   const T* __restrict__ H, const T* __restrict__ c, T* __restrict__ out) {
-  using WS = L0TeamWs<T, D, DY>;
-  POF_BTEAM_PROLOGUE(WS)
+  using WS = L0FoldWs<T, D, DY, false>;
+  POF_BL0_PROLOGUE(WS)
   if (t >= v.n1) return;
   if (v.frozen[v.cp[t]]) return;
-  StepTeamWs<T, D, DY>& w = ws_.s;
+  StepFoldWs<T, D, DY>& w = ws_.s;
   constexpr int L1 = Ld<D>::v;
   const int64_t s0 = v.cs[t], s1 = v.ce[t];
-  StepModel sm{F, QL, 0, nullptr, nullptr, nullptr, 0};
-  t_load_FQ<T, TS, D, DY>(tm, w, sm, 0);
   t_fill<T, TS, D, D, L1>(tm, w.A, T(0), T(1));
   t_fill<T, TS, D, D, L1>(tm, w.L, T(0), T(0));
   t_fill<T, TS, D, D, L1>(tm, w.Z, T(0), T(0));
@@ -104,7 +115,7 @@ __global__ void kb_filt_l0_reduce(BView v, const T* __restrict__ F, const T* __r
   for (int64_t s = s0; s < s1; ++s) {
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     tm.sync();
-    t_cond_fold_step<T, TS, D, DY>(tm, w);
+    t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL);
   }
   tm.sync();
   t_store_filt<T, TS, D>(tm, out, v.n1, t, w.A, w.b, w.L, w.eta, w.Z);
@@ -181,21 +192,18 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
                                 const T* __restrict__ H, const T* __restrict__ c, const T* __restrict__ states1,
                                 T* __restrict__ means, T* __restrict__ chols, T* __restrict__ selems,
                                 double* __restrict__ partials) {
-  using WS = L0TeamWs<T, D, DY>;
-  POF_BTEAM_PROLOGUE(WS)
+  using WS = L0KFWs<T, D, DY, false>;
+  POF_BL0_PROLOGUE(WS)
   if (t >= v.n1) return;
   const int b = v.cp[t];
   if (v.frozen[b]) return;
-  StepTeamWs<T, D, DY>& w = ws_.s;
+  StepKFWs<T, D, DY>& w = ws_.s;
   using GL = SmoLayout<D>;
   constexpr int L1 = Ld<D>::v, L2 = Ld<2 * D>::v;
   const int64_t s0 = v.cs[t], s1 = v.ce[t];
   const int64_t n = v.n;
-  StepModel sm{F, QL, 0, nullptr, nullptr, nullptr, 0};
-  t_load_FQ<T, TS, D, DY>(tm, w, sm, 0);
   t_load_state<T, TS, D>(tm, states1, v.n1, t, w.m, w.L);
   tm.sync();
-  t_inv_lower<T, TS, D>(tm, w.QL, ws_.QLi);
   if (s0 == v.gb[b]) {  // first chunk of the problem: its grid point 0 holds x0
     const int64_t g = s0;
     for (int f = tm.r; f < D + D * D; f += TS) {
@@ -210,10 +218,10 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
     tm.sync();
-    t_kf_step<T, TS, D, DY, true>(tm, w);
+    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL);
     ssq += (double)w.sc[0];
     nll += (double)w.sc[1];
-    fobj += (double)t_objective<T, TS, D>(tm, w.F, ws_.QLi, ws_.mold, w.m, ws_.r);
+    fobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, ws_.mold, w.m, ws_.r);
     for (int f = tm.r; f < GL::NG; f += TS) {
       T val;
       if (f < GL::E)
@@ -331,8 +339,8 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
                                T* __restrict__ chols, const double* __restrict__ scale,
                                const T* __restrict__ means_old, double c_mrtol, double c_matol,
                                double* __restrict__ partials) {
-  using WS = SmoL0TeamWs<T, D>;
-  POF_BTEAM_PROLOGUE(WS)
+  using WS = SmoL0Ws<T, D, false>;
+  POF_BL0_PROLOGUE(WS)
   if (t >= v.n1) return;
   const int b = v.cp[t];
   if (v.frozen[b]) return;
@@ -340,12 +348,6 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
   constexpr int L1 = Ld<D>::v;
   const int64_t s0 = v.cs[t], s1 = v.ce[t];
   const T sc = scale ? (T)scale[b] : T(1);
-  for (int f = tm.r; f < D * D; f += TS) {
-    ws_.F[(f / D) * L1 + f % D] = F[f];
-    ws_.QL[(f / D) * L1 + f % D] = QL[f];
-  }
-  tm.sync();
-  t_inv_lower<T, TS, D>(tm, ws_.QL, ws_.QLi);
   t_load_state<T, TS, D>(tm, ends1, v.n1, t, w.g1, w.D1);
   tm.sync();
   double sobj = 0.0, notclose = 0.0;
@@ -372,7 +374,7 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
     t_load_smo<T, TS, D>(tm, selems, v.n, k, w.g2, w.E2, w.D2m);
     tm.sync();
     t_smooth_apply<T, TS, D>(tm, w);
-    sobj += (double)t_objective<T, TS, D>(tm, ws_.F, ws_.QLi, w.g1, ws_.mnext, ws_.r);
+    sobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, w.g1, ws_.mnext, ws_.r);
     const int64_t g = k;
     close_count(g);
     for (int f = tm.r; f < D + D * D; f += TS) {
@@ -391,6 +393,7 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
 }
 
 #undef POF_BTEAM_PROLOGUE
+#undef POF_BL0_PROLOGUE
 
 // Fixed-order sum of a problem's chunk partials over [c0, c1) by one warp:
 // lane l sums chunks c0 + l, c0 + l + 32, ... in order, then a fixed
@@ -604,10 +607,11 @@ __global__ void kb_ychange(BView v, const float* __restrict__ mnew, const double
 // The float32 phase's stopping rules per problem (pof_ieks_solve_mixed):
 // a non-finite candidate is dropped and ends the phase; otherwise it is
 // kept; the phase ends when the relative change is below rtol_f32, after
-// three changes in a row that did not shrink, or after maxiters_f32 kept
-// iterations.  done32 marks the problems whose phase has ended.
+// three changes in a row that did not shrink (counted once the smallest
+// change is below settle_f32), or after maxiters_f32 kept iterations.
+// done32 marks the problems whose phase has ended.
 static __global__ void kb_ctl32(BView v, double* __restrict__ mst, int32_t* __restrict__ done32, int64_t maxiters_f32,
-                                double rtol_f32, int32_t* __restrict__ nactive) {
+                                double rtol_f32, double settle_f32, int32_t* __restrict__ nactive) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= v.Ba) return;
   const int b = v.ap[k];
@@ -623,7 +627,11 @@ static __global__ void kb_ctl32(BView v, double* __restrict__ mst, int32_t* __re
   const double rel = m[M_AY] > 0.0 ? m[M_DY] / m[M_AY] : m[M_DY];
   m[M_BEST] = rel < m[M_BEST] ? rel : m[M_BEST];
   bool stop = rel < rtol_f32;
-  m[M_WORSE] = rel >= m[M_PREV] ? m[M_WORSE] + 1.0 : 0.0;
+  // non-shrinking changes count once the smallest change is below settle_f32
+  if (rel >= m[M_PREV])
+    m[M_WORSE] += m[M_BEST] < settle_f32 ? 1.0 : 0.0;
+  else
+    m[M_WORSE] = 0.0;
   stop = stop || m[M_WORSE] >= 3.0 || m[M_IT] >= (double)maxiters_f32;
   m[M_PREV] = rel;
   if (stop)
@@ -715,8 +723,11 @@ struct BatchDriver {
   static constexpr int TSN = TSW / 2 >= 4 ? TSW / 2 : 4;
   using FWS = FiltTeamWs<T, D>;
   using SWS = SmoTeamWs<T, D>;
-  using L0WS = L0TeamWs<T, D, DY>;
-  using SL0WS = SmoL0TeamWs<T, D>;
+  template <int TS, typename WS, typename... KArgs, typename... Args>
+  static void launch_l0(void (*kern)(KArgs...), int64_t nteams, cudaStream_t st, Args... args) {
+    using B = TeamBlockH<WS, TS, FQHeader<T, D, false>::bytes>;
+    kern<<<(unsigned)((nteams + B::teams - 1) / B::teams), B::threads, B::smem, st>>>(args...);
+  }
 
   template <typename U>
   static U* at(char* base, size_t off) {
@@ -769,8 +780,8 @@ struct BatchDriver {
     const int32_t* frozen = a.frozen;
     {
       ProfScope ps(PK_FILT_L0_REDUCE, st);
-      launch_team<L0WS, TS>(kb_filt_l0_reduce<T, D, DY, TS>, n1, st, v, F, QL, (const T*)H, (const T*)c,
-                            at<T>(lw, L.felem[1]));
+      launch_l0<TS, L0FoldWs<T, D, DY, false>>(kb_filt_l0_reduce<T, D, DY, TS>, n1, st, v, F, QL, (const T*)H,
+                                               (const T*)c, at<T>(lw, L.felem[1]));
     }
     for (int l = 2; l <= L.nlev; ++l) {
       ProfScope ps(PK_FILT_REDUCE, st);
@@ -790,8 +801,9 @@ struct BatchDriver {
     }
     {
       ProfScope ps(PK_FILT_L0_DOWN, st);
-      launch_team<L0WS, TS>(kb_filt_l0_down<T, D, DY, TS>, n1, st, v, F, QL, (const T*)H, (const T*)c,
-                            (const T*)at<T>(lw, L.fstate[1]), mnew, chols, selem, at<double>(lw, L.partials));
+      launch_l0<TS, L0KFWs<T, D, DY, false>>(kb_filt_l0_down<T, D, DY, TS>, n1, st, v, F, QL, (const T*)H,
+                                             (const T*)c, (const T*)at<T>(lw, L.fstate[1]), mnew, chols, selem,
+                                             at<double>(lw, L.partials));
     }
     {
       ProfScope ps(PK_FILT_FINALIZE, st);
@@ -820,10 +832,10 @@ struct BatchDriver {
     }
     {
       ProfScope ps(PK_SMO_L0_DOWN, st);
-      launch_team<SL0WS, TS>(kb_smo_l0_down<T, D, TS>, n1, st, v, F, QL, (const T*)selem,
-                             (const T*)at<T>(lw, L.gend[1]), mnew, chols,
-                             a.calibrate ? (const double*)a.pscale : nullptr, mold, a.mrtol, a.matol,
-                             at<double>(lw, L.partials));
+      launch_l0<TS, SmoL0Ws<T, D, false>>(kb_smo_l0_down<T, D, TS>, n1, st, v, F, QL, (const T*)selem,
+                                          (const T*)at<T>(lw, L.gend[1]), mnew, chols,
+                                          a.calibrate ? (const double*)a.pscale : nullptr, mold, a.mrtol, a.matol,
+                                          at<double>(lw, L.partials));
     }
   }
 

@@ -544,7 +544,8 @@ size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d) {
 
 int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, const double* params, double h,
                          const double* x0_mean, const double* x0_chol, const double* F, const double* QL,
-                         double* means, double* chols, int64_t maxiters_f32, double rtol_f32, int64_t maxiters,
+                         double* means, double* chols, int64_t maxiters_f32, double rtol_f32, double settle_f32,
+                         int64_t maxiters,
                          int32_t calibrate, double* info, void* workspace, size_t workspace_bytes, void* stream) {
   const Ops* ops64 = nullptr;
   const Ops* ops32 = nullptr;
@@ -554,7 +555,7 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
   if (rc) return rc;
   if (field <= 0 || field >= FIELD_COUNT || field_dim(field) != d) return POF_ERR_FIELD;
   if (!params || !x0_mean || !x0_chol || !F || !QL || !means || !chols || !workspace || maxiters < 0 ||
-      maxiters_f32 < 0 || !(rtol_f32 > 0))
+      maxiters_f32 < 0 || !(rtol_f32 > 0) || !(settle_f32 > 0))
     return POF_ERR_ARG;
   MixedLayout m = mixed_layout(n_steps, D, d);
   if (workspace_bytes < m.total) return POF_ERR_WORKSPACE;
@@ -590,6 +591,7 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
   int64_t it32 = 0;
   double prev = 1e300, best = 1e300;
   int worse = 0;
+  const double settle = settle_f32;
   {
     cudaError_t e = cudaMemcpyAsync(keep, means, sizeof(double) * NM, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return cuda_status(e);
@@ -619,7 +621,10 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
     const double rel = ay > 0.0 ? dy / ay : dy;
     best = rel < best ? rel : best;
     if (rel < rtol_f32) break;       // converged as far as float32 goes
-    worse = rel >= prev ? worse + 1 : 0;
+    // non-shrinking changes count once the change is below `settle` (the
+    // IEKS's first iterations from a crude initial trajectory are not
+    // monotone); 0 counts every one
+    worse = (rel >= prev && best < settle) ? worse + 1 : (rel >= prev ? worse : 0);
     if (worse >= 3) break;           // float32 stopped helping
     prev = rel;
   }

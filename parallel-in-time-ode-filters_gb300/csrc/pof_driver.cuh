@@ -123,8 +123,15 @@ struct Driver {
   static constexpr bool kTeamL0 = D >= 6;  // pof_plan.h l0_lanes
   using FWS = FiltTeamWs<T, D>;
   using SWS = SmoTeamWs<T, D>;
-  using L0WS = L0TeamWs<T, D, DY>;
-  using SL0WS = SmoL0TeamWs<T, D>;
+
+  // level-0 team kernels: block-shared transition model unless it varies
+  // per step (PS)
+  template <int TS, bool PS, typename WS, typename... KArgs, typename... Args>
+  static void launch_l0(void (*kern)(KArgs...), int64_t nteams, cudaStream_t st, Args... args) {
+    using B = TeamBlockH<WS, TS, FQHeader<T, D, PS>::bytes>;
+    const unsigned grid = (unsigned)((nteams + B::teams - 1) / B::teams);
+    kern<<<grid, B::threads, B::smem, st>>>(args...);
+  }
 
   static void filter(const Plan& p, char* ws, const StepModel& sm, const T* x0m, const T* x0L, T* means, T* chols,
                      cudaStream_t st) {
@@ -160,9 +167,14 @@ struct Driver {
     const int64_t n1 = p.cnt[1];
     {
       ProfScope ps(PK_FILT_L0_REDUCE, st);
-      if constexpr (kTeamL0)
-        launch_team<L0WS, TS>(k_filt_l0_reduce_team<T, D, DY, TS>, n1, st, n, p.C0, sm, x0m, x0L,
-                              b.template at<T>(p.felem[1]), n1);
+      if constexpr (kTeamL0) {
+        if (sm.ft_stride)
+          launch_l0<TS, true, L0FoldWs<T, D, DY, true>>(k_filt_l0_reduce_team<T, D, DY, TS, true>, n1, st, n, p.C0,
+                                                        sm, x0m, x0L, b.template at<T>(p.felem[1]), n1);
+        else
+          launch_l0<TS, false, L0FoldWs<T, D, DY, false>>(k_filt_l0_reduce_team<T, D, DY, TS, false>, n1, st, n,
+                                                          p.C0, sm, x0m, x0L, b.template at<T>(p.felem[1]), n1);
+      }
       else
         k_filt_l0_reduce<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(n, p.C0, sm, x0m, x0L,
                                                                              b.template at<T>(p.felem[1]), n1);
@@ -185,10 +197,16 @@ struct Driver {
     }
     {
       ProfScope ps(PK_FILT_L0_DOWN, st);
-      if constexpr (kTeamL0)
-        launch_team<L0WS, TS>(k_filt_l0_down_team<T, D, DY, TS>, n1, st, n, p.C0, sm,
-                              (const T*)b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
-                              b.template at<double>(p.partials));
+      if constexpr (kTeamL0) {
+        if (sm.ft_stride)
+          launch_l0<TS, true, L0KFWs<T, D, DY, true>>(k_filt_l0_down_team<T, D, DY, TS, true>, n1, st, n, p.C0, sm,
+                                                      (const T*)b.template at<T>(p.fstate[1]), n1, means, chols,
+                                                      b.template at<T>(p.selem), b.template at<double>(p.partials));
+        else
+          launch_l0<TS, false, L0KFWs<T, D, DY, false>>(k_filt_l0_down_team<T, D, DY, TS, false>, n1, st, n, p.C0,
+                                                        sm, (const T*)b.template at<T>(p.fstate[1]), n1, means, chols,
+                                                        b.template at<T>(p.selem), b.template at<double>(p.partials));
+      }
       else
         k_filt_l0_down<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
             n, p.C0, sm, b.template at<T>(p.fstate[1]), n1, means, chols, b.template at<T>(p.selem),
@@ -238,10 +256,18 @@ struct Driver {
     {
       ProfScope ps(PK_SMO_L0_DOWN, st);
       const T* scl = calibrate ? b.template at<T>(p.scale) : nullptr;
-      if constexpr (kTeamL0)
-        launch_team<SL0WS, TS>(k_smo_l0_down_team<T, D, TS>, n1, st, n, p.C0, F, QL, ft_stride,
-                               (const T*)b.template at<T>(p.selem), (const T*)b.template at<T>(p.gend[1]), n1,
-                               means, chols, scl, means_old, p.mrtol, p.matol, b.template at<double>(p.partials));
+      if constexpr (kTeamL0) {
+        if (ft_stride)
+          launch_l0<TS, true, SmoL0Ws<T, D, true>>(k_smo_l0_down_team<T, D, TS, true>, n1, st, n, p.C0, F, QL,
+                                                   ft_stride, (const T*)b.template at<T>(p.selem),
+                                                   (const T*)b.template at<T>(p.gend[1]), n1, means, chols, scl,
+                                                   means_old, p.mrtol, p.matol, b.template at<double>(p.partials));
+        else
+          launch_l0<TS, false, SmoL0Ws<T, D, false>>(k_smo_l0_down_team<T, D, TS, false>, n1, st, n, p.C0, F, QL,
+                                                     ft_stride, (const T*)b.template at<T>(p.selem),
+                                                     (const T*)b.template at<T>(p.gend[1]), n1, means, chols, scl,
+                                                     means_old, p.mrtol, p.matol, b.template at<double>(p.partials));
+      }
       else
         k_smo_l0_down<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(
             n, p.C0, F, QL, ft_stride, b.template at<T>(p.selem), b.template at<T>(p.gend[1]), n1, means, chols,

@@ -393,27 +393,45 @@ namespace pof {
 // kf_step / cond_fold_step of pof_ops.cuh.
 // ---------------------------------------------------------------------------
 template <typename T, int D, int DY>
-struct StepTeamWs {
+struct StepDims {
   static constexpr int D2 = 2 * D;
   static constexpr int DP = D + DY;
   static constexpr int LD2 = Ld<D2>::v;
   static constexpr int LD1 = Ld<D>::v;
   static constexpr int LDP = Ld<DP>::v;
   static constexpr int LDZ = Ld<D + DY>::v;
-  T F[D * LD1], QL[D * LD1];                // transition model
-  T H[DY * LD1], c[DY], R[DY * DY];         // observation model of the step
-  T m[D], L[D * LD1];                       // filtered state (or conditional L)
-  T X[D * LD2], Y[D * LD2];                 // [F L, QL], [L, 0]
-  T P[DP * LDP];                            // Psi
-  T E[D * LD1], g[D], mp[D];                // smoother element, predicted mean
-  T A[D * LD1], b[D], eta[D], Z[D * LD1];   // conditional fold state
-  T FA[D * LD1], Fb[D], W[DY * LD1], w[DY], ZX[D * LDZ];
-  T sc[4];                                  // scalars: ssq term, nll term
 };
 
-template <typename T, int TS, int D, int DY>
-__device__ __forceinline__ void t_load_step(const Team<TS>& tm, StepTeamWs<T, D, DY>& w, const T* H, const T* c,
-                                            const T* R) {
+// Shared-memory workspace of one team for the Kalman filter step fused with
+// the smoother element (the transition model F, QL is passed separately:
+// one copy per block).
+template <typename T, int D, int DY>
+struct StepKFWs : StepDims<T, D, DY> {
+  using B = StepDims<T, D, DY>;
+  T H[DY * B::LD1], c[DY], R[DY * DY];          // observation model of the step
+  T m[D], L[D * B::LD1];                        // filtered state
+  T X[D * B::LD2], Y[D * B::LD2];               // [F L, QL], [L, 0]
+  T P[B::DP * B::LDP];                          // Psi
+  T E[D * B::LD1], g[D], mp[D];                 // smoother element, predicted mean
+  T sc[4];                                      // scalars: ssq term, nll term
+};
+
+// ... for the conditional fold (and the plain Kalman step of a first chunk).
+template <typename T, int D, int DY>
+struct StepFoldWs : StepDims<T, D, DY> {
+  using B = StepDims<T, D, DY>;
+  T H[DY * B::LD1], c[DY], R[DY * DY];
+  T m[D], L[D * B::LD1];                        // conditional L (or the filtered state)
+  T X[D * B::LD2];                              // [F L, QL]
+  T P[B::DP * B::LDP];
+  T mp[D];
+  T A[D * B::LD1], b[D], eta[D], Z[D * B::LD1];  // conditional fold state
+  T FA[D * B::LD1], Fb[D], W[DY * B::LD1], w[DY], ZX[D * B::LDZ];
+  T sc[4];
+};
+
+template <typename T, int TS, int D, int DY, typename WS>
+__device__ __forceinline__ void t_load_step(const Team<TS>& tm, WS& w, const T* H, const T* c, const T* R) {
   constexpr int L1 = Ld<D>::v;
   for (int f = tm.r; f < DY * D; f += TS) w.H[(f / D) * L1 + f % D] = H[f];
   for (int f = tm.r; f < DY; f += TS) w.c[f] = c[f];
@@ -422,9 +440,9 @@ __device__ __forceinline__ void t_load_step(const Team<TS>& tm, StepTeamWs<T, D,
 
 // Psi = tria([[H Lp, R], [Lp, 0]]) with Lp = X[:, :D]; then r = H mp + c,
 // ssq / nll terms, m <- mp + Psi21 Psi11^{-1} (-r), L <- Psi22.
-template <typename T, int TS, int D, int DY, bool UPDATE_STATE>
-__device__ __forceinline__ void t_update(const Team<TS>& tm, StepTeamWs<T, D, DY>& w) {
-  using W = StepTeamWs<T, D, DY>;
+template <typename T, int TS, int D, int DY, bool UPDATE_STATE, typename WS>
+__device__ __forceinline__ void t_update(const Team<TS>& tm, WS& w) {
+  using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, LP = W::LDP, DP = W::DP;
   // rows 0..DY-1: [H Lp, R]; rows DY..: [Lp, 0]
   for (int idx = tm.r; idx < DY * D; idx += TS) {
@@ -479,14 +497,15 @@ __device__ __forceinline__ void t_update(const Team<TS>& tm, StepTeamWs<T, D, DY
 }
 
 // One square-root KF step from the filtered state (m, L) at grid s, fused with
-// the smoother element (g, E, Dm = Y[:, D:]) of grid s when SMOOTH.
-template <typename T, int TS, int D, int DY, bool SMOOTH>
-__device__ __forceinline__ void t_kf_step(const Team<TS>& tm, StepTeamWs<T, D, DY>& w) {
-  using W = StepTeamWs<T, D, DY>;
+// the smoother element (g, E, Dm = Y[:, D:]) of grid s when SMOOTH.  F and
+// QL (D x D, leading dimension Ld<D>) are the step's transition model.
+template <typename T, int TS, int D, int DY, bool SMOOTH, typename WS>
+__device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F, const T* QL) {
+  using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, D2 = W::D2;
-  t_mm<T, TS, D, D, D, L1, L1, L2>(tm, w.F, w.L, w.X);
-  t_copy<T, TS, D, D, L1, L2>(tm, w.QL, w.X + D);
-  t_mv<T, TS, D, D, L1>(tm, w.F, w.m, w.mp);
+  t_mm<T, TS, D, D, D, L1, L1, L2>(tm, F, w.L, w.X);
+  t_copy<T, TS, D, D, L1, L2>(tm, QL, w.X + D);
+  t_mv<T, TS, D, D, L1>(tm, F, w.m, w.mp);
   if constexpr (SMOOTH) {
     t_copy<T, TS, D, D, L1, L2>(tm, w.L, w.Y);
     t_fill<T, TS, D, D, L2>(tm, w.Y + D, T(0), T(0));
@@ -511,13 +530,14 @@ __device__ __forceinline__ void t_kf_step(const Team<TS>& tm, StepTeamWs<T, D, D
 
 // One step of the conditional fold (cond_fold_step of pof_ops.cuh).
 template <typename T, int TS, int D, int DY>
-__device__ __forceinline__ void t_cond_fold_step(const Team<TS>& tm, StepTeamWs<T, D, DY>& w) {
-  using W = StepTeamWs<T, D, DY>;
+__device__ __forceinline__ void t_cond_fold_step(const Team<TS>& tm, StepFoldWs<T, D, DY>& w, const T* F,
+                                                 const T* QL) {
+  using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, LP = W::LDP, LZ = W::LDZ, D2 = W::D2;
-  t_mm<T, TS, D, D, D, L1, L1, L2>(tm, w.F, w.L, w.X);
-  t_copy<T, TS, D, D, L1, L2>(tm, w.QL, w.X + D);
-  t_mm<T, TS, D, D, D, L1, L1, L1>(tm, w.F, w.A, w.FA);
-  t_mv<T, TS, D, D, L1>(tm, w.F, w.b, w.Fb);
+  t_mm<T, TS, D, D, D, L1, L1, L2>(tm, F, w.L, w.X);
+  t_copy<T, TS, D, D, L1, L2>(tm, QL, w.X + D);
+  t_mm<T, TS, D, D, D, L1, L1, L1>(tm, F, w.A, w.FA);
+  t_mv<T, TS, D, D, L1>(tm, F, w.b, w.Fb);
   tm.sync();
   t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X);
   t_update<T, TS, D, DY, false>(tm, w);

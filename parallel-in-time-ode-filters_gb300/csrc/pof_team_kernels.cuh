@@ -262,22 +262,68 @@ __global__ void k_smo_top_team(const T* __restrict__ elems, int64_t n, const T* 
 // Level 0 with teams (large D, where per-thread state does not fit registers)
 // ---------------------------------------------------------------------------
 
-template <typename T, int D, int DY>
-struct L0TeamWs {
-  StepTeamWs<T, D, DY> s;
-  T QLi[D * Ld<D>::v];  // QL^{-1} (objective terms)
-  T mold[D], r[D];
+// Transition model of a level-0 kernel and QL^{-1} (objective terms): one
+// copy per block, shared by its teams, when it is the same for every step
+// (PS = false: the preconditioned IWP); one per team, reloaded each step,
+// when it varies (PS = true).
+template <typename T, int D>
+struct FQ {
+  T F[D * Ld<D>::v], QL[D * Ld<D>::v], QLi[D * Ld<D>::v];
 };
 
-template <typename T, int TS, int D, int DY>
-__device__ __forceinline__ void t_load_FQ(const Team<TS>& tm, StepTeamWs<T, D, DY>& w, const StepModel& sm,
-                                          int64_t s) {
+template <typename Base, typename T, int D, bool PS>
+struct WithFQ : Base {};
+template <typename Base, typename T, int D>
+struct WithFQ<Base, T, D, true> : Base {
+  FQ<T, D> fq;
+};
+
+template <typename T, int D, int DY>
+struct L0KFBase {
+  StepKFWs<T, D, DY> s;
+  T mold[D], r[D];
+};
+template <typename T, int D, int DY>
+struct L0FoldBase {
+  StepFoldWs<T, D, DY> s;
+};
+template <typename T, int D>
+struct SmoL0Base {
+  SmoTeamWs<T, D> s;
+  T mnext[D], r[D];
+};
+template <typename T, int D, int DY, bool PS>
+using L0KFWs = WithFQ<L0KFBase<T, D, DY>, T, D, PS>;
+template <typename T, int D, int DY, bool PS>
+using L0FoldWs = WithFQ<L0FoldBase<T, D, DY>, T, D, PS>;
+template <typename T, int D, bool PS>
+using SmoL0Ws = WithFQ<SmoL0Base<T, D>, T, D, PS>;
+
+// Bytes of the block-shared transition model in front of the team array.
+template <typename T, int D, bool PS>
+struct FQHeader {
+  static constexpr int bytes = PS ? 0 : (int)sizeof(FQ<T, D>);
+};
+
+// teams per block of a level-0 kernel with a shared header of HB bytes:
+// up to 64 / TS teams within the default 48 KB of dynamic shared memory
+template <typename WS, int TS, int HB>
+struct TeamBlockH {
+  static constexpr int per_warp_max = 64 / TS;
+  static constexpr int fit = (int)((49152 - HB) / sizeof(WS));
+  static constexpr int teams = fit < 1 ? 1 : (fit < per_warp_max ? fit : per_warp_max);
+  static constexpr int threads = teams * TS;
+  static constexpr int smem = HB + teams * (int)sizeof(WS);
+};
+
+template <typename T, int TS, int D>
+__device__ __forceinline__ void t_load_FQ(const Team<TS>& tm, FQ<T, D>& q, const StepModel& sm, int64_t s) {
   constexpr int L1 = Ld<D>::v;
   const T* F = static_cast<const T*>(sm.F) + s * sm.ft_stride;
   const T* QL = static_cast<const T*>(sm.QL) + s * sm.ft_stride;
   for (int f = tm.r; f < D * D; f += TS) {
-    w.F[(f / D) * L1 + f % D] = F[f];
-    w.QL[(f / D) * L1 + f % D] = QL[f];
+    q.F[(f / D) * L1 + f % D] = F[f];
+    q.QL[(f / D) * L1 + f % D] = QL[f];
   }
 }
 
@@ -289,6 +335,20 @@ __device__ __forceinline__ void t_inv_lower(const Team<TS>& tm, const T* QL, T* 
   tm.sync();
   t_trsm_l<T, TS, D, D, L1, L1>(tm, QL, QLi);
   tm.sync();
+}
+
+// The block's shared transition model (every thread of the block takes
+// part: call before any team leaves).
+template <typename T, int TS, int D>
+__device__ __forceinline__ void load_fq_block(const Team<TS>& tm, FQ<T, D>& q, const T* F, const T* QL) {
+  constexpr int L1 = Ld<D>::v;
+  for (int f = threadIdx.x; f < D * D; f += blockDim.x) {
+    q.F[(f / D) * L1 + f % D] = F[f];
+    q.QL[(f / D) * L1 + f % D] = QL[f];
+  }
+  __syncthreads();
+  if (threadIdx.x < TS) t_inv_lower<T, TS, D>(tm, q.QL, q.QLi);
+  __syncthreads();
 }
 
 // || QL^{-1} (a - F b) ||^2 with QLi = QL^{-1}; every lane gets the value.
@@ -315,33 +375,58 @@ __device__ __forceinline__ T t_objective(const Team<TS>& tm, const T* F, const T
   return tot;
 }
 
-#define POF_TEAM_PROLOGUE0(WS)                                            \
-  using B_ = TeamBlock<WS, TS>;                                           \
-  extern __shared__ __align__(16) unsigned char smem_raw_[];              \
-  const int team_in_block = threadIdx.x / TS;                             \
-  WS& ws_ = reinterpret_cast<WS*>(smem_raw_)[team_in_block];             \
-  const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;     \
-  Team<TS> tm;
+// Prologue of a level-0 kernel: the shared header (when PS is false), this
+// thread's team workspace ws_, its chunk t and the team handle; `fq` is the
+// transition model the team reads (the block's, or its own copy).
+#define POF_L0_PROLOGUE(WS, PS)                                                          \
+  constexpr int HB_ = FQHeader<T, D, PS>::bytes;                                         \
+  using B_ = TeamBlockH<WS, TS, HB_>;                                                    \
+  extern __shared__ __align__(16) unsigned char smem_raw_[];                             \
+  const int team_in_block = threadIdx.x / TS;                                            \
+  WS& ws_ = reinterpret_cast<WS*>(smem_raw_ + HB_)[team_in_block];                      \
+  const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;                    \
+  Team<TS> tm;                                                                           \
+  FQ<T, D>& fq = fq_ref<PS, T, D>(ws_, smem_raw_);
 
-template <typename T, int D, int DY, int TS>
+template <bool PS, typename T, int D, typename WS>
+__device__ __forceinline__ FQ<T, D>& fq_ref(WS& ws, unsigned char* smem) {
+  if constexpr (PS)
+    return ws.fq;
+  else
+    return *reinterpret_cast<FQ<T, D>*>(smem);
+}
+
+// Per-step transition model into the team's copy (PS), or nothing.
+template <bool PS, typename T, int TS, int D>
+__device__ __forceinline__ void fq_step(const Team<TS>& tm, FQ<T, D>& q, const StepModel& sm, int64_t s,
+                                        bool objective) {
+  if constexpr (PS) {
+    tm.sync();
+    t_load_FQ<T, TS, D>(tm, q, sm, s);
+    tm.sync();
+    if (objective) t_inv_lower<T, TS, D>(tm, q.QL, q.QLi);
+  }
+}
+
+template <typename T, int D, int DY, int TS, bool PS>
 __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* __restrict__ x0m,
                                       const T* __restrict__ x0L, T* __restrict__ out, int64_t n1) {
-  using WS = L0TeamWs<T, D, DY>;
-  POF_TEAM_PROLOGUE0(WS)
+  using WS = L0FoldWs<T, D, DY, PS>;
+  POF_L0_PROLOGUE(WS, PS)
+  if constexpr (!PS) load_fq_block<T, TS, D>(tm, fq, static_cast<const T*>(sm.F), static_cast<const T*>(sm.QL));
   if (t >= n1) return;
-  StepTeamWs<T, D, DY>& w = ws_.s;
+  StepFoldWs<T, D, DY>& w = ws_.s;
   constexpr int L1 = Ld<D>::v;
   const int64_t s0 = t * C0;
   const int64_t s1 = (s0 + C0 < n) ? s0 + C0 : n;
-  t_load_FQ<T, TS, D, DY>(tm, w, sm, s0);
   if (t == 0) {
     t_load_state_plain<T, TS, D>(tm, x0m, x0L, w.m, w.L);
     for (int64_t s = s0; s < s1; ++s) {
-      if (sm.ft_stride && s > s0) t_load_FQ<T, TS, D, DY>(tm, w, sm, s);
+      fq_step<PS, T, TS, D>(tm, fq, sm, s, false);
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
       tm.sync();
-      t_kf_step<T, TS, D, DY, false>(tm, w);
+      t_kf_step<T, TS, D, DY, false>(tm, w, fq.F, fq.QL);
     }
     t_fill<T, TS, D, D, L1>(tm, w.A, T(0), T(0));
     t_fill<T, TS, D, D, L1>(tm, w.Z, T(0), T(0));
@@ -357,33 +442,32 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
       w.eta[i] = T(0);
     }
     for (int64_t s = s0; s < s1; ++s) {
-      if (sm.ft_stride && s > s0) t_load_FQ<T, TS, D, DY>(tm, w, sm, s);
+      fq_step<PS, T, TS, D>(tm, fq, sm, s, false);
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
       tm.sync();
-      t_cond_fold_step<T, TS, D, DY>(tm, w);
+      t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL);
     }
     tm.sync();
     t_store_filt<T, TS, D>(tm, out, n1, t, w.A, w.b, w.L, w.eta, w.Z);
   }
 }
 
-template <typename T, int D, int DY, int TS>
+template <typename T, int D, int DY, int TS, bool PS>
 __global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __restrict__ states1, int64_t n1,
                                     T* __restrict__ means, T* __restrict__ chols, T* __restrict__ selems,
                                     double* __restrict__ partials) {
-  using WS = L0TeamWs<T, D, DY>;
-  POF_TEAM_PROLOGUE0(WS)
+  using WS = L0KFWs<T, D, DY, PS>;
+  POF_L0_PROLOGUE(WS, PS)
+  if constexpr (!PS) load_fq_block<T, TS, D>(tm, fq, static_cast<const T*>(sm.F), static_cast<const T*>(sm.QL));
   if (t >= n1) return;
-  StepTeamWs<T, D, DY>& w = ws_.s;
+  StepKFWs<T, D, DY>& w = ws_.s;
   using GL = SmoLayout<D>;
   constexpr int L1 = Ld<D>::v, L2 = Ld<2 * D>::v;
   const int64_t s0 = t * C0;
   const int64_t s1 = (s0 + C0 < n) ? s0 + C0 : n;
-  t_load_FQ<T, TS, D, DY>(tm, w, sm, s0);
   t_load_state<T, TS, D>(tm, states1, n1, t, w.m, w.L);
   tm.sync();
-  t_inv_lower<T, TS, D>(tm, w.QL, ws_.QLi);
   if (t == 0) {
     for (int f = tm.r; f < D + D * D; f += TS) {
       if (f < D)
@@ -394,19 +478,15 @@ __global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __
   }
   double ssq = 0.0, nll = 0.0, fobj = 0.0;
   for (int64_t s = s0; s < s1; ++s) {
-    if (sm.ft_stride && s > s0) {
-      t_load_FQ<T, TS, D, DY>(tm, w, sm, s);
-      tm.sync();
-      t_inv_lower<T, TS, D>(tm, w.QL, ws_.QLi);
-    }
+    fq_step<PS, T, TS, D>(tm, fq, sm, s, true);
     StepView<T, D, DY> v(sm, s);
     t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
     for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
     tm.sync();
-    t_kf_step<T, TS, D, DY, true>(tm, w);
+    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL);
     ssq += (double)w.sc[0];
     nll += (double)w.sc[1];
-    fobj += (double)t_objective<T, TS, D>(tm, w.F, ws_.QLi, ws_.mold, w.m, ws_.r);
+    fobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, ws_.mold, w.m, ws_.r);
     // smoother element of grid s: g, E (stored transposed in w.E), Dm = Y[:, D:]
     for (int f = tm.r; f < GL::NG; f += TS) {
       T val;
@@ -433,36 +513,22 @@ __global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __
   }
 }
 
-template <typename T, int D>
-struct SmoL0TeamWs {
-  SmoTeamWs<T, D> s;
-  T F[D * Ld<D>::v], QL[D * Ld<D>::v], QLi[D * Ld<D>::v];
-  T mnext[D], r[D];
-};
-
-template <typename T, int D, int TS>
+template <typename T, int D, int TS, bool PS>
 __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, const T* __restrict__ QL,
                                    int64_t ft_stride, const T* __restrict__ selems, const T* __restrict__ ends1,
                                    int64_t n1, T* __restrict__ means, T* __restrict__ chols,
                                    const T* __restrict__ scale, const T* __restrict__ means_old, double c_mrtol,
                                    double c_matol, double* __restrict__ partials) {
-  using WS = SmoL0TeamWs<T, D>;
-  POF_TEAM_PROLOGUE0(WS)
+  using WS = SmoL0Ws<T, D, PS>;
+  POF_L0_PROLOGUE(WS, PS)
+  if constexpr (!PS) load_fq_block<T, TS, D>(tm, fq, F, QL);
   if (t >= n1) return;
   SmoTeamWs<T, D>& w = ws_.s;
   constexpr int L1 = Ld<D>::v;
   const int64_t s0 = t * C0;
   const int64_t s1 = (s0 + C0 < n) ? s0 + C0 : n;
   const T sc = scale ? *scale : T(1);
-  auto load_FQ = [&](int64_t k) {
-    for (int f = tm.r; f < D * D; f += TS) {
-      ws_.F[(f / D) * L1 + f % D] = F[k * ft_stride + f];
-      ws_.QL[(f / D) * L1 + f % D] = QL[k * ft_stride + f];
-    }
-    tm.sync();
-    t_inv_lower<T, TS, D>(tm, ws_.QL, ws_.QLi);
-  };
-  load_FQ(s1 - 1);
+  const StepModel sm{F, QL, ft_stride, nullptr, nullptr, nullptr, 0};
   t_load_state<T, TS, D>(tm, ends1, n1, t, w.g1, w.D1);
   tm.sync();
   double sobj = 0.0, notclose = 0.0;
@@ -484,12 +550,12 @@ __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, c
       for (int f = tm.r; f < D * D; f += TS) chols[n * D * D + f] = w.D1[(f / D) * L1 + f % D] * sc;
   }
   for (int64_t k = s1 - 1; k >= s0; --k) {
-    if (ft_stride && k < s1 - 1) load_FQ(k);
+    fq_step<PS, T, TS, D>(tm, fq, sm, k, true);
     for (int i = tm.r; i < D; i += TS) ws_.mnext[i] = w.g1[i];
     t_load_smo<T, TS, D>(tm, selems, n, k, w.g2, w.E2, w.D2m);
     tm.sync();
     t_smooth_apply<T, TS, D>(tm, w);
-    sobj += (double)t_objective<T, TS, D>(tm, ws_.F, ws_.QLi, w.g1, ws_.mnext, ws_.r);
+    sobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, w.g1, ws_.mnext, ws_.r);
     close_count(k);
     for (int f = tm.r; f < D + D * D; f += TS) {
       if (f < D)
@@ -506,7 +572,8 @@ __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, c
   }
 }
 
-#undef POF_TEAM_PROLOGUE0
+#undef POF_L0_PROLOGUE
+
 #undef POF_TEAM_PROLOGUE
 
 }  // namespace pof

@@ -82,7 +82,8 @@ _SIGS = {
     "pof_ieks_mixed_workspace_bytes": (_sz, [_i64, _i32, _i32]),
     "pof_ieks_solve_mixed": (
         _c.c_int,
-        [_i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _f64, _i64, _i32, _dp, _vp, _sz, _vp],
+        [_i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _f64, _f64, _i64, _i32, _dp, _vp, _sz,
+         _vp],
     ),
     "pof_profile_enable": (None, [_i32]),
     "pof_profile_read": (_c.c_int, [_vp, _vp, _i32, _i32]),
@@ -107,8 +108,8 @@ _SIGS = {
     "pof_batch_mixed_workspace_bytes": (_sz, [_i64, _vp, _i32, _i32, _i32, _i32]),
     "pof_ieks_solve_batch_mixed": (
         _c.c_int,
-        [_i64, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _f64, _i64, _i32, _i32, _i32, _dp,
-         _dp, _vp, _sz, _vp],
+        [_i64, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _f64, _f64, _i64, _i32, _i32, _i32,
+         _dp, _dp, _vp, _sz, _vp],
     ),
 }
 

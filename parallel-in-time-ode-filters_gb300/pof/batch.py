@@ -197,7 +197,7 @@ def workspace_bytes(prep, precision="float64", C0=0, Cg=0):
 
 
 def run_batch(prep, means, chols, info, maxiters=10_000, calibrate=True, C0=0, Cg=0, workspace=None,
-              precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, info_f32=None):
+              precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, info_f32=None, settle_f32=float("inf")):
     """pof_ieks_solve_batch (precision="float64") or
     pof_ieks_solve_batch_mixed ("mixed") on prepared inputs; means (G, D)
     holds the initial trajectories on entry and the results on return.
@@ -212,6 +212,7 @@ def run_batch(prep, means, chols, info, maxiters=10_000, calibrate=True, C0=0, C
               _lib.ptr(prep["QL"]), _lib.ptr(means), _lib.ptr(chols))
     if precision == "mixed":
         rc = lib.pof_ieks_solve_batch_mixed(B, _vp(ns), D, d, _vp(fl), *common, int(maxiters_f32), float(rtol_f32),
+                                            float(settle_f32),
                                             int(maxiters), int(bool(calibrate)), int(C0), int(Cg), _lib.ptr(info),
                                             _lib.ptr(info_f32), _lib.ptr(workspace), int(workspace.numel()),
                                             _lib.stream_handle())
@@ -267,7 +268,7 @@ def project(prep, means, chols):
 
 
 def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_000, C0=0, Cg=0,
-                precision="float64", maxiters_f32=10_000, rtol_f32=1e-5):
+                precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, settle_f32=float("inf")):
     """Solve every (field name, params, y0, ts) of ``problems`` with the
     parallel IEKS of pof.solver.solve (built-in fields, constant init).
     precision="mixed": float32 iterations first, float64 polish after, per
@@ -285,7 +286,7 @@ def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_00
     info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
     info32 = torch.zeros((prep["B"], 2), dtype=torch.float64, device=dev) if precision == "mixed" else None
     run_batch(prep, means, chols, info, maxiters=maxiters, calibrate=calibrate, C0=C0, Cg=Cg, precision=precision,
-              maxiters_f32=maxiters_f32, rtol_f32=rtol_f32, info_f32=info32)
+              maxiters_f32=maxiters_f32, rtol_f32=rtol_f32, info_f32=info32, settle_f32=settle_f32)
     ym, yc = project(prep, means, chols)
     info_d = {"iterations": info[:, _lib.I_ITERATIONS].to(torch.int64), "nll": info[:, _lib.I_NLL],
               "obj": info[:, _lib.I_OBJ], "sigma_squared": info[:, _lib.I_SSQ], "calibrated": bool(calibrate)}

@@ -10,7 +10,8 @@ from .step import ieks_step
 from .utils import MVNSqrt, gmul_stack
 
 
-def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxiters_f32=10_000, rtol_f32=1e-5):
+def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxiters_f32=10_000, rtol_f32=1e-5,
+                   settle_f32=float("inf")):
     """The whole IEKS loop in libpof (pof_ieks_solve): linearization, chunked
     filter/smoother, calibration and the convergence test all on the device.
     precision="mixed": float32 iterations first, float64 polish after
@@ -37,7 +38,8 @@ def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxi
         ws = _lib.workspace(wsb, dev)
         rc = lib.pof_ieks_solve_mixed(n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]), _lib.ptr(m0),
                                       _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means), _lib.ptr(chols),
-                                      int(maxiters_f32), float(rtol_f32), int(maxiters), int(bool(calibrate)),
+                                      int(maxiters_f32), float(rtol_f32), float(settle_f32), int(maxiters),
+                                      int(bool(calibrate)),
                                       _lib.ptr(info), _lib.ptr(ws), wsb, _lib.stream_handle())
         _lib.check(rc, "pof_ieks_solve_mixed")
     else:
@@ -62,7 +64,7 @@ def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxi
 
 
 def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, sequential=False,
-          precision="float64", maxiters_f32=10_000, rtol_f32=1e-5):
+          precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, settle_f32=float("inf")):
     """Parallel-in-time IEKS (pof/solver.py:11-73).
 
     Returns (MVNSqrt(means (N, d), chol_covs (N, d, D)), info) with
@@ -83,7 +85,8 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     states = get_initial_trajectory(setup, method=init)
 
     if om.field is not None and not sequential and _lib.shape_supported(x0.mean.shape[0], setup["iwp"].wiener_process_dimension):
-        states, info_dict = _solve_builtin(setup, states, calibrate, maxiters, precision, maxiters_f32, rtol_f32)
+        states, info_dict = _solve_builtin(setup, states, calibrate, maxiters, precision, maxiters_f32, rtol_f32,
+                                           settle_f32)
         return gmul_stack(setup["E0"], states), info_dict
     if precision != "float64":
         raise NotImplementedError("precision=%r needs a built-in field (pof.ivp)" % (precision,))

@@ -208,6 +208,21 @@ def test_batch_mixed_precision(spec, q):
     assert it32.sum() > 0
 
 
+def test_batch_mixed_settled_float32_phase():
+    """settle_f32 = 0.1 (non-shrinking float32 changes counted only below a
+    10 % change): more float32 iterations, and on these well-resolved
+    problems still the float64 fixed point to 1e-6."""
+    spec, q = MIXED_D2, 3
+    ref = pbatch.solve_batch(problems(spec), order=q, maxiters=1000)
+    mix = pbatch.solve_batch(problems(spec), order=q, maxiters=1000, precision="mixed", settle_f32=0.1)
+    base = pbatch.solve_batch(problems(spec), order=q, maxiters=1000, precision="mixed")
+    assert int(mix.info["iterations_float32"].sum()) >= int(base.info["iterations_float32"].sum())
+    for b in range(len(spec)):
+        (ma, _), _ = ref.problem(b)
+        (mb, _), _ = mix.problem(b)
+        assert rel(mb.cpu().numpy(), ma.cpu().numpy()) <= 1e-6, (b, spec[b][0])
+
+
 def test_batch_mixed_independent_of_the_mix():
     full = pbatch.solve_batch(problems(MIXED_D2), order=3, maxiters=1000, C0=8, precision="mixed")
     for b in (0, 3):

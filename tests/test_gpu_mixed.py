@@ -41,11 +41,28 @@ def test_mixed_matches_float64(name, mk, N, q):
 
 
 def test_mixed_against_oracle():
-    """logistic at N = 300 is a case where float32 is too coarse for the
-    smoother (errors of O(1) even at the solution): the float32 phase must be
-    dropped and the result still match the float64 oracle."""
+    """logistic at N = 300 has two IEKS fixed points: the reference's float64
+    loop from the constant start settles on one that decays towards 0, while
+    enough float32 iterations reach the other (near the true solution 1).
+    With the default rule (non-shrinking float32 changes counted from the
+    first iteration) the float32 phase is dropped here and the result is the
+    float64 oracle's."""
     p, o = pivp.logistic(r=3.0), oivp.logistic(r=3.0)
     ts = np.linspace(0.0, 10.0, 300)
     (om, _), _ = osolver.solve(o, ts, 3, init="constant", maxiters=1000)
     mix, _ = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=3, init="constant", precision="mixed")
     assert rel(mix.mean.cpu().numpy(), om) <= 1e-6
+
+
+def test_mixed_settled_float32_phase():
+    """settle_f32 = 0.1: the float32 phase goes on through the non-monotone
+    first iterations; on Van der Pol mu = 10 (q = 4) it then does most of the
+    work and the float64 polish ends at the float64 fixed point."""
+    p = pivp.vanderpol(stiffness_constant=10.0)
+    ts = np.linspace(0.0, 6.3, 4096)
+    ref, rinfo = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=4, init="constant", maxiters=1000)
+    mix, minfo = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=4, init="constant", maxiters=1000, precision="mixed",
+                               settle_f32=0.1)
+    assert int(minfo["iterations_float32"]) > 0
+    assert int(minfo["iterations"]) < int(rinfo["iterations"])
+    assert rel(mix.mean.cpu().numpy(), ref.mean.cpu().numpy()) <= 1e-6
