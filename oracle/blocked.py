@@ -120,12 +120,29 @@ def _propagate_state(b1, U1, e2):
     return out[1][0], out[2][0]
 
 
-def _filter_states_at_starts(elems, Cs, m0, L0):
+def _filter_states_ks(elems, m0, L0):
+    """Filtering state before each element of a level by a Kogge-Stone
+    prefix scan (the kernels' parallel top level, k_filt_ks_team): step s
+    replaces P_i by P_{i-s} (x) P_i for i >= s; element 0 is absolute, so
+    (b, U) of P_{i-1} is the state before element i."""
+    n = elems[0].shape[0]
+    P = [tuple(x[i : i + 1] for x in elems) for i in range(n)]
+    s = 1
+    while s < n:
+        P = [P[i] if i < s else sqrt_filtering_operator(P[i - s], P[i]) for i in range(n)]
+        s *= 2
+    return [(m0, L0)] + [(P[i][1][0], P[i][2][0]) for i in range(n - 1)]
+
+
+def _filter_states_at_starts(elems, Cs, m0, L0, ks_max=0):
     """Given level-l elements (element 0 holds x0), return the filtering state
     before each element: element 0 starts at x0; element i > 0 starts after
-    elements 0..i-1.  Hierarchical with chunk sizes Cs."""
+    elements 0..i-1.  Hierarchical with chunk sizes Cs; a level of at most
+    ks_max (and more than 2) elements is scanned by _filter_states_ks."""
     n = elems[0].shape[0]
     C = Cs[0]
+    if 2 < n <= ks_max:
+        return _filter_states_ks(elems, m0, L0)
     if n <= C or len(Cs) == 1:
         states = [(m0, L0)]
         for i in range(n - 1):
@@ -138,7 +155,7 @@ def _filter_states_at_starts(elems, Cs, m0, L0):
     chunks = _chunks(n, C)
     totals = [_fold_general(tuple(x[s:t] for x in elems)) for s, t in chunks]
     totals = tuple(np.stack([tt[j] for tt in totals]) for j in range(5))
-    starts = _filter_states_at_starts(totals, Cs[1:], m0, L0)
+    starts = _filter_states_at_starts(totals, Cs[1:], m0, L0, ks_max)
     states = []
     for (s, t), st in zip(chunks, starts):
         cur = st
@@ -171,9 +188,10 @@ def _filter_states_segmented(elems, Cg, m0, L0):
     return states
 
 
-def filter_blocked(x0, dtm, dom, C0=4, Cs=(4,), segmented=False):
+def filter_blocked(x0, dtm, dom, C0=4, Cs=(4,), segmented=False, ks_max=0):
     """Filtered marginals with the chunked schedule; returns
-    ((means, chols), nll, obj, ssq, chunk_states).
+    ((means, chols), nll, obj, ssq, chunk_states).  ks_max: the largest level
+    scanned by a parallel prefix scan instead of the tree (0: none).
 
     segmented=True restates the batched solve's schedule for one problem
     (csrc/pof_batch.cuh): chunk 0 is a conditional fold like the others, the
@@ -199,7 +217,7 @@ def filter_blocked(x0, dtm, dom, C0=4, Cs=(4,), segmented=False):
     if segmented:
         starts = _filter_states_segmented(totals, Cs[0], m0, L0)
     else:
-        starts = _filter_states_at_starts(totals, list(Cs), m0, L0)
+        starts = _filter_states_at_starts(totals, list(Cs), m0, L0, ks_max)
     # phase 3: KF inside every chunk
     means = [m0]
     chols = [L0]
@@ -255,11 +273,33 @@ def _apply_composite(e, m, L):
     return E @ m + g, tria(np.concatenate([E @ L, D], axis=-1))
 
 
-def _smoother_states_at_ends(elems, Cs, mT, LT):
+def _smoother_ends_ks(elems, mT, LT):
+    """Smoothed state after each element of a level by a Kogge-Stone suffix
+    scan (k_smo_abs_team, k_smo_ks_team): the terminal state is pushed
+    through the last element, which becomes absolute (E = 0); step s
+    replaces S_i by S_i o S_{i+s} for i + s < n; (g, D) of S_i is then the
+    state at the start of element i, i.e. after element i - 1."""
+    n = elems[0].shape[0]
+    S = [tuple(x[i : i + 1] for x in elems) for i in range(n)]
+    g, L = _apply_composite(tuple(x[0] for x in S[-1]), mT, LT)
+    D = g.shape[-1]
+    S[-1] = (g[None], np.zeros((1, D, D)), L[None])
+    s = 1
+    while s < n:
+        S = [sqrt_smoothing_operator(S[i + s], S[i]) if i + s < n else S[i] for i in range(n)]
+        s *= 2
+    return [(S[i][0][0], S[i][2][0]) for i in range(1, n)] + [(mT, LT)]
+
+
+def _smoother_states_at_ends(elems, Cs, mT, LT, ks_max=0):
     """Smoothed state right after each element (element i maps the state at
-    its end to the state at its start); the last element ends at the terminal."""
+    its end to the state at its start); the last element ends at the terminal.
+    A level of at most ks_max (and more than 2) elements is scanned by
+    _smoother_ends_ks."""
     n = elems[0].shape[0]
     C = Cs[0]
+    if 2 < n <= ks_max:
+        return _smoother_ends_ks(elems, mT, LT)
     if n <= C or len(Cs) == 1:
         ends = [None] * n
         cur = (mT, LT)
@@ -270,7 +310,7 @@ def _smoother_states_at_ends(elems, Cs, mT, LT):
     chunks = _chunks(n, C)
     totals = [_fold_smoother(tuple(x[s:t] for x in elems)) for s, t in chunks]
     totals = tuple(np.stack([tt[j] for tt in totals]) for j in range(3))
-    cends = _smoother_states_at_ends(totals, Cs[1:], mT, LT)
+    cends = _smoother_states_at_ends(totals, Cs[1:], mT, LT, ks_max)
     ends = [None] * n
     for (s, t), ce in zip(chunks, cends):
         cur = ce
@@ -299,9 +339,10 @@ def _smoother_states_segmented(elems, Cg, mT, LT):
     return ends
 
 
-def smoother_blocked(dtm, filt, C0=4, Cs=(4,), segmented=False):
+def smoother_blocked(dtm, filt, C0=4, Cs=(4,), segmented=False, ks_max=0):
     """Smoothed marginals with the chunked schedule; returns ((means, chols), obj).
-    segmented=True: the batched solve's hierarchy (see filter_blocked)."""
+    segmented=True: the batched solve's hierarchy (see filter_blocked); ks_max
+    as in filter_blocked."""
     F, QL = dtm
     fm, fL = filt
     N, D = fm.shape
@@ -317,7 +358,7 @@ def smoother_blocked(dtm, filt, C0=4, Cs=(4,), segmented=False):
     if segmented:
         ends = _smoother_states_segmented(totals, Cs[0], fm[-1], fL[-1])
     else:
-        ends = _smoother_states_at_ends(totals, list(Cs), fm[-1], fL[-1])
+        ends = _smoother_states_at_ends(totals, list(Cs), fm[-1], fL[-1], ks_max)
     means = np.zeros((N, D))
     chols = np.zeros((N, D, D))
     means[-1], chols[-1] = fm[-1], fL[-1]
@@ -334,10 +375,10 @@ def smoother_blocked(dtm, filt, C0=4, Cs=(4,), segmented=False):
     return (means, chols), sum(obj_c)
 
 
-def linear_filtsmooth_blocked(x0, dtm, dom, C0=4, Cs=(4,), segmented=False):
+def linear_filtsmooth_blocked(x0, dtm, dom, C0=4, Cs=(4,), segmented=False, ks_max=0):
     """``pof/parallel_filtsmooth/__init__.py:5-10`` with the chunked schedule."""
-    out, nll, _, ssq, _ = filter_blocked(x0, dtm, dom, C0=C0, Cs=Cs, segmented=segmented)
-    out, obj = smoother_blocked(dtm, out, C0=C0, Cs=Cs, segmented=segmented)
+    out, nll, _, ssq, _ = filter_blocked(x0, dtm, dom, C0=C0, Cs=Cs, segmented=segmented, ks_max=ks_max)
+    out, obj = smoother_blocked(dtm, out, C0=C0, Cs=Cs, segmented=segmented, ks_max=ks_max)
     return out, nll, obj, ssq
 
 

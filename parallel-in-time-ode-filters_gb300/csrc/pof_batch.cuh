@@ -115,7 +115,7 @@ __global__ void kb_filt_l0_reduce(BView v, const T* __restrict__ F, const T* __r
   for (int64_t s = s0; s < s1; ++s) {
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     tm.sync();
-    t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL);
+    t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL, fq.wq, true);
   }
   tm.sync();
   t_store_filt<T, TS, D>(tm, out, v.n1, t, w.A, w.b, w.L, w.eta, w.Z);
@@ -218,7 +218,7 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
     tm.sync();
-    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL);
+    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL, fq.wq, true);
     ssq += (double)w.sc[0];
     nll += (double)w.sc[1];
     fobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, ws_.mold, w.m, ws_.r);

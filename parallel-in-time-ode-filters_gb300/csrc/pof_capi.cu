@@ -45,14 +45,20 @@ const Ops* find_ops(int dtype, int D, int DY) {
 int esz(int dtype) { return dtype == POF_F32 ? 4 : 8; }
 
 // Optional overrides (tuning): POF_C0, POF_CG chunk sizes; POF_TEAM_WIDE_L0=1
-// runs level 0 with the wide team kernels.
-int env_int(const char* name) {
+// runs level 0 with the wide team kernels; POF_KS the largest top level
+// scanned in parallel (ks_limit: 0, the default, always the binary tree up to
+// kTop elements; -1 the lane-count rule).  In the float32 iterations of the
+// mixed-precision solve the parallel top also settles higher (Van der Pol
+// mu = 10, q = 4, N = 4096: smallest float32 change 2.0e-3 with a 512-element
+// parallel top, 6.5e-4 with the tree).
+int env_int(const char* name, int dflt = 0) {
   const char* v = getenv(name);
-  return v ? atoi(v) : 0;
+  return v ? atoi(v) : dflt;
 }
 
 Plan plan_for(int dtype, int64_t n, int D, int DY, bool solver) {
-  return make_plan(n, D, DY, esz(dtype), solver, env_int("POF_C0"), env_int("POF_CG"), env_int("POF_TEAM_WIDE_L0") != 0);
+  return make_plan(n, D, DY, esz(dtype), solver, env_int("POF_C0"), env_int("POF_CG"),
+                   env_int("POF_TEAM_WIDE_L0") != 0, env_int("POF_KS", 0));
 }
 
 int check_common(int dtype, int64_t n, int D, int DY, const Ops** ops) {

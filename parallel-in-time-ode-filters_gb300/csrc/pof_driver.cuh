@@ -184,7 +184,18 @@ struct Driver {
       launch_team<FWS, TU>(k_filt_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
                            p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
     }
-    {
+    if (p.ks) {
+      // parallel scan of the top level, ping-ponging between its element
+      // buffer and ksbuf; the last step writes the states
+      const int64_t K = p.cnt[p.nlev];
+      T* bufs[2] = {b.template at<T>(p.felem[p.nlev]), b.template at<T>(p.ksbuf)};
+      int cur = 0;
+      for (int64_t s = 1; s < K; s *= 2, cur ^= 1) {
+        ProfScope ps(PK_FILT_TOP, st);
+        launch_team<FWS, TU>(k_filt_ks_team<T, D, TU>, K, st, (const T*)bufs[cur], K, s, (int)(2 * s >= K),
+                             bufs[cur ^ 1], b.template at<T>(p.fstate[p.nlev]), x0m, x0L);
+      }
+    } else {
       ProfScope ps(PK_FILT_TOP, st);
       launch_team<FWS, TU>(k_filt_top_team<T, D, TU>, 1, st, (const T*)b.template at<T>(p.felem[p.nlev]),
                            p.cnt[p.nlev], x0m, x0L, b.template at<T>(p.fstate[p.nlev]));
@@ -241,7 +252,22 @@ struct Driver {
       launch_team<SWS, TU>(k_smo_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
                            p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
     }
-    {
+    if (p.ks) {
+      const int64_t K = p.cnt[p.nlev];
+      const T* mT = means + n * D;
+      const T* LT = chols + n * D * D;
+      T* bufs[2] = {b.template at<T>(p.gelem[p.nlev]), b.template at<T>(p.ksbuf)};
+      {
+        ProfScope ps(PK_SMO_TOP, st);
+        launch_team<SWS, TU>(k_smo_abs_team<T, D, TU>, 1, st, bufs[0], K, mT, LT);
+      }
+      int cur = 0;
+      for (int64_t s = 1; s < K; s *= 2, cur ^= 1) {
+        ProfScope ps(PK_SMO_TOP, st);
+        launch_team<SWS, TU>(k_smo_ks_team<T, D, TU>, K, st, (const T*)bufs[cur], K, s, (int)(2 * s >= K),
+                             bufs[cur ^ 1], b.template at<T>(p.gend[p.nlev]), mT, LT);
+      }
+    } else {
       ProfScope ps(PK_SMO_TOP, st);
       launch_team<SWS, TU>(k_smo_top_team<T, D, TU>, 1, st, (const T*)b.template at<T>(p.gelem[p.nlev]),
                            p.cnt[p.nlev], (const T*)(means + n * D), (const T*)(chols + n * D * D),

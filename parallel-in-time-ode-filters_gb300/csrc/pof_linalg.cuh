@@ -26,43 +26,51 @@ namespace pof {
 // SM sub-partition's FP64 pipe for the same time however many of its lanes
 // are active, so the instruction sequences of IEEE double division and
 // square root -- computed once per reflector, often on one lane -- are a
-// large share of a small factorization's FP64 instructions.  These start
-// from a single-precision hardware approximation on an exponent-normalized
-// argument (FP32 pipe, integer exponent arithmetic) and take two
-// Newton-Raphson steps in double precision, each of which squares the
-// relative error (y <- y + y (1 - a y) for 1/a; y <- y + y (1 - a y^2) / 2
-// for 1/sqrt(a)): from the seed's ~2^-22 to below double rounding, so the
-// result is within a few units in the last place of the correctly rounded
-// value.  Arguments whose binary exponent is beyond +-1000 (zero,
-// subnormals, infinities, NaN included) take the IEEE operations.
+// large share of a small factorization's FP64 instructions.  These take a
+// single-precision hardware approximation of the exponent-normalized
+// argument as the seed (the float operand and the widened result are built
+// with integer operations, so no FP64 conversion is issued), then ONE
+// third-order correction in double precision (Householder's iteration of
+// order 3; Halley's method for the square root):
+//   1/a:       r = 1 - a y,     y <- y (1 + r + r^2)
+//   1/sqrt(a): r = 1 - a y^2,   y <- y (1 + r/2 + 3 r^2/8)
+// which cubes the seed's relative error (below ~4e-7: truncation of the
+// argument to 23 fraction bits plus the approximation) to below 1e-19, so
+// the result is within a few units in the last place of the correctly
+// rounded value: 3 and 5 FP64 instructions.  Arguments whose binary
+// exponent is beyond +-1000 (zero, subnormals, infinities, NaN included)
+// take the IEEE operations.
 // ---------------------------------------------------------------------------
+
+// double with the sign bit `sign`, binary exponent `e` and the fraction of
+// the float f (exact)
+__device__ __forceinline__ double widen_with_exp(float f, int e, long long sign) {
+  const unsigned fb = __float_as_uint(f);
+  const long long ex = (long long)((int)((fb >> 23) & 0xff) - 127 + e + 1023) << 52;
+  return __longlong_as_double(sign | ex | ((long long)(fb & 0x7fffff) << 29));
+}
+
 __device__ __forceinline__ double rcp_nr(double a) {
   const long long bits = __double_as_longlong(a);
   const int e = (int)((bits >> 52) & 0x7ff) - 1023;
   if (e < -1000 || e > 1000) return 1.0 / a;
-  // m = a with exponent 0 (|m| in [1, 2), sign of a); 1/a = (1/m) 2^-e
-  const double m = __longlong_as_double((bits & ~(0x7ffLL << 52)) | (1023LL << 52));
-  double y = (double)__frcp_rn((float)m);
-  y = __longlong_as_double(__double_as_longlong(y) - ((long long)e << 52));
-  double r = fma(-a, y, 1.0);
-  y = fma(y, r, y);
-  r = fma(-a, y, 1.0);
-  return fma(y, r, y);
+  // |a| = m 2^e, m in [1, 2): seed 1/m in single precision, times 2^-e
+  const float mf = __int_as_float(0x3f800000 | (int)((bits >> 29) & 0x7fffff));
+  const double y = widen_with_exp(__frcp_rn(mf), -e, bits & (1LL << 63));
+  const double r = fma(-a, y, 1.0);
+  return fma(y, fma(r, r, r), y);
 }
 
 __device__ __forceinline__ double rsqrt_nr(double a) {
   const long long bits = __double_as_longlong(a);
   const int e = (int)((bits >> 52) & 0x7ff) - 1023;
   if (e < -1000 || e > 1000 || bits < 0) return 1.0 / sqrt(a);
-  // a = m 4^k with m in [1, 4); 1/sqrt(a) = (1/sqrt(m)) 2^-k
+  // a = m 4^k with m in [1, 4): seed 1/sqrt(m) in single precision, times 2^-k
   const int k = e >> 1;
-  const double m = __longlong_as_double((bits & ((1LL << 52) - 1)) | ((long long)(1023 + e - 2 * k) << 52));
-  double y = (double)rsqrtf((float)m);
-  y = __longlong_as_double(__double_as_longlong(y) - ((long long)k << 52));
-  double r = fma(-(a * y), y, 1.0);
-  y = fma(0.5 * y, r, y);
-  r = fma(-(a * y), y, 1.0);
-  return fma(0.5 * y, r, y);
+  const float mf = __int_as_float(((127 + e - 2 * k) << 23) | (int)((bits >> 29) & 0x7fffff));
+  const double y = widen_with_exp(rsqrtf(mf), -k, 0);
+  const double r = fma(-(a * y), y, 1.0);
+  return fma(y, r * fma(r, 0.375, 0.5), y);
 }
 
 template <typename T>
@@ -84,11 +92,12 @@ __device__ __forceinline__ void householder(T alpha, T xn2, T& beta, T& tau, T& 
   if constexpr (std::is_same<T, double>::value) {
     const double a2 = fma(alpha, alpha, xn2);
     const double g = rsqrt_nr(a2);  // 1 / ||(alpha, x)||
-    const double sgn = alpha >= 0.0 ? -1.0 : 1.0;
-    const double b = sgn * (a2 * g);
+    // sg = -sign(alpha) g = 1 / beta (sign flipped with an integer operation)
+    const double sg = __longlong_as_double(__double_as_longlong(g) ^ (alpha >= 0.0 ? (1LL << 63) : 0LL));
+    const double b = a2 * sg;  // beta = -sign(alpha) ||(alpha, x)||
     const double u = alpha - b;
     beta = zero ? alpha : b;
-    tau = zero ? 0.0 : -u * (sgn * g);  // (beta - alpha) / beta, 1 / beta = sgn g
+    tau = zero ? 0.0 : -u * sg;  // (beta - alpha) / beta
     scal = zero ? 0.0 : rcp_nr(u);
   } else {
     const T nrm = sqrt(fma(alpha, alpha, xn2));

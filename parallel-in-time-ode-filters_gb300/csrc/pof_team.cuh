@@ -76,16 +76,31 @@ __device__ __forceinline__ void t_mv(const Team<TS>& tm, const T* A, const T* x,
 // reflectors and sign conventions as pof::tria (LAPACK dgeqr2/dlarfg).
 // The norm is a team reduction over columns; the row updates run one row per
 // lane.  Zeroes X's tails at the end.
+//
+// wlow > 0 declares X = [X1, X2] with X2 = X[:, wlow:] lower-triangular and
+// Y[:, wlow:] zero (the shape of every tria([A, L]) of the filter and
+// smoother: [F L, QL], [U1^T Z2, I], [M^T, U2], [E L, D], ...).  Reflector j
+// then has no entry beyond column wlow + j (row j of X2 starts with j + 1
+// nonzeros and the earlier reflectors only fill columns below wlow + j), so
+// its norm, the dot products and the row updates stop there: the same
+// arithmetic without the exact zeros.  ncut < NC declares the columns from
+// ncut on zero in every row (the observation block [[H Lp, 0], [Lp, 0]] of a
+// noiseless update): they stay zero, and the reflectors from ncut - 1 on
+// have an empty tail (no reflection: LAPACK's tau = 0, beta = alpha), so
+// they are skipped.
 template <typename T, int TS, int M, int MB, int NC, int LD, int LDY>
-__device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y) {
+__device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y, int wlow = 0, int ncut = NC) {
   const int src = (threadIdx.x & 31) / TS * TS;  // lane 0 of this team within the warp
+  const int mlim = (ncut < NC && ncut - 1 < M) ? ncut - 1 : M;
 #pragma unroll 1
-  for (int j = 0; j < M; ++j) {
+  for (int j = 0; j < mlim; ++j) {
     T* xj = X + j * LD;
+    int kend = (wlow > 0 && wlow + j + 1 < NC) ? wlow + j + 1 : NC;
+    if (ncut < kend) kend = ncut;
     tm.sync();
     // ||x[j, j+1:]||^2: column partials, reduced across the team
     T part = T(0);
-    for (int k = j + 1 + tm.r; k < NC; k += TS) part = fma(xj[k], xj[k], part);
+    for (int k = j + 1 + tm.r; k < kend; k += TS) part = fma(xj[k], xj[k], part);
     const T xn2 = tm.sum(part);
     // the reflector's scalars on one lane (a square root and two divisions
     // are long FP64 sequences), then broadcast
@@ -94,17 +109,17 @@ __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y) {
     tau = __shfl_sync(tm.mask, tau, src);
     scal = __shfl_sync(tm.mask, scal, src);
     tm.sync();
-    for (int k = j + 1 + tm.r; k < NC; k += TS) xj[k] *= scal;
+    for (int k = j + 1 + tm.r; k < kend; k += TS) xj[k] *= scal;
     if (tm.r == 0) xj[j] = beta;
     tm.sync();
     // rows below j (X rows j+1..M-1, then Y rows 0..MB-1): one row per lane
     for (int rr = tm.r; rr < (M - j - 1) + MB; rr += TS) {
       T* xi = (rr < M - j - 1) ? X + (j + 1 + rr) * LD : Y + (rr - (M - j - 1)) * LDY;
       T w = xi[j];
-      for (int k = j + 1; k < NC; ++k) w = fma(xi[k], xj[k], w);
+      for (int k = j + 1; k < kend; ++k) w = fma(xi[k], xj[k], w);
       w *= tau;
       xi[j] -= w;
-      for (int k = j + 1; k < NC; ++k) xi[k] = fma(-w, xj[k], xi[k]);
+      for (int k = j + 1; k < kend; ++k) xi[k] = fma(-w, xj[k], xi[k]);
     }
   }
   tm.sync();
@@ -231,7 +246,7 @@ __device__ __forceinline__ void t_filt_combine(const Team<TS>& tm, FiltTeamWs<T,
   t_fill<T, TS, D, D, L2>(tm, w.Xt + D, T(0), T(1));
   t_copy<T, TS, D, D, L1, L2>(tm, w.Z2, w.Xb);
   t_fill<T, TS, D, D, L2>(tm, w.Xb + D, T(0), T(0));
-  t_tria<T, TS, D, D, D2, L2, L2>(tm, w.Xt, w.Xb);      // Xi11 = Xt[:, :D], Xi21 = Xb[:, :D]
+  t_tria<T, TS, D, D, D2, L2, L2>(tm, w.Xt, w.Xb, D);   // Xi11 = Xt[:, :D], Xi21 = Xb[:, :D]
   t_tria<T, TS, D, 0, D, L2, L2>(tm, w.Xb + D, w.Xb);  // Xi22 = Xb[:, D:]
   // M = Xi11^{-1} U1^T A2^T ; Mu = Xi11^{-1} U1^T
   t_mm<T, TS, D, D, D, L1, L1, L1, true, true>(tm, w.U1, w.A2, w.M);
@@ -293,8 +308,8 @@ __device__ __forceinline__ void t_filt_combine(const Team<TS>& tm, FiltTeamWs<T,
   tm.sync();
   t_copy<T, TS, D, D, L1, L2, true>(tm, w.M, w.UX);
   t_copy<T, TS, D, D, L1, L2>(tm, w.U2, w.UX + D);
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.UX, w.UX);
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.Xt, w.Xt);
+  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.UX, w.UX, D);
+  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.Xt, w.Xt, D);
   t_copy<T, TS, D, D, L2, L1>(tm, w.UX, w.U1);
   t_copy<T, TS, D, D, L2, L1>(tm, w.Xt, w.Z1);
   tm.sync();
@@ -310,7 +325,7 @@ __device__ __forceinline__ void t_filt_apply(const Team<TS>& tm, FiltTeamWs<T, D
   t_fill<T, TS, D, D, L2>(tm, w.Xt + D, T(0), T(1));
   t_copy<T, TS, D, D, L1, L2>(tm, w.Z2, w.Xb);
   t_fill<T, TS, D, D, L2>(tm, w.Xb + D, T(0), T(0));
-  t_tria<T, TS, D, D, D2, L2, L2>(tm, w.Xt, w.Xb);
+  t_tria<T, TS, D, D, D2, L2, L2>(tm, w.Xt, w.Xb, D);
   t_mm<T, TS, D, D, D, L1, L1, L1, true, true>(tm, w.U1, w.A2, w.M);
   t_copy<T, TS, D, D, L1, L1, true>(tm, w.U1, w.Mu);
   tm.sync();
@@ -334,7 +349,7 @@ __device__ __forceinline__ void t_filt_apply(const Team<TS>& tm, FiltTeamWs<T, D
   t_copy<T, TS, D, D, L1, L2>(tm, w.U2, w.UX + D);
   tm.sync();
   for (int i = tm.r; i < D; i += TS) w.b1[i] = w.v3[i] + w.b2[i];
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.UX, w.UX);
+  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.UX, w.UX, D);
   t_copy<T, TS, D, D, L2, L1>(tm, w.UX, w.U1);
   tm.sync();
 }
@@ -362,7 +377,7 @@ __device__ __forceinline__ void t_smooth_combine(const Team<TS>& tm, SmoTeamWs<T
   t_copy<T, TS, D, D, L1, L2>(tm, w.D2m, w.X + D);
   t_mm<T, TS, D, D, D, L1, L1, L1>(tm, w.E2, w.E1, w.En);
   tm.sync();
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X);
+  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X, D);
   for (int i = tm.r; i < D; i += TS) w.g2[i] += w.v[i];
   t_copy<T, TS, D, D, L1, L1>(tm, w.En, w.E2);
   t_copy<T, TS, D, D, L2, L1>(tm, w.X, w.D2m);
@@ -378,7 +393,7 @@ __device__ __forceinline__ void t_smooth_apply(const Team<TS>& tm, SmoTeamWs<T, 
   t_mm<T, TS, D, D, D, L1, L1, L2>(tm, w.E2, w.D1, w.X);
   t_copy<T, TS, D, D, L1, L2>(tm, w.D2m, w.X + D);
   tm.sync();
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X);
+  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X, D);
   for (int i = tm.r; i < D; i += TS) w.g1[i] = w.v[i] + w.g2[i];
   t_copy<T, TS, D, D, L2, L1>(tm, w.X, w.D1);
   tm.sync();
@@ -439,9 +454,10 @@ __device__ __forceinline__ void t_load_step(const Team<TS>& tm, WS& w, const T* 
 }
 
 // Psi = tria([[H Lp, R], [Lp, 0]]) with Lp = X[:, :D]; then r = H mp + c,
-// ssq / nll terms, m <- mp + Psi21 Psi11^{-1} (-r), L <- Psi22.
+// ssq / nll terms, m <- mp + Psi21 Psi11^{-1} (-r), L <- Psi22.  rzero: R is
+// zero (noiseless observation, the EK1 model), so Psi's last DY columns are.
 template <typename T, int TS, int D, int DY, bool UPDATE_STATE, typename WS>
-__device__ __forceinline__ void t_update(const Team<TS>& tm, WS& w) {
+__device__ __forceinline__ void t_update(const Team<TS>& tm, WS& w, bool rzero) {
   using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, LP = W::LDP, DP = W::DP;
   // rows 0..DY-1: [H Lp, R]; rows DY..: [Lp, 0]
@@ -458,7 +474,7 @@ __device__ __forceinline__ void t_update(const Team<TS>& tm, WS& w) {
     w.P[(DY + i) * LP + j] = (j < D) ? w.X[i * L2 + j] : T(0);
   }
   tm.sync();
-  t_tria<T, TS, DP, 0, DP, LP, LP>(tm, w.P, w.P);
+  t_tria<T, TS, DP, 0, DP, LP, LP>(tm, w.P, w.P, 0, rzero ? D : DP);
   if constexpr (UPDATE_STATE) {
     // the DY x DY solves are tiny: every lane does them redundantly
     T r[DY], wv[DY], wq[DY];
@@ -498,9 +514,11 @@ __device__ __forceinline__ void t_update(const Team<TS>& tm, WS& w) {
 
 // One square-root KF step from the filtered state (m, L) at grid s, fused with
 // the smoother element (g, E, Dm = Y[:, D:]) of grid s when SMOOTH.  F and
-// QL (D x D, leading dimension Ld<D>) are the step's transition model.
+// QL (D x D, leading dimension Ld<D>) are the step's transition model; wq = D
+// when QL is lower-triangular (t_tria's wlow), else 0; rzero as in t_update.
 template <typename T, int TS, int D, int DY, bool SMOOTH, typename WS>
-__device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F, const T* QL) {
+__device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F, const T* QL, int wq,
+                                          bool rzero) {
   using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, D2 = W::D2;
   t_mm<T, TS, D, D, D, L1, L1, L2>(tm, F, w.L, w.X);
@@ -510,7 +528,7 @@ __device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F,
     t_copy<T, TS, D, D, L1, L2>(tm, w.L, w.Y);
     t_fill<T, TS, D, D, L2>(tm, w.Y + D, T(0), T(0));
     tm.sync();
-    t_tria<T, TS, D, D, D2, L2, L2>(tm, w.X, w.Y);   // Phi11, Phi21
+    t_tria<T, TS, D, D, D2, L2, L2>(tm, w.X, w.Y, wq);  // Phi11, Phi21
     t_tria<T, TS, D, 0, D, L2, L2>(tm, w.Y + D, w.Y);  // Phi22
     // E^T = Phi11^{-T} Phi21^T  (E stored transposed in w.E, fixed below)
     t_copy<T, TS, D, D, L2, L1, true>(tm, w.Y, w.E);
@@ -523,15 +541,15 @@ __device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F,
     for (int i = tm.r; i < D; i += TS) w.g[i] = w.m[i] - w.g[i];
   } else {
     tm.sync();
-    t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X);
+    t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X, wq);
   }
-  t_update<T, TS, D, DY, true>(tm, w);
+  t_update<T, TS, D, DY, true>(tm, w, rzero);
 }
 
 // One step of the conditional fold (cond_fold_step of pof_ops.cuh).
 template <typename T, int TS, int D, int DY>
 __device__ __forceinline__ void t_cond_fold_step(const Team<TS>& tm, StepFoldWs<T, D, DY>& w, const T* F,
-                                                 const T* QL) {
+                                                 const T* QL, int wq, bool rzero) {
   using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, LP = W::LDP, LZ = W::LDZ, D2 = W::D2;
   t_mm<T, TS, D, D, D, L1, L1, L2>(tm, F, w.L, w.X);
@@ -539,8 +557,8 @@ __device__ __forceinline__ void t_cond_fold_step(const Team<TS>& tm, StepFoldWs<
   t_mm<T, TS, D, D, D, L1, L1, L1>(tm, F, w.A, w.FA);
   t_mv<T, TS, D, D, L1>(tm, F, w.b, w.Fb);
   tm.sync();
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X);
-  t_update<T, TS, D, DY, false>(tm, w);
+  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X, wq);
+  t_update<T, TS, D, DY, false>(tm, w, rzero);
   // W = H FA (DY x D), w = H Fb + c, then Psi11^{-1} on both
   t_mm<T, TS, DY, D, D, L1, L1, L1>(tm, w.H, w.FA, w.W);
   for (int i = tm.r; i < DY; i += TS) {

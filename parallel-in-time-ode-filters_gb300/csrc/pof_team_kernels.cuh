@@ -259,6 +259,91 @@ __global__ void k_smo_top_team(const T* __restrict__ elems, int64_t n, const T* 
 }
 
 // ---------------------------------------------------------------------------
+// Parallel scan of the top level (Kogge-Stone), one team per element.
+// Element 0 of a level is absolute (it holds x0), so the prefix
+// P_i = E_0 (x) ... (x) E_i carries the state after element i in its (b, U);
+// step s computes P_i <- P_{i-s} (x) P_i for i >= s.  The last step writes
+// the states before each element (states[0] = x0, states[i] = (b, U) of
+// P_{i-1}) instead of the elements.  Same result as the binary tree up to
+// rounding (another bracketing of the same associative operator,
+// pof/parallel_filtsmooth/filter.py:117-142).
+// ---------------------------------------------------------------------------
+template <typename T, int D, int TS>
+__global__ void k_filt_ks_team(const T* __restrict__ in, int64_t K, int64_t s, int last, T* __restrict__ out,
+                               T* __restrict__ states, const T* __restrict__ x0m, const T* __restrict__ x0L) {
+  using WS = FiltTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t >= K || (last && t + 1 >= K && t != 0)) return;  // P_{K-1} is not needed
+  if (t >= s) {
+    t_load_filt<T, TS, D>(tm, in, K, t - s, w.A1, w.b1, w.U1, w.e1, w.Z1);
+    t_load_filt<T, TS, D>(tm, in, K, t, w.A2, w.b2, w.U2, w.e2, w.Z2);
+    tm.sync();
+    t_filt_combine<T, TS, D>(tm, w);
+  } else {
+    t_load_filt<T, TS, D>(tm, in, K, t, w.A1, w.b1, w.U1, w.e1, w.Z1);
+  }
+  tm.sync();
+  if (!last) {
+    t_store_filt<T, TS, D>(tm, out, K, t, w.A1, w.b1, w.U1, w.e1, w.Z1);
+    return;
+  }
+  if (t + 1 < K) t_store_state<T, TS, D>(tm, states, K, t + 1, w.b1, w.U1);
+  if (t == 0) {
+    t_load_state_plain<T, TS, D>(tm, x0m, x0L, w.b2, w.U2);
+    tm.sync();
+    t_store_state<T, TS, D>(tm, states, K, 0, w.b2, w.U2);
+  }
+}
+
+// The last element of the smoother's top level made absolute: the terminal
+// state (mT, LT) pushed through it, stored as (g = m, E = 0, Dm = L).
+template <typename T, int D, int TS>
+__global__ void k_smo_abs_team(T* __restrict__ elems, int64_t K, const T* __restrict__ mT,
+                               const T* __restrict__ LT) {
+  using WS = SmoTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t != 0) return;
+  t_load_state_plain<T, TS, D>(tm, mT, LT, w.g1, w.D1);
+  t_load_smo<T, TS, D>(tm, elems, K, K - 1, w.g2, w.E2, w.D2m);
+  tm.sync();
+  t_smooth_apply<T, TS, D>(tm, w);
+  t_fill<T, TS, D, D, Ld<D>::v>(tm, w.E2, T(0), T(0));
+  tm.sync();
+  t_store_smo<T, TS, D>(tm, elems, K, K - 1, w.g1, w.E2, w.D1);
+}
+
+// Suffix scan of the smoother's top level after k_smo_abs_team: S_i <- S_i o
+// S_{i+s} for i + s < K (pof/parallel_filtsmooth/smoother.py:53-63); S_i is
+// absolute and its (g, Dm) is the state at the start of block i.  The last
+// step writes ends[i - 1] = (g, Dm) of S_i and ends[K - 1] = (mT, LT).
+template <typename T, int D, int TS>
+__global__ void k_smo_ks_team(const T* __restrict__ in, int64_t K, int64_t s, int last, T* __restrict__ out,
+                              T* __restrict__ ends, const T* __restrict__ mT, const T* __restrict__ LT) {
+  using WS = SmoTeamWs<T, D>;
+  POF_TEAM_PROLOGUE(WS)
+  if (t >= K || (last && t == 0 && K > 1)) return;  // S_0 is not needed
+  if (t + s < K) {
+    t_load_smo<T, TS, D>(tm, in, K, t, w.g2, w.E2, w.D2m);
+    t_load_smo<T, TS, D>(tm, in, K, t + s, w.g1, w.E1, w.D1);
+    tm.sync();
+    t_smooth_combine<T, TS, D>(tm, w);
+  } else {
+    t_load_smo<T, TS, D>(tm, in, K, t, w.g2, w.E2, w.D2m);
+  }
+  tm.sync();
+  if (!last) {
+    t_store_smo<T, TS, D>(tm, out, K, t, w.g2, w.E2, w.D2m);
+    return;
+  }
+  t_store_state<T, TS, D>(tm, ends, K, t - 1, w.g2, w.D2m);
+  if (t == K - 1) {
+    t_load_state_plain<T, TS, D>(tm, mT, LT, w.g1, w.D1);
+    tm.sync();
+    t_store_state<T, TS, D>(tm, ends, K, K - 1, w.g1, w.D1);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Level 0 with teams (large D, where per-thread state does not fit registers)
 // ---------------------------------------------------------------------------
 
@@ -269,6 +354,7 @@ __global__ void k_smo_top_team(const T* __restrict__ elems, int64_t n, const T* 
 template <typename T, int D>
 struct FQ {
   T F[D * Ld<D>::v], QL[D * Ld<D>::v], QLi[D * Ld<D>::v];
+  int wq;  // D when QL is lower-triangular (t_tria's wlow for [F L, QL]), else 0
 };
 
 template <typename Base, typename T, int D, bool PS>
@@ -321,10 +407,14 @@ __device__ __forceinline__ void t_load_FQ(const Team<TS>& tm, FQ<T, D>& q, const
   constexpr int L1 = Ld<D>::v;
   const T* F = static_cast<const T*>(sm.F) + s * sm.ft_stride;
   const T* QL = static_cast<const T*>(sm.QL) + s * sm.ft_stride;
+  bool upper = false;
   for (int f = tm.r; f < D * D; f += TS) {
     q.F[(f / D) * L1 + f % D] = F[f];
     q.QL[(f / D) * L1 + f % D] = QL[f];
+    upper |= (f % D > f / D) && QL[f] != T(0);
   }
+  const bool any_upper = __any_sync(tm.mask, upper);
+  if (tm.r == 0) q.wq = any_upper ? 0 : D;
 }
 
 // QL^{-1} by forward substitution on the identity (objective terms)
@@ -342,11 +432,14 @@ __device__ __forceinline__ void t_inv_lower(const Team<TS>& tm, const T* QL, T* 
 template <typename T, int TS, int D>
 __device__ __forceinline__ void load_fq_block(const Team<TS>& tm, FQ<T, D>& q, const T* F, const T* QL) {
   constexpr int L1 = Ld<D>::v;
+  int upper = 0;
   for (int f = threadIdx.x; f < D * D; f += blockDim.x) {
     q.F[(f / D) * L1 + f % D] = F[f];
     q.QL[(f / D) * L1 + f % D] = QL[f];
+    upper |= (f % D > f / D) && QL[f] != T(0);
   }
-  __syncthreads();
+  upper = __syncthreads_or(upper);
+  if (threadIdx.x == 0) q.wq = upper ? 0 : D;
   if (threadIdx.x < TS) t_inv_lower<T, TS, D>(tm, q.QL, q.QLi);
   __syncthreads();
 }
@@ -426,7 +519,7 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
       tm.sync();
-      t_kf_step<T, TS, D, DY, false>(tm, w, fq.F, fq.QL);
+      t_kf_step<T, TS, D, DY, false>(tm, w, fq.F, fq.QL, fq.wq, sm.R == nullptr);
     }
     t_fill<T, TS, D, D, L1>(tm, w.A, T(0), T(0));
     t_fill<T, TS, D, D, L1>(tm, w.Z, T(0), T(0));
@@ -446,7 +539,7 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
       tm.sync();
-      t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL);
+      t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL, fq.wq, sm.R == nullptr);
     }
     tm.sync();
     t_store_filt<T, TS, D>(tm, out, n1, t, w.A, w.b, w.L, w.eta, w.Z);
@@ -483,7 +576,7 @@ __global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __
     t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
     for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
     tm.sync();
-    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL);
+    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL, fq.wq, sm.R == nullptr);
     ssq += (double)w.sc[0];
     nll += (double)w.sc[1];
     fobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, ws_.mold, w.m, ws_.r);

@@ -157,6 +157,26 @@ def test_ragged_sizes(n):
     assert close(gssq, ossq, sssq)
 
 
+@pytest.mark.parametrize("key,ks", [("fhn_q3", "4"), ("vdp_q3", "-1"), ("logistic_q5", "3"), ("rigid_q2", "-1")])
+def test_parallel_top_matches_tree(key, ks, monkeypatch):
+    """The binary tree to the end (the default) and the top level scanned in
+    parallel (POF_KS: -1 the lane-count rule, else the largest such level)
+    are two bracketings of the same scan: both within the parity tolerance of
+    the oracle, and of each other."""
+    st, dtm, dom = problem(key)
+    (om, oL), onll, oobj, _ = ofs.linear_filtsmooth(st.x0, dtm, dom)
+    (_, _), sell, sobj, _ = ofs.sequential_linear_filtsmooth(st.x0, dtm, dom)
+    args = gpu_args(st, dtm, dom)
+    (am, aL), anll, aobj, _ = pfs.linear_filtsmooth(*args)
+    monkeypatch.setenv("POF_KS", ks)
+    (bm, bL), bnll, bobj, _ = pfs.linear_filtsmooth(*args)
+    for m, L, nll, obj in ((am, aL, anll, aobj), (bm, bL, bnll, bobj)):
+        assert rel(N_(m), om) <= TOL and covrel(N_(L), oL) <= TOL
+        assert close(nll, onll, -sell)
+        assert close(obj, oobj, sobj)
+    assert rel(N_(am), N_(bm)) <= TOL and covrel(N_(aL), N_(bL)) <= TOL
+
+
 def test_deterministic():
     st, dtm, dom = problem("fhn_q3")
     args = gpu_args(st, dtm, dom)
@@ -201,8 +221,12 @@ def test_solve_parity(name, mk, N, q):
 
 def test_solve_user_field_matches_builtin():
     """A plain torch vector field (linearized with torch.func on the GPU)
-    gives the built-in field's result."""
-    p = pivp.logistic(r=3.0)
+    gives the built-in field's result: the same iteration count, means within
+    1e-10 or 10x the change of the oracle's result when its field is
+    perturbed by one unit in the last place (the two linearizations differ
+    by rounding, and this IEKS fixed point -- a solution decaying to 1e-7 --
+    amplifies a relative 2^-52 in f to ~1.5e-10 in the means)."""
+    p, o = pivp.logistic(r=3.0), oivp.logistic(r=3.0)
     ts = np.linspace(0.0, 10.0, 100)
 
     def f(t, y):
@@ -210,8 +234,12 @@ def test_solve_user_field_matches_builtin():
 
     a, ia = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=3, init="constant")
     b, ib = psolver.solve(f=f, y0=p.y0, ts=ts, order=3, init="constant")
-    assert int(ia["iterations"]) == int(ib["iterations"])
-    assert rel(N_(b.mean), N_(a.mean)) <= TOL
+    (om, _), _ = osolver.solve(o, ts, 3, init="constant")
+    o_ulp = o._replace(components=lambda y: [3.0 * y[0] * (1 - y[0]) * (1 + 2.0**-52)])
+    (um, _), _ = osolver.solve(o_ulp, ts, 3, init="constant")
+    assert int(ia["iterations"]) == int(ib["iterations"]), (int(ia["iterations"]), int(ib["iterations"]))
+    d, tol = rel(N_(b.mean), N_(a.mean)), max(TOL, 10 * rel(um, om))
+    assert d <= tol, (d, tol)
 
 
 @pytest.mark.parametrize("init", ["prior", "coarse"])

@@ -1,5 +1,5 @@
 """The double reciprocal and reciprocal square root of the kernels' reflector
-scalars (Newton-Raphson from a single-precision seed, csrc/pof_linalg.cuh)
+scalars (one third-order correction of a single-precision seed, csrc/pof_linalg.cuh)
 against IEEE division and square root: within 2 units in the last place
 over the whole exponent range the kernels meet, and the IEEE results for
 the arguments they hand over (zero, subnormal, huge)."""

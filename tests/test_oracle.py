@@ -183,6 +183,29 @@ def test_segmented_schedule_equals_reference_scan(ivpf, N, q, C0, Cg):
     assert abs(sobj - bsobj) <= 1e-11 * abs(sobj)
 
 
+@pytest.mark.parametrize("ivpf,N,q", [(lambda: oivp.logistic(r=3.0), 77, 2),
+                                      (lambda: oivp.vanderpol(stiffness_constant=1.0), 130, 3)])
+@pytest.mark.parametrize("C0,Cs,ks_max", [(1, (2,) * 12, 1024), (2, (2,) * 12, 16), (4, (2,) * 12, 3),
+                                          (1, (2,) * 12, 37)])
+def test_parallel_top_scan_equals_reference_scan(ivpf, N, q, C0, Cs, ks_max):
+    """The plain path's schedule with its top level scanned in parallel
+    (Kogge-Stone prefix scan of the filter, suffix scan of the smoother after
+    pushing the terminal state through the last element) gives the reference
+    scan's marginals, NLL and objectives to rounding."""
+    st, dtm, dom = _converged_problem(ivpf(), N, q, 50)
+    (fm, fL), nll, obj, ssq = ofs.linear_noiseless_filtering(st.x0, dtm, dom)
+    (bm, bL), bnll, bobj, bssq, _ = blocked.filter_blocked(st.x0, dtm, dom, C0=C0, Cs=Cs, ks_max=ks_max)
+    assert np.abs(fm - bm).max() <= 1e-12 * np.abs(fm).max()
+    assert _covd(bL, fL) <= 1e-12
+    assert abs(nll - bnll) <= 1e-11 * abs(nll)
+    assert abs(obj - bobj) <= 1e-11 * abs(obj)
+    (sm, sL), sobj = ofs.smoothing(dtm, (fm, fL))
+    (bsm, bsL), bsobj = blocked.smoother_blocked(dtm, (bm, bL), C0=C0, Cs=Cs, ks_max=ks_max)
+    assert np.abs(sm - bsm).max() <= 1e-12 * np.abs(sm).max()
+    assert _covd(bsL, sL) <= 1e-12
+    assert abs(sobj - bsobj) <= 1e-11 * abs(sobj)
+
+
 def test_scan_orders_agree():
     """JAX's odd/even recursion and a left fold give the same prefix sums."""
     rng = np.random.default_rng(0)
