@@ -32,6 +32,11 @@ char* aligned_ws(void* ws) {
   a = (a + 255) & ~uintptr_t(255);
   return reinterpret_cast<char*>(a);
 }
+
+int wide_lane_limit() {
+  const char* v = getenv("POF_WIDE_LANES");
+  return v ? atoi(v) : 16384;
+}
 }  // namespace pof
 
 namespace {

@@ -115,11 +115,18 @@ inline void launch_team(void (*kern)(KArgs...), int64_t nteams, cudaStream_t st,
   kern<<<grid, B::threads, B::teams * sizeof(WS), st>>>(args...);
 }
 
+// Upper-level launches with few combines (at most this many lanes of wide
+// teams) use the wide teams: they are latency-bound, and a wider team
+// shortens each combine's chain of FP64 instructions (t_tria's column
+// phases, more outputs per t_mm step).  POF_WIDE_LANES overrides.
+int wide_lane_limit();
+
 template <typename T, int D, int DY>
 struct Driver {
   static constexpr int kBlock = 64;
   static constexpr int TSW = TeamSize<D>::v;                     // wide teams
   static constexpr int TSN = TSW / 2 >= 4 ? TSW / 2 : 4;          // narrow teams
+  static constexpr int TSX = TSW < 32 ? 2 * TSW : 32;             // widest teams (latency-bound levels)
   static constexpr bool kTeamL0 = D >= 6;  // pof_plan.h l0_lanes
   using FWS = FiltTeamWs<T, D>;
   using SWS = SmoTeamWs<T, D>;
@@ -179,10 +186,16 @@ struct Driver {
         k_filt_l0_reduce<T, D, DY><<<grid_for(n1, kBlock), kBlock, 0, st>>>(n, p.C0, sm, x0m, x0L,
                                                                              b.template at<T>(p.felem[1]), n1);
     }
+    const int64_t wide = wide_lane_limit() / TSX;  // teams up to which the widest teams run
     for (int l = 1; l < p.nlev; ++l) {
       ProfScope ps(PK_FILT_REDUCE, st);
-      launch_team<FWS, TU>(k_filt_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
-                           p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
+      if (p.cnt[l + 1] <= wide)
+        launch_team<FWS, TSX>(k_filt_reduce_team<T, D, TSX>, p.cnt[l + 1], st,
+                              (const T*)b.template at<T>(p.felem[l]), p.cnt[l], p.Cg,
+                              b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
+      else
+        launch_team<FWS, TU>(k_filt_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
+                             p.cnt[l], p.Cg, b.template at<T>(p.felem[l + 1]), p.cnt[l + 1]);
     }
     if (p.ks) {
       // parallel scan of the top level, ping-ponging between its element
@@ -197,14 +210,20 @@ struct Driver {
       }
     } else {
       ProfScope ps(PK_FILT_TOP, st);
-      launch_team<FWS, TU>(k_filt_top_team<T, D, TU>, 1, st, (const T*)b.template at<T>(p.felem[p.nlev]),
-                           p.cnt[p.nlev], x0m, x0L, b.template at<T>(p.fstate[p.nlev]));
+      launch_team<FWS, TSX>(k_filt_top_team<T, D, TSX>, 1, st, (const T*)b.template at<T>(p.felem[p.nlev]),
+                            p.cnt[p.nlev], x0m, x0L, b.template at<T>(p.fstate[p.nlev]));
     }
     for (int l = p.nlev - 1; l >= 1; --l) {
       ProfScope ps(PK_FILT_DOWN, st);
-      launch_team<FWS, TU>(k_filt_down_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
-                           p.cnt[l], p.Cg, (const T*)b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
-                           b.template at<T>(p.fstate[l]));
+      if (p.cnt[l + 1] <= wide)
+        launch_team<FWS, TSX>(k_filt_down_team<T, D, TSX>, p.cnt[l + 1], st,
+                              (const T*)b.template at<T>(p.felem[l]), p.cnt[l], p.Cg,
+                              (const T*)b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
+                              b.template at<T>(p.fstate[l]));
+      else
+        launch_team<FWS, TU>(k_filt_down_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.felem[l]),
+                             p.cnt[l], p.Cg, (const T*)b.template at<T>(p.fstate[l + 1]), p.cnt[l + 1],
+                             b.template at<T>(p.fstate[l]));
     }
     {
       ProfScope ps(PK_FILT_L0_DOWN, st);
@@ -247,10 +266,16 @@ struct Driver {
         k_smo_reduce<T, D><<<grid_for(n1, kBlock), kBlock, 0, st>>>(b.template at<T>(p.selem), n, p.C0,
                                                                     b.template at<T>(p.gelem[1]), n1);
     }
+    const int64_t wide = wide_lane_limit() / TSX;
     for (int l = 1; l < p.nlev; ++l) {
       ProfScope ps(PK_SMO_REDUCE, st);
-      launch_team<SWS, TU>(k_smo_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
-                           p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
+      if (p.cnt[l + 1] <= wide)
+        launch_team<SWS, TSX>(k_smo_reduce_team<T, D, TSX>, p.cnt[l + 1], st,
+                              (const T*)b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg,
+                              b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
+      else
+        launch_team<SWS, TU>(k_smo_reduce_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
+                             p.cnt[l], p.Cg, b.template at<T>(p.gelem[l + 1]), p.cnt[l + 1]);
     }
     if (p.ks) {
       const int64_t K = p.cnt[p.nlev];
@@ -269,15 +294,21 @@ struct Driver {
       }
     } else {
       ProfScope ps(PK_SMO_TOP, st);
-      launch_team<SWS, TU>(k_smo_top_team<T, D, TU>, 1, st, (const T*)b.template at<T>(p.gelem[p.nlev]),
-                           p.cnt[p.nlev], (const T*)(means + n * D), (const T*)(chols + n * D * D),
-                           b.template at<T>(p.gend[p.nlev]));
+      launch_team<SWS, TSX>(k_smo_top_team<T, D, TSX>, 1, st, (const T*)b.template at<T>(p.gelem[p.nlev]),
+                            p.cnt[p.nlev], (const T*)(means + n * D), (const T*)(chols + n * D * D),
+                            b.template at<T>(p.gend[p.nlev]));
     }
     for (int l = p.nlev - 1; l >= 1; --l) {
       ProfScope ps(PK_SMO_DOWN, st);
-      launch_team<SWS, TU>(k_smo_down_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
-                           p.cnt[l], p.Cg, (const T*)b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
-                           b.template at<T>(p.gend[l]));
+      if (p.cnt[l + 1] <= wide)
+        launch_team<SWS, TSX>(k_smo_down_team<T, D, TSX>, p.cnt[l + 1], st,
+                              (const T*)b.template at<T>(p.gelem[l]), p.cnt[l], p.Cg,
+                              (const T*)b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
+                              b.template at<T>(p.gend[l]));
+      else
+        launch_team<SWS, TU>(k_smo_down_team<T, D, TU>, p.cnt[l + 1], st, (const T*)b.template at<T>(p.gelem[l]),
+                             p.cnt[l], p.Cg, (const T*)b.template at<T>(p.gend[l + 1]), p.cnt[l + 1],
+                             b.template at<T>(p.gend[l]));
     }
     {
       ProfScope ps(PK_SMO_L0_DOWN, st);

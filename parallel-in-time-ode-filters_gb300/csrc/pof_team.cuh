@@ -88,8 +88,23 @@ __device__ __forceinline__ void t_mv(const Team<TS>& tm, const T* A, const T* x,
 // noiseless update): they stay zero, and the reflectors from ncut - 1 on
 // have an empty tail (no reflection: LAPACK's tau = 0, beta = alpha), so
 // they are skipped.
+//
+// A team with at least twice as many lanes as a reflector has rows to update
+// (M - 1 + MB) gives each row G = TS / RS lanes (RS: row slots, the next
+// power of two): lane phase p takes the columns j + 1 + p, j + 1 + p + G, ...,
+// the G partial dot products are summed by shuffles, and each lane updates
+// its own columns -- G times fewer FP64 instructions per reflector on the
+// latency-bound combines of the upper levels.
+template <int R, int TS>
+struct RowSlots {
+  static constexpr int p2 = R <= 1 ? 1 : (R <= 2 ? 2 : (R <= 4 ? 4 : (R <= 8 ? 8 : (R <= 16 ? 16 : 32))));
+  static constexpr int v = p2 < TS ? p2 : TS;
+};
+
 template <typename T, int TS, int M, int MB, int NC, int LD, int LDY>
 __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y, int wlow = 0, int ncut = NC) {
+  constexpr int RS = RowSlots<M - 1 + MB, TS>::v;
+  constexpr int G = TS / RS;
   const int src = (threadIdx.x & 31) / TS * TS;  // lane 0 of this team within the warp
   const int mlim = (ncut < NC && ncut - 1 < M) ? ncut - 1 : M;
 #pragma unroll 1
@@ -112,14 +127,34 @@ __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y, int wlow 
     for (int k = j + 1 + tm.r; k < kend; k += TS) xj[k] *= scal;
     if (tm.r == 0) xj[j] = beta;
     tm.sync();
-    // rows below j (X rows j+1..M-1, then Y rows 0..MB-1): one row per lane
-    for (int rr = tm.r; rr < (M - j - 1) + MB; rr += TS) {
-      T* xi = (rr < M - j - 1) ? X + (j + 1 + rr) * LD : Y + (rr - (M - j - 1)) * LDY;
-      T w = xi[j];
-      for (int k = j + 1; k < kend; ++k) w = fma(xi[k], xj[k], w);
-      w *= tau;
-      xi[j] -= w;
-      for (int k = j + 1; k < kend; ++k) xi[k] = fma(-w, xj[k], xi[k]);
+    // rows below j (X rows j+1..M-1, then Y rows 0..MB-1)
+    if constexpr (G == 1) {  // one row per lane
+      for (int rr = tm.r; rr < (M - j - 1) + MB; rr += TS) {
+        T* xi = (rr < M - j - 1) ? X + (j + 1 + rr) * LD : Y + (rr - (M - j - 1)) * LDY;
+        T w = xi[j];
+        for (int k = j + 1; k < kend; ++k) w = fma(xi[k], xj[k], w);
+        w *= tau;
+        xi[j] -= w;
+        for (int k = j + 1; k < kend; ++k) xi[k] = fma(-w, xj[k], xi[k]);
+      }
+    } else {  // G lanes per row, column phases; the shuffles need every lane
+      const int slot = tm.r % RS, ph = tm.r / RS;
+      const int nrows = (M - j - 1) + MB;
+      for (int base = 0; base < nrows; base += RS) {
+        const int rr = base + slot;
+        const bool act = rr < nrows;
+        T* xi = act ? ((rr < M - j - 1) ? X + (j + 1 + rr) * LD : Y + (rr - (M - j - 1)) * LDY) : X;
+        T part = (act && ph == 0) ? xi[j] : T(0);
+        if (act)
+          for (int k = j + 1 + ph; k < kend; k += G) part = fma(xi[k], xj[k], part);
+#pragma unroll
+        for (int o = RS; o < TS; o <<= 1) part += __shfl_xor_sync(tm.mask, part, o, TS);
+        if (act) {
+          const T w = part * tau;
+          if (ph == 0) xi[j] -= w;
+          for (int k = j + 1 + ph; k < kend; k += G) xi[k] = fma(-w, xj[k], xi[k]);
+        }
+      }
     }
   }
   tm.sync();
