@@ -193,7 +193,7 @@ def run_reference(args, workload):
 # algorithm.
 EXPECTED_ITERATIONS = {
     "fhn_q3_N16384": 141,
-    "fhn_q3_N65536": 166,
+    "fhn_q3_N65536": 155,
     "logistic_q3_N65536": 38,
     "logistic_q3_N1048576": 40,
     "fhn_q3_N1000": 657,  # the oracle's own count (tree order) on this workload
@@ -482,24 +482,38 @@ def run_gpu(args, workload):
 # ---------------------------------------------------------------------------
 
 BATCH_WORKLOADS = {
-    # name: (instances, seed, q, maxiters).  About one instance in six cycles
-    # without meeting the reference's criterion (mostly N in [512, 2048]) and
-    # runs to maxiters + 1: the capped forms bound a solve's length.
-    "fhn_batch4096": (4096, 0, 3, MAXITERS),
-    "fhn_batch4096_it100": (4096, 0, 3, 100),
-    "fhn_batch512_it300": (512, 0, 3, 300),
+    # name: (family, instances, seed, q, maxiters).  FHN: about one instance
+    # in six cycles without meeting the reference's criterion (mostly N in
+    # [512, 2048]) and runs to maxiters + 1, so the capped forms bound a
+    # solve's length, and its IEKS has several fixed points per instance.
+    # Van der Pol mu ~ 1: every instance converges, to one fixed point.
+    "fhn_batch4096": ("fhn", 4096, 0, 3, MAXITERS),
+    "fhn_batch4096_it100": ("fhn", 4096, 0, 3, 100),
+    "fhn_batch512_it300": ("fhn", 512, 0, 3, 300),
+    "vdp_batch512": ("vdp", 512, 0, 3, MAXITERS),
+    "vdp_batch4096": ("vdp", 4096, 0, 3, MAXITERS),
+}
+
+BATCH_FAMILIES = {
+    # family: (field, nominal params, y0 mean, t1, config description)
+    "fhn": ("fhn_classic", (0.2, 0.2, 3.0), (-1.0, 1.0), 100.0,
+            {"ivp": "fhn_classic", "params": "a, b, c uniform within +-20% of (0.2, 0.2, 3)",
+             "y0": "N((-1, 1), 0.1^2 I)", "t1": 100.0}),
+    "vdp": ("vanderpol", (1.0,), (2.0, 0.0), 6.3,
+            {"ivp": "vanderpol", "params": "mu uniform within +-20% of 1", "y0": "N((2, 0), 0.1^2 I)", "t1": 6.3}),
 }
 
 
-def fhn_batch_problems(B, seed):
-    """B FitzHugh-Nagumo IVPs: (a, b, c) each uniform within +-20 % of
-    (0.2, 0.2, 3), y0 ~ N((-1, 1), 0.1^2 I), t in [0, 100], N log-uniform
-    in [256, 8192] (seeded)."""
+def batch_problems(family, B, seed):
+    """B IVPs of a family: each parameter uniform within +-20 % of its nominal
+    value, y0 ~ N(y0 mean, 0.1^2 I), t in [0, t1], N log-uniform in
+    [256, 8192] (seeded)."""
+    field, p0, y0m, t1, _ = BATCH_FAMILIES[family]
     rng = np.random.default_rng(seed)
-    abc = np.array([0.2, 0.2, 3.0]) * rng.uniform(0.8, 1.2, size=(B, 3))
-    y0 = np.array([-1.0, 1.0]) + 0.1 * rng.standard_normal((B, 2))
+    prm = np.array(p0) * rng.uniform(0.8, 1.2, size=(B, len(p0)))
+    y0 = np.array(y0m) + 0.1 * rng.standard_normal((B, len(y0m)))
     N = np.floor(np.exp(rng.uniform(np.log(256), np.log(8192), size=B))).astype(int)
-    return [("fhn_classic", tuple(abc[b]), y0[b], np.linspace(0.0, 100.0, N[b])) for b in range(B)]
+    return [(field, tuple(prm[b]), y0[b], np.linspace(0.0, t1, N[b])) for b in range(B)]
 
 
 def run_gpu_batch(args, workload):
@@ -515,8 +529,8 @@ def run_gpu_batch(args, workload):
 
     _build.build(verbose=False)
     lib = _lib.lib()
-    B, seed, q, maxiters = BATCH_WORKLOADS[workload]
-    problems = fhn_batch_problems(B, seed + rank)
+    family, B, seed, q, maxiters = BATCH_WORKLOADS[workload]
+    problems = batch_problems(family, B, seed + rank)
     dev = torch.device("cuda", local)
     prep = pbatch.prepare_batch(problems, q, device=dev)
     n_steps = prep["n_steps"]
@@ -678,9 +692,8 @@ def run_gpu_batch(args, workload):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": workload, "instances": B, "seed": seed, "ivp": "fhn_classic",
-                   "params": "a, b, c uniform within +-20% of (0.2, 0.2, 3)", "y0": "N((-1, 1), 0.1^2 I)",
-                   "t1": 100.0, "N": "log-uniform in [256, 8192]", "q": q, "D": D, "init": "constant",
+        "config": {"workload": workload, "instances": B, "seed": seed, **BATCH_FAMILIES[family][4],
+                   "N": "log-uniform in [256, 8192]", "q": q, "D": D, "init": "constant",
                    "maxiters": maxiters, "total_steps": total_steps, "step_iterations": step_iters,
                    "iterations_percentiles": {str(p): float(np.percentile(its, p)) for p in (0, 50, 90, 99, 100)},
                    "l2": "inputs (%.2f GB of iterates) exceed L2" % (G * D * 8 / 1e9)},
@@ -728,7 +741,10 @@ def cpu_sample_batch(problems, q, its, budget_s=20.0):
     from oracle import ivp as oivp, solver as osolver
 
     nm, p, y0, ts = problems[0]
-    ivp = oivp.fhn_classic(tmax=float(ts[-1]), y0=list(y0), a=p[0], b=p[1], c=p[2])
+    if nm == "fhn_classic":
+        ivp = oivp.fhn_classic(tmax=float(ts[-1]), y0=list(y0), a=p[0], b=p[1], c=p[2])
+    else:
+        ivp = oivp.vanderpol(tmax=float(ts[-1]), y0=list(y0), stiffness_constant=p[0])
     M = 256
     while True:
         st = osolver.set_up_solver(ivp, ts[: M + 1], q)
