@@ -39,8 +39,9 @@ struct BView {
   Team<TS> tm;
 
 // Level-0 batch kernels: the block shares one copy of F, QL, QL^{-1} (the
-// preconditioned transition model is the same for every step and problem).
-#define POF_BL0_PROLOGUE(WS)                                                             \
+// preconditioned transition model is the same for every step and problem);
+// Q: block size of F's block-upper-triangular pattern to test for (0: none).
+#define POF_BL0_PROLOGUE(WS, Q)                                                          \
   constexpr int HB_ = FQHeader<T, D, false>::bytes;                                      \
   using B_ = TeamBlockH<WS, TS, HB_>;                                                    \
   extern __shared__ __align__(16) unsigned char smem_raw_[];                             \
@@ -49,7 +50,7 @@ struct BView {
   const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;                    \
   Team<TS> tm;                                                                           \
   FQ<T, D>& fq = *reinterpret_cast<FQ<T, D>*>(smem_raw_);                               \
-  load_fq_block<T, TS, D>(tm, fq, F, QL);
+  load_fq_block<T, TS, D>(tm, fq, F, QL, Q);
 
 // EK1 linearization (pof/step.py:12-22, observations.py:35-40) at the
 // previous iterate, one thread per step of an active chunk: the residual
@@ -99,7 +100,7 @@ template <typename T, int D, int DY, int TS>
 __global__ void kb_filt_l0_reduce(BView v, const T* __restrict__ F, const T* __restrict__ QL,
                                   const T* __restrict__ H, const T* __restrict__ c, T* __restrict__ out) {
   using WS = L0FoldWs<T, D, DY, false>;
-  POF_BL0_PROLOGUE(WS)
+  POF_BL0_PROLOGUE(WS, D / DY)
   if (t >= v.n1) return;
   if (v.frozen[v.cp[t]]) return;
   StepFoldWs<T, D, DY>& w = ws_.s;
@@ -115,7 +116,7 @@ __global__ void kb_filt_l0_reduce(BView v, const T* __restrict__ F, const T* __r
   for (int64_t s = s0; s < s1; ++s) {
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     tm.sync();
-    t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL, fq.wq, true);
+    t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL, StepStruct{fq.wq, fq.wf, true});
   }
   tm.sync();
   t_store_filt<T, TS, D>(tm, out, v.n1, t, w.A, w.b, w.L, w.eta, w.Z);
@@ -193,7 +194,7 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
                                 T* __restrict__ means, T* __restrict__ chols, T* __restrict__ selems,
                                 double* __restrict__ partials) {
   using WS = L0KFWs<T, D, DY, false>;
-  POF_BL0_PROLOGUE(WS)
+  POF_BL0_PROLOGUE(WS, D / DY)
   if (t >= v.n1) return;
   const int b = v.cp[t];
   if (v.frozen[b]) return;
@@ -218,7 +219,7 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
     tm.sync();
-    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL, fq.wq, true);
+    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL, StepStruct{fq.wq, fq.wf, true});
     ssq += (double)w.sc[0];
     nll += (double)w.sc[1];
     fobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, ws_.mold, w.m, ws_.r);
@@ -340,7 +341,7 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
                                const T* __restrict__ means_old, double c_mrtol, double c_matol,
                                double* __restrict__ partials) {
   using WS = SmoL0Ws<T, D, false>;
-  POF_BL0_PROLOGUE(WS)
+  POF_BL0_PROLOGUE(WS, 0)
   if (t >= v.n1) return;
   const int b = v.cp[t];
   if (v.frozen[b]) return;

@@ -8,6 +8,11 @@
 // few lanes are active, so a combine spread over TS lanes finishes up to TS
 // times sooner than one run by a single lane.
 //
+// Independent operations of the same shape inside a combine (the two
+// triangularizations U and Z, the two triangular solves M and Mu of the
+// filter operator) run side by side on the two halves of the team: one
+// instruction stream, different operands, half the FP64 instructions.
+//
 // Layout: row-major with an odd leading dimension (LD = cols + 1 for even
 // cols) so the lanes of a team reading one column hit distinct banks.
 #pragma once
@@ -113,10 +118,15 @@ __device__ __forceinline__ void t_tria(const Team<TS>& tm, T* X, T* Y, int wlow 
     int kend = (wlow > 0 && wlow + j + 1 < NC) ? wlow + j + 1 : NC;
     if (ncut < kend) kend = ncut;
     tm.sync();
-    // ||x[j, j+1:]||^2: column partials, reduced across the team
+    // ||x[j, j+1:]||^2: column partials, reduced onto lane 0 (the only one
+    // that uses it) over the lanes that hold partials -- the same additions as
+    // the full butterfly, without the ones of zeros
     T part = T(0);
     for (int k = j + 1 + tm.r; k < kend; k += TS) part = fma(xj[k], xj[k], part);
-    const T xn2 = tm.sum(part);
+    int span = 1;
+    while (span < kend - j - 1 && span < TS) span <<= 1;
+    for (int o = span >> 1; o > 0; o >>= 1) part += __shfl_xor_sync(tm.mask, part, o, TS);
+    const T xn2 = part;
     // the reflector's scalars on one lane (a square root and two divisions
     // are long FP64 sequences), then broadcast
     T tau = T(0), scal = T(0), beta = T(0);
@@ -287,8 +297,10 @@ __device__ __forceinline__ void t_filt_combine(const Team<TS>& tm, FiltTeamWs<T,
   t_mm<T, TS, D, D, D, L1, L1, L1, true, true>(tm, w.U1, w.A2, w.M);
   t_copy<T, TS, D, D, L1, L1, true>(tm, w.U1, w.Mu);
   tm.sync();
-  t_trsm_l<T, TS, D, D, L2, L1>(tm, w.Xt, w.M);
-  t_trsm_l<T, TS, D, D, L2, L1>(tm, w.Xt, w.Mu);
+  {  // M and Mu side by side on the two halves of the team
+    const Team<TS / 2> h;
+    t_trsm_l<T, TS / 2, D, D, L2, L1>(h, w.Xt, tm.r >= TS / 2 ? w.Mu : w.M);
+  }
   tm.sync();
   // W = M^T Xi21^T  ; A_new = (A2 - W) A1  (into UX scratch, then copied)
   t_mm<T, TS, D, D, D, L1, L2, L1, true, true>(tm, w.M, w.Xb, w.W);
@@ -343,8 +355,12 @@ __device__ __forceinline__ void t_filt_combine(const Team<TS>& tm, FiltTeamWs<T,
   tm.sync();
   t_copy<T, TS, D, D, L1, L2, true>(tm, w.M, w.UX);
   t_copy<T, TS, D, D, L1, L2>(tm, w.U2, w.UX + D);
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.UX, w.UX, D);
-  t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.Xt, w.Xt, D);
+  {  // U and Z side by side on the two halves of the team
+    const Team<TS / 2> h;
+    T* X = tm.r >= TS / 2 ? w.Xt : w.UX;
+    t_tria<T, TS / 2, D, 0, D2, L2, L2>(h, X, X, D);
+  }
+  tm.sync();
   t_copy<T, TS, D, D, L2, L1>(tm, w.UX, w.U1);
   t_copy<T, TS, D, D, L2, L1>(tm, w.Xt, w.Z1);
   tm.sync();
@@ -364,8 +380,10 @@ __device__ __forceinline__ void t_filt_apply(const Team<TS>& tm, FiltTeamWs<T, D
   t_mm<T, TS, D, D, D, L1, L1, L1, true, true>(tm, w.U1, w.A2, w.M);
   t_copy<T, TS, D, D, L1, L1, true>(tm, w.U1, w.Mu);
   tm.sync();
-  t_trsm_l<T, TS, D, D, L2, L1>(tm, w.Xt, w.M);
-  t_trsm_l<T, TS, D, D, L2, L1>(tm, w.Xt, w.Mu);
+  {  // M and Mu side by side on the two halves of the team
+    const Team<TS / 2> h;
+    t_trsm_l<T, TS / 2, D, D, L2, L1>(h, w.Xt, tm.r >= TS / 2 ? w.Mu : w.M);
+  }
   tm.sync();
   t_mv<T, TS, D, D, L1, true>(tm, w.U1, w.e2, w.v1);
   tm.sync();
@@ -547,18 +565,55 @@ __device__ __forceinline__ void t_update(const Team<TS>& tm, WS& w, bool rzero) 
   }
 }
 
+// Zero structure of a step's transition model, found when the model is
+// loaded (it is the caller's data: a TransitionModel need not have any).
+//   wq: D when QL is lower-triangular (t_tria's wlow for [F L, QL]), else 0;
+//   wf: Q when F is block-diagonal with upper-triangular Q x Q blocks (the
+//       IWP prior, I_d (x) A_1 with A_1 upper-triangular), else 0;
+//   rzero: the observation noise R is zero (noiseless EK1 model).
+struct StepStruct {
+  int wq, wf;
+  bool rzero;
+};
+
+// C(D x N) = F B with F's zeros skipped when wf > 0: row i of F has its
+// nonzeros in columns i .. (i / wf + 1) wf - 1.  The skipped terms are exact
+// zeros, so the result is the dense product's.
+template <typename T, int TS, int D, int N, int LDA, int LDB, int LDC>
+__device__ __forceinline__ void t_mm_f(const Team<TS>& tm, const T* F, const T* B, T* C, int wf) {
+  for (int idx = tm.r; idx < D * N; idx += TS) {
+    const int i = idx / N, j = idx % N;
+    const int k0 = wf ? i : 0, k1 = wf ? (i / wf + 1) * wf : D;
+    T s = T(0);
+    for (int k = k0; k < k1; ++k) s = fma(F[i * LDA + k], B[k * LDB + j], s);
+    C[i * LDC + j] = s;
+  }
+}
+
+// y(D) = F x, F's zeros skipped when wf > 0 (as t_mm_f).
+template <typename T, int TS, int D, int LDA>
+__device__ __forceinline__ void t_mv_f(const Team<TS>& tm, const T* F, const T* x, T* y, int wf) {
+  for (int i = tm.r; i < D; i += TS) {
+    const int k0 = wf ? i : 0, k1 = wf ? (i / wf + 1) * wf : D;
+    T s = T(0);
+    for (int k = k0; k < k1; ++k) s = fma(F[i * LDA + k], x[k], s);
+    y[i] = s;
+  }
+}
+
 // One square-root KF step from the filtered state (m, L) at grid s, fused with
 // the smoother element (g, E, Dm = Y[:, D:]) of grid s when SMOOTH.  F and
-// QL (D x D, leading dimension Ld<D>) are the step's transition model; wq = D
-// when QL is lower-triangular (t_tria's wlow), else 0; rzero as in t_update.
+// QL (D x D, leading dimension Ld<D>) are the step's transition model, ss
+// its zero structure.
 template <typename T, int TS, int D, int DY, bool SMOOTH, typename WS>
-__device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F, const T* QL, int wq,
-                                          bool rzero) {
+__device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F, const T* QL, StepStruct ss) {
   using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, D2 = W::D2;
-  t_mm<T, TS, D, D, D, L1, L1, L2>(tm, F, w.L, w.X);
+  const int wq = ss.wq;
+  const bool rzero = ss.rzero;
+  t_mm_f<T, TS, D, D, L1, L1, L2>(tm, F, w.L, w.X, ss.wf);
   t_copy<T, TS, D, D, L1, L2>(tm, QL, w.X + D);
-  t_mv<T, TS, D, D, L1>(tm, F, w.m, w.mp);
+  t_mv_f<T, TS, D, L1>(tm, F, w.m, w.mp, ss.wf);
   if constexpr (SMOOTH) {
     t_copy<T, TS, D, D, L1, L2>(tm, w.L, w.Y);
     t_fill<T, TS, D, D, L2>(tm, w.Y + D, T(0), T(0));
@@ -584,13 +639,15 @@ __device__ __forceinline__ void t_kf_step(const Team<TS>& tm, WS& w, const T* F,
 // One step of the conditional fold (cond_fold_step of pof_ops.cuh).
 template <typename T, int TS, int D, int DY>
 __device__ __forceinline__ void t_cond_fold_step(const Team<TS>& tm, StepFoldWs<T, D, DY>& w, const T* F,
-                                                 const T* QL, int wq, bool rzero) {
+                                                 const T* QL, StepStruct ss) {
   using W = StepDims<T, D, DY>;
   constexpr int L1 = W::LD1, L2 = W::LD2, LP = W::LDP, LZ = W::LDZ, D2 = W::D2;
-  t_mm<T, TS, D, D, D, L1, L1, L2>(tm, F, w.L, w.X);
+  const int wq = ss.wq;
+  const bool rzero = ss.rzero;
+  t_mm_f<T, TS, D, D, L1, L1, L2>(tm, F, w.L, w.X, ss.wf);
   t_copy<T, TS, D, D, L1, L2>(tm, QL, w.X + D);
-  t_mm<T, TS, D, D, D, L1, L1, L1>(tm, F, w.A, w.FA);
-  t_mv<T, TS, D, D, L1>(tm, F, w.b, w.Fb);
+  t_mm_f<T, TS, D, D, L1, L1, L1>(tm, F, w.A, w.FA, ss.wf);
+  t_mv_f<T, TS, D, L1>(tm, F, w.b, w.Fb, ss.wf);
   tm.sync();
   t_tria<T, TS, D, 0, D2, L2, L2>(tm, w.X, w.X, wq);
   t_update<T, TS, D, DY, false>(tm, w, rzero);

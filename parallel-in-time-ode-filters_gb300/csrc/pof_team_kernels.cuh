@@ -355,7 +355,15 @@ template <typename T, int D>
 struct FQ {
   T F[D * Ld<D>::v], QL[D * Ld<D>::v], QLi[D * Ld<D>::v];
   int wq;  // D when QL is lower-triangular (t_tria's wlow for [F L, QL]), else 0
+  int wf;  // Q when F is block-diagonal with upper-triangular Q x Q blocks, else 0
 };
+
+// 1 if the (D x D, row-major, leading dimension ld) entry (i, k) of F breaks
+// the block-upper-triangular pattern with blocks of Q (Q = 0: no pattern)
+template <typename T>
+__device__ __forceinline__ bool breaks_fblocks(T v, int i, int k, int Q) {
+  return Q <= 0 || (v != T(0) && (k < i || k >= (i / Q + 1) * Q));
+}
 
 template <typename Base, typename T, int D, bool PS>
 struct WithFQ : Base {};
@@ -403,18 +411,23 @@ struct TeamBlockH {
 };
 
 template <typename T, int TS, int D>
-__device__ __forceinline__ void t_load_FQ(const Team<TS>& tm, FQ<T, D>& q, const StepModel& sm, int64_t s) {
+__device__ __forceinline__ void t_load_FQ(const Team<TS>& tm, FQ<T, D>& q, const StepModel& sm, int64_t s, int Q) {
   constexpr int L1 = Ld<D>::v;
   const T* F = static_cast<const T*>(sm.F) + s * sm.ft_stride;
   const T* QL = static_cast<const T*>(sm.QL) + s * sm.ft_stride;
-  bool upper = false;
+  bool upper = false, fdense = false;
   for (int f = tm.r; f < D * D; f += TS) {
     q.F[(f / D) * L1 + f % D] = F[f];
     q.QL[(f / D) * L1 + f % D] = QL[f];
     upper |= (f % D > f / D) && QL[f] != T(0);
+    fdense |= breaks_fblocks(F[f], f / D, f % D, Q);
   }
   const bool any_upper = __any_sync(tm.mask, upper);
-  if (tm.r == 0) q.wq = any_upper ? 0 : D;
+  const bool any_fdense = __any_sync(tm.mask, fdense);
+  if (tm.r == 0) {
+    q.wq = any_upper ? 0 : D;
+    q.wf = any_fdense ? 0 : Q;
+  }
 }
 
 // QL^{-1} by forward substitution on the identity (objective terms)
@@ -430,16 +443,21 @@ __device__ __forceinline__ void t_inv_lower(const Team<TS>& tm, const T* QL, T* 
 // The block's shared transition model (every thread of the block takes
 // part: call before any team leaves).
 template <typename T, int TS, int D>
-__device__ __forceinline__ void load_fq_block(const Team<TS>& tm, FQ<T, D>& q, const T* F, const T* QL) {
+__device__ __forceinline__ void load_fq_block(const Team<TS>& tm, FQ<T, D>& q, const T* F, const T* QL, int Q) {
   constexpr int L1 = Ld<D>::v;
-  int upper = 0;
+  int upper = 0, fdense = 0;
   for (int f = threadIdx.x; f < D * D; f += blockDim.x) {
     q.F[(f / D) * L1 + f % D] = F[f];
     q.QL[(f / D) * L1 + f % D] = QL[f];
     upper |= (f % D > f / D) && QL[f] != T(0);
+    fdense |= breaks_fblocks(F[f], f / D, f % D, Q);
   }
   upper = __syncthreads_or(upper);
-  if (threadIdx.x == 0) q.wq = upper ? 0 : D;
+  fdense = __syncthreads_or(fdense);
+  if (threadIdx.x == 0) {
+    q.wq = upper ? 0 : D;
+    q.wf = fdense ? 0 : Q;
+  }
   if (threadIdx.x < TS) t_inv_lower<T, TS, D>(tm, q.QL, q.QLi);
   __syncthreads();
 }
@@ -492,10 +510,10 @@ __device__ __forceinline__ FQ<T, D>& fq_ref(WS& ws, unsigned char* smem) {
 // Per-step transition model into the team's copy (PS), or nothing.
 template <bool PS, typename T, int TS, int D>
 __device__ __forceinline__ void fq_step(const Team<TS>& tm, FQ<T, D>& q, const StepModel& sm, int64_t s,
-                                        bool objective) {
+                                        bool objective, int Q) {
   if constexpr (PS) {
     tm.sync();
-    t_load_FQ<T, TS, D>(tm, q, sm, s);
+    t_load_FQ<T, TS, D>(tm, q, sm, s, Q);
     tm.sync();
     if (objective) t_inv_lower<T, TS, D>(tm, q.QL, q.QLi);
   }
@@ -506,7 +524,8 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
                                       const T* __restrict__ x0L, T* __restrict__ out, int64_t n1) {
   using WS = L0FoldWs<T, D, DY, PS>;
   POF_L0_PROLOGUE(WS, PS)
-  if constexpr (!PS) load_fq_block<T, TS, D>(tm, fq, static_cast<const T*>(sm.F), static_cast<const T*>(sm.QL));
+  if constexpr (!PS)
+    load_fq_block<T, TS, D>(tm, fq, static_cast<const T*>(sm.F), static_cast<const T*>(sm.QL), D / DY);
   if (t >= n1) return;
   StepFoldWs<T, D, DY>& w = ws_.s;
   constexpr int L1 = Ld<D>::v;
@@ -515,11 +534,11 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
   if (t == 0) {
     t_load_state_plain<T, TS, D>(tm, x0m, x0L, w.m, w.L);
     for (int64_t s = s0; s < s1; ++s) {
-      fq_step<PS, T, TS, D>(tm, fq, sm, s, false);
+      fq_step<PS, T, TS, D>(tm, fq, sm, s, false, D / DY);
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
       tm.sync();
-      t_kf_step<T, TS, D, DY, false>(tm, w, fq.F, fq.QL, fq.wq, sm.R == nullptr);
+      t_kf_step<T, TS, D, DY, false>(tm, w, fq.F, fq.QL, StepStruct{fq.wq, fq.wf, sm.R == nullptr});
     }
     t_fill<T, TS, D, D, L1>(tm, w.A, T(0), T(0));
     t_fill<T, TS, D, D, L1>(tm, w.Z, T(0), T(0));
@@ -535,11 +554,11 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
       w.eta[i] = T(0);
     }
     for (int64_t s = s0; s < s1; ++s) {
-      fq_step<PS, T, TS, D>(tm, fq, sm, s, false);
+      fq_step<PS, T, TS, D>(tm, fq, sm, s, false, D / DY);
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
       tm.sync();
-      t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL, fq.wq, sm.R == nullptr);
+      t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL, StepStruct{fq.wq, fq.wf, sm.R == nullptr});
     }
     tm.sync();
     t_store_filt<T, TS, D>(tm, out, n1, t, w.A, w.b, w.L, w.eta, w.Z);
@@ -552,7 +571,8 @@ __global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __
                                     double* __restrict__ partials) {
   using WS = L0KFWs<T, D, DY, PS>;
   POF_L0_PROLOGUE(WS, PS)
-  if constexpr (!PS) load_fq_block<T, TS, D>(tm, fq, static_cast<const T*>(sm.F), static_cast<const T*>(sm.QL));
+  if constexpr (!PS)
+    load_fq_block<T, TS, D>(tm, fq, static_cast<const T*>(sm.F), static_cast<const T*>(sm.QL), D / DY);
   if (t >= n1) return;
   StepKFWs<T, D, DY>& w = ws_.s;
   using GL = SmoLayout<D>;
@@ -571,12 +591,12 @@ __global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __
   }
   double ssq = 0.0, nll = 0.0, fobj = 0.0;
   for (int64_t s = s0; s < s1; ++s) {
-    fq_step<PS, T, TS, D>(tm, fq, sm, s, true);
+    fq_step<PS, T, TS, D>(tm, fq, sm, s, true, D / DY);
     StepView<T, D, DY> v(sm, s);
     t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
     for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
     tm.sync();
-    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL, fq.wq, sm.R == nullptr);
+    t_kf_step<T, TS, D, DY, true>(tm, w, fq.F, fq.QL, StepStruct{fq.wq, fq.wf, sm.R == nullptr});
     ssq += (double)w.sc[0];
     nll += (double)w.sc[1];
     fobj += (double)t_objective<T, TS, D>(tm, fq.F, fq.QLi, ws_.mold, w.m, ws_.r);
@@ -614,7 +634,7 @@ __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, c
                                    double c_matol, double* __restrict__ partials) {
   using WS = SmoL0Ws<T, D, PS>;
   POF_L0_PROLOGUE(WS, PS)
-  if constexpr (!PS) load_fq_block<T, TS, D>(tm, fq, F, QL);
+  if constexpr (!PS) load_fq_block<T, TS, D>(tm, fq, F, QL, 0);
   if (t >= n1) return;
   SmoTeamWs<T, D>& w = ws_.s;
   constexpr int L1 = Ld<D>::v;
@@ -643,7 +663,7 @@ __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, c
       for (int f = tm.r; f < D * D; f += TS) chols[n * D * D + f] = w.D1[(f / D) * L1 + f % D] * sc;
   }
   for (int64_t k = s1 - 1; k >= s0; --k) {
-    fq_step<PS, T, TS, D>(tm, fq, sm, k, true);
+    fq_step<PS, T, TS, D>(tm, fq, sm, k, true, 0);
     for (int i = tm.r; i < D; i += TS) ws_.mnext[i] = w.g1[i];
     t_load_smo<T, TS, D>(tm, selems, n, k, w.g2, w.E2, w.D2m);
     tm.sync();

@@ -177,6 +177,37 @@ def test_parallel_top_matches_tree(key, ks, monkeypatch):
     assert rel(N_(am), N_(bm)) <= TOL and covrel(N_(aL), N_(bL)) <= TOL
 
 
+@pytest.mark.parametrize("per_step", [False, True])
+def test_unstructured_models(per_step):
+    """A TransitionModel whose F is dense and Q_L not triangular, and a
+    nonzero, non-triangular observation noise: the kernels detect that the
+    zero patterns they exploit for the IWP prior (block-upper-triangular F,
+    lower-triangular Q_L, R = 0) are absent and run the dense forms (D = 8,
+    team kernels; constant and per-step models)."""
+    rng = np.random.default_rng(5)
+    n, D, d = 300, 8, 2
+    F0 = np.eye(D) + 0.05 * rng.standard_normal((D, D))
+    Q0 = 0.5 * np.eye(D) + 0.1 * rng.standard_normal((D, D))
+    if per_step:
+        F = F0 + 0.01 * rng.standard_normal((n, D, D))
+        QL = Q0 + 0.01 * rng.standard_normal((n, D, D))
+    else:
+        F = np.broadcast_to(F0, (n, D, D)).copy()
+        QL = np.broadcast_to(Q0, (n, D, D)).copy()
+    H = rng.standard_normal((n, d, D))
+    c = 0.1 * rng.standard_normal((n, d))
+    R = 0.1 * rng.standard_normal((n, d, d))
+    x0 = (rng.standard_normal(D), 0.3 * np.eye(D) + 0.05 * np.tril(rng.standard_normal((D, D))))
+    (om, oL), onll, oobj, _ = ofs.linear_filtsmooth(x0, (F, QL), (H, c, R))
+    (_, _), sell, sobj, _ = ofs.sequential_linear_filtsmooth(x0, (F, QL), (H, c, R))
+    gx0 = MVNSqrt(T(x0[0]), T(x0[1]))
+    gdtm = TransitionModel(T(F), T(QL)) if per_step else TransitionModel(T(F0), T(Q0))
+    (gm, gL), gnll, gobj, _ = pfs.linear_filtsmooth(gx0, gdtm, AffineModel(T(H), T(c), T(R)))
+    assert rel(N_(gm), om) <= TOL and covrel(N_(gL), oL) <= TOL
+    assert close(gnll, onll, -sell)
+    assert close(gobj, oobj, sobj)
+
+
 def test_deterministic():
     st, dtm, dom = problem("fhn_q3")
     args = gpu_args(st, dtm, dom)
