@@ -1,8 +1,8 @@
 """Mixed precision (float32 IEKS iterations, float64 polish) against the
-float64 path and the float64 oracle.  The benchmark spec asks every form other
-than the plain float64 path to state its maximum relative error against the
-float64 oracle; the bound asserted here is 1e-6 on the means, in practice the
-polish converges to the float64 fixed point."""
+float64 path and the float64 oracle.  Every form other than the plain
+float64 path states its maximum relative error against the float64 oracle;
+the bound asserted here is 1e-6 on the means (in practice the polish
+converges to the float64 fixed point)."""
 
 import numpy as np
 import pytest
