@@ -1,23 +1,44 @@
 """Floating-point operation counts of libpof's kernels (host-side model).
 
-Counts follow the loops of csrc/pof_linalg.cuh and csrc/pof_ops.cuh one to
-one: an FMA is 2 flops; add, multiply, divide, square root and log are 1.
-They are the algorithmic work of each kernel, the numerator of its
-achieved-FLOP/s figure.  ``reference_step_flops`` is the work per step and
-IEKS iteration of the reference's own formulation (per-step elements,
-~2 combines per element in the associative scan, sigma^2/NLL pass).
+Counts follow the loops of the kernels: an FMA is 2 flops; add, multiply,
+divide, square root and log are 1.  They are the algorithmic work of each
+kernel -- the operations it performs, the structural zeros it skips not
+counted (a few products over a triangular factor that the team kernels run
+dense are counted at their triangular size, mm_lowerB, so the figure errs
+low) -- and the numerator of its achieved-FLOP/s figure.  The thread-per-
+chunk level 0 (D < 6, csrc/pof_ops.cuh) runs the dense loops; the team
+kernels (level 0 from D = 6 on, every level >= 1, csrc/pof_team.cuh) skip the
+zeros of the lower-triangular right blocks of the triangularizations, the
+zero columns of the noiseless update and the zero blocks of the IWP
+transition matrix (structured=True).  ``reference_step_flops`` is the work
+per step and IEKS iteration of the reference's own formulation (per-step
+elements, ~2 combines per element in the associative scan, sigma^2/NLL pass).
 """
 
 
-def tria(M, NC, MB=0):
-    """tria<M, NC> (+ MB extra rows for tria_top)."""
+def tria(M, NC, MB=0, wlow=0, ncut=None):
+    """tria<M, NC> (+ MB extra rows for tria_top); wlow > 0: the right block
+    from column wlow is lower-triangular, reflector j stops at column
+    wlow + j; ncut: the columns from ncut on are zero (reflectors from
+    ncut - 1 on are skipped)."""
     f = 0
-    for j in range(M):
-        t = NC - j - 1
+    mlim = M if ncut is None else min(M, ncut - 1)
+    for j in range(mlim):
+        kend = NC if wlow <= 0 else min(NC, wlow + j + 1)
+        if ncut is not None:
+            kend = min(kend, ncut)
+        t = kend - j - 1
         f += 2 * t + 2 + 1 + 3 + t  # |x|^2, nrm (fma + sqrt), beta/tau/scal, scale tail
         rows = (M - j - 1) + MB
         f += rows * (4 * t + 2)
     return f
+
+
+def mm_f(D, N, d):
+    """F B for the IWP transition matrix F = I_d (x) A_1, A_1 upper-triangular
+    (q + 1) x (q + 1): row i of F has (q + 1) - i mod (q + 1) nonzeros."""
+    Q = D // d
+    return 2 * N * d * (Q * (Q + 1) // 2)
 
 
 def mm(M, K, N):
@@ -40,16 +61,18 @@ def trsm(M, NR):
     return NR * M * (M - 1) + M * NR + M
 
 
-def kf_step(D, d, smooth):
-    f = mm_lowerB(D, D)
+def kf_step(D, d, smooth, structured=None):
+    st = D >= 6 if structured is None else structured
+    w = D if st else 0
+    f = mm_f(D, D, d) if st else mm_lowerB(D, D)
     if smooth:
-        f += tria(D, 2 * D, MB=D) + tria(D, D)
+        f += tria(D, 2 * D, MB=D, wlow=w) + tria(D, D)
         f += trsm(D, D) + mv(D, D) + D
     else:
-        f += tria(D, 2 * D)
-    f += mv(D, D)  # predicted mean
+        f += tria(D, 2 * D, wlow=w)
+    f += mm_f(D, 1, d) if st else mv(D, D)  # predicted mean
     f += mm_lowerB(d, D)  # H Lp (Lp lower)
-    f += tria(D + d, D + d)
+    f += tria(D + d, D + d, ncut=D if st else None)
     f += mv(d, D) + d  # r
     f += 2 * trsv(d)
     f += d * (2 + 2 + 1)  # ssq, y^2, log
@@ -58,10 +81,11 @@ def kf_step(D, d, smooth):
     return f
 
 
-def cond_fold_step(D, d):
-    f = mm_lowerB(D, D) + tria(D, 2 * D)
-    f += mm_lowerB(d, D) + tria(D + d, D + d)
-    f += mm(D, D, D) + mv(D, D)  # F A, F b
+def cond_fold_step(D, d, structured=None):
+    st = D >= 6 if structured is None else structured
+    f = (mm_f(D, D, d) + tria(D, 2 * D, wlow=D)) if st else (mm_lowerB(D, D) + tria(D, 2 * D))
+    f += mm_lowerB(d, D) + tria(D + d, D + d, ncut=D if st else None)
+    f += (mm_f(D, D, d) + mm_f(D, 1, d)) if st else (mm(D, D, D) + mv(D, D))  # F A, F b
     f += mm(d, D, D) + mv(d, D) + d  # H FA, H Fb + c
     f += trsm(d, D) + trsv(d)
     f += D * D * 2 * d + D * 2 * d + D * 2 * d  # A, b, eta
@@ -71,7 +95,7 @@ def cond_fold_step(D, d):
 
 def filt_combine(D):
     f = mm(D, D, D)  # U1^T Z2
-    f += tria(D, 2 * D, MB=D) + tria(D, D)
+    f += tria(D, 2 * D, MB=D, wlow=D) + tria(D, D)
     f += mm(D, D, D) + trsm(D, D)  # M
     f += trsm(D, D)  # Mu
     f += mm(D, D, D)  # MX
@@ -79,25 +103,27 @@ def filt_combine(D):
     f += 2 * mv(D, D) + D + mv(D, D) + mv(D, D) + D + mv(D, D) + D  # b
     f += trsm(D, D)  # e
     f += 2 * mv(D, D) + D + mv(D, D) + mv(D, D) + D + mv(D, D) + D  # eta
-    f += tria(D, 2 * D)  # U
-    f += mm(D, D, D) + tria(D, 2 * D)  # Z
+    f += tria(D, 2 * D, wlow=D)  # U
+    f += mm(D, D, D) + tria(D, 2 * D, wlow=D)  # Z
     return f
 
 
 def filt_apply(D):
-    f = mm(D, D, D) + tria(D, 2 * D, MB=D)
+    f = mm(D, D, D) + tria(D, 2 * D, MB=D, wlow=D)
     f += mm(D, D, D) + trsm(D, D) + trsm(D, D)
     f += 2 * mv(D, D) + D + mv(D, D) + mv(D, D) + D + mv(D, D) + D
-    f += tria(D, 2 * D)
+    f += tria(D, 2 * D, wlow=D)
     return f
 
 
-def smooth_combine(D):
-    return mv(D, D) + mm_lowerB(D, D) + tria(D, 2 * D) + mm(D, D, D) + D
+def smooth_combine(D, structured=True):
+    w = D if structured else 0
+    return mv(D, D) + mm_lowerB(D, D) + tria(D, 2 * D, wlow=w) + mm(D, D, D) + D
 
 
-def smooth_apply(D):
-    return mv(D, D) + mm_lowerB(D, D) + tria(D, 2 * D) + D
+def smooth_apply(D, structured=True):
+    w = D if structured else 0
+    return mv(D, D) + mm_lowerB(D, D) + tria(D, 2 * D, wlow=w) + D
 
 
 def objective_term(D):
@@ -116,9 +142,9 @@ def kernel_flops(kind, n, D, d, C0, cnt):
     if kind == "filt_l0_down":
         return n * (kf_step(D, d, True) + objective_term(D))
     if kind == "smo_l0_reduce":
-        return (n - n1) * smooth_combine(D)
+        return (n - n1) * smooth_combine(D, D >= 6)
     if kind == "smo_l0_down":
-        return n * (smooth_apply(D) + objective_term(D) + D * D)
+        return n * (smooth_apply(D, D >= 6) + objective_term(D) + D * D)
     if kind == "filt_reduce":
         return sum(cnt[l] - cnt[l + 1] for l in range(1, levels)) * filt_combine(D)
     if kind == "filt_down":
