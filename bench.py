@@ -58,7 +58,7 @@ MAXITERS = 10_000  # the reference's default (pof/solver.py:12)
 
 # DRAM bytes (read + write) per launch of a workload's dominant kernel from
 # one ncu capture (profiles/k_filt_l0_down_team_fhn_q3_N65536.md)
-NCU_TRAFFIC = {("fhn_q3_N65536", "filt_l0_down"): 66.866944e6 + 107.703040e6}
+NCU_TRAFFIC = {("fhn_q3_N65536", "filt_l0_down"): 66.193664e6 + 108.293888e6}
 
 
 def jprint(obj):
