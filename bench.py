@@ -765,6 +765,67 @@ def cpu_sample_batch(problems, q, its, budget_s=20.0):
 
 
 # ---------------------------------------------------------------------------
+# Scan-length sweep: parallel IEKS solves against the sequential EKS pass on
+# the same GPU, one IVP per launch
+# ---------------------------------------------------------------------------
+
+SWEEP_WORKLOADS = {
+    # name: (cases (field, kwargs, t1, q, largest N), N values, largest N of the sequential pass)
+    "scan_sweep": ([("logistic", {"r": 3.0}, 10.0, q, 2**20) for q in (1, 2, 3, 5)]
+                   + [("fhn_classic", {}, 100.0, 3, 2**16)],
+                   [2**10, 2**12, 2**14, 2**16, 2**18, 2**20], 2**14),
+}
+
+
+def run_sweep(args, workload):
+    """Wall time (device synchronized on both sides) of one full parallel
+    IEKS solve (pof.solver.solve, the reference's criterion) and of one
+    sequential extended Kalman smoother pass (pof.solver.sequential_eks_solve,
+    one GPU thread running the square-root EKF + RTS recursion) per (IVP, q,
+    N).  The sequential pass is one linearization, not an iterated solve."""
+    import torch
+
+    from pof import _build, ivp as pivp, solver as psolver
+
+    _build.build(verbose=False)
+    cases, Ns, seq_max = SWEEP_WORKLOADS[workload]
+    rows = []
+
+    def wall(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, out
+
+    for name, kw, t1, q, nmax in cases:
+        p = getattr(pivp, name)(**kw)
+        for N in Ns:
+            if N > nmax:
+                continue
+            ts = np.linspace(0.0, t1, N)
+            par = lambda: psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant", maxiters=MAXITERS)  # noqa: E731
+            if N <= 2**16:
+                wall(par)
+            tp, (_, info) = wall(par)
+            it = int(info["iterations"])
+            row = {"ivp": name, "q": q, "N": N, "parallel_ieks_ms": tp * 1e3, "iterations": it,
+                   "parallel_ms_per_iteration": tp * 1e3 / max(it, 1)}
+            if N <= seq_max:
+                seq = lambda: psolver.sequential_eks_solve(f=p.f, y0=p.y0, ts=ts, order=q)  # noqa: E731
+                wall(seq)
+                tsq, _ = wall(seq)
+                row["sequential_eks_ms"] = tsq * 1e3
+                row["parallel_iteration_vs_sequential_pass"] = row["parallel_ms_per_iteration"] / (tsq * 1e3)
+            rows.append(row)
+    jprint({"metric": "ms per solve, parallel IEKS vs sequential EKS pass (float64, one IVP per launch)",
+            "value": None, "unit": "ms", "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": workload, "init": "constant", "maxiters": MAXITERS,
+                                            "timing": "wall clock, device synchronized, 1 warm-up for N <= 2^16"},
+            "rows": rows})
+
+
+# ---------------------------------------------------------------------------
 # Served request stream: continuous batching against one-request-at-a-time
 # ---------------------------------------------------------------------------
 
@@ -1064,7 +1125,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(SERVE_WORKLOADS)
-                    + sorted(MIXED_WORKLOADS))
+                    + sorted(MIXED_WORKLOADS) + sorted(SWEEP_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--f32-settle", type=float, default=0.1,
@@ -1081,6 +1142,8 @@ def main():
         run_serve(args, args.workload)
     elif args.workload in MIXED_WORKLOADS:
         run_mixed(args, args.workload)
+    elif args.workload in SWEEP_WORKLOADS:
+        run_sweep(args, args.workload)
     else:
         run_gpu(args, args.workload)
 

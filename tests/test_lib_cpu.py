@@ -61,6 +61,38 @@ def test_shapes_and_workspace_queries(lib):
     assert lib.pof_filtsmooth_workspace_bytes(0, 0, 8, 2) == 0
 
 
+def test_parallel_top_option_changes_the_plan(lib, monkeypatch):
+    """POF_KS (read at each call): 0, the default, keeps the binary tree to two
+    top elements; -1 stops it at the first level of at most 16384 / team lanes
+    elements and adds the parallel scan's ping-pong buffer, which at N = 2^16,
+    D = 8 costs less than the dropped levels' buffers."""
+    dflt = lib.pof_filtsmooth_workspace_bytes(0, 65535, 8, 2)
+    monkeypatch.setenv("POF_KS", "0")
+    assert lib.pof_filtsmooth_workspace_bytes(0, 65535, 8, 2) == dflt
+    monkeypatch.setenv("POF_KS", "-1")
+    ks = lib.pof_filtsmooth_workspace_bytes(0, 65535, 8, 2)
+    assert ks != dflt and ks > 0
+    monkeypatch.setenv("POF_KS", "2")  # not above the two-element top: the tree
+    assert lib.pof_filtsmooth_workspace_bytes(0, 65535, 8, 2) == dflt
+
+
+def test_flop_model_counts_skipped_zeros_out():
+    """The flop model counts the team kernels' operations without the
+    structural zeros they skip: fewer than the dense loops from D = 6 on,
+    equal below (thread-per-chunk level 0 runs the dense loops)."""
+    from pof import _flops
+
+    for D, d in ((8, 2), (6, 2), (10, 2)):
+        assert _flops.kf_step(D, d, True) < _flops.kf_step(D, d, True, structured=False)
+        assert _flops.cond_fold_step(D, d) < _flops.cond_fold_step(D, d, structured=False)
+    assert _flops.kf_step(4, 1, True) == _flops.kf_step(4, 1, True, structured=False)
+    # a lower-triangular right block: reflector j spans columns j+1 .. D+j
+    assert _flops.tria(8, 16, wlow=8) < _flops.tria(8, 16)
+    assert _flops.tria(8, 16, wlow=15) == _flops.tria(8, 16)
+    # zero columns from ncut on: the reflectors from ncut - 1 on vanish
+    assert _flops.tria(10, 10, ncut=8) == _flops.tria(7, 10, MB=3, ncut=8)
+
+
 def test_argument_errors_without_gpu(lib):
     """Invalid arguments are rejected on the host before any CUDA call."""
     null = ctypes.c_void_p(0)
