@@ -770,10 +770,16 @@ def cpu_sample_batch(problems, q, its, budget_s=20.0):
 # ---------------------------------------------------------------------------
 
 SWEEP_WORKLOADS = {
-    # name: (cases (field, kwargs, t1, q, largest N), N values, largest N of the sequential pass)
-    "scan_sweep": ([("logistic", {"r": 3.0}, 10.0, q, 2**20) for q in (1, 2, 3, 5)]
-                   + [("fhn_classic", {}, 100.0, 3, 2**16)],
-                   [2**10, 2**12, 2**14, 2**16, 2**18, 2**20], 2**14),
+    # name: (cases (field, kwargs, t1 or None for the IVP's own span, q, N values), largest N of the
+    # sequential pass, maxiters)
+    "scan_sweep": ([("logistic", {"r": 3.0}, 10.0, q, [2**10, 2**12, 2**14, 2**16, 2**18, 2**20]) for q in (1, 2, 3, 5)]
+                   + [("fhn_classic", {}, 100.0, 3, [2**10, 2**12, 2**14, 2**16])], 2**14, MAXITERS),
+    # the rows of the reference's published V100 benchmark (pof.ivp default problems, constant init,
+    # maxiters 1000) that fit the compiled shapes
+    "v100_table": ([("logistic", {}, None, 3, [2**10, 2**14, 2**19]),
+                    ("fitzhughnagumo", {}, None, 3, [2**10, 2**14, 2**19]),
+                    ("vanderpol", {"stiffness_constant": 1.0}, None, 3, [2**19]),
+                    ("henonheiles", {}, None, 1, [2**19])], 0, 1000),
 }
 
 
@@ -788,7 +794,7 @@ def run_sweep(args, workload):
     from pof import _build, ivp as pivp, solver as psolver
 
     _build.build(verbose=False)
-    cases, Ns, seq_max = SWEEP_WORKLOADS[workload]
+    cases, seq_max, maxiters = SWEEP_WORKLOADS[workload]
     rows = []
 
     def wall(fn):
@@ -798,13 +804,11 @@ def run_sweep(args, workload):
         torch.cuda.synchronize()
         return time.perf_counter() - t0, out
 
-    for name, kw, t1, q, nmax in cases:
+    for name, kw, t1, q, Ns in cases:
         p = getattr(pivp, name)(**kw)
         for N in Ns:
-            if N > nmax:
-                continue
-            ts = np.linspace(0.0, t1, N)
-            par = lambda: psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant", maxiters=MAXITERS)  # noqa: E731
+            ts = np.linspace(p.t0, p.tmax, N) if t1 is None else np.linspace(0.0, t1, N)
+            par = lambda: psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant", maxiters=maxiters)  # noqa: E731
             if N <= 2**16:
                 wall(par)
             tp, (_, info) = wall(par)
@@ -820,7 +824,7 @@ def run_sweep(args, workload):
             rows.append(row)
     jprint({"metric": "ms per solve, parallel IEKS vs sequential EKS pass (float64, one IVP per launch)",
             "value": None, "unit": "ms", "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": workload, "init": "constant", "maxiters": MAXITERS,
+            "data": "synthetic", "config": {"workload": workload, "init": "constant", "maxiters": maxiters,
                                             "timing": "wall clock, device synchronized, 1 warm-up for N <= 2^16"},
             "rows": rows})
 
