@@ -65,6 +65,19 @@ def jprint(obj):
     print(json.dumps(obj), flush=True)
 
 
+def max_over_ranks(x, world, device):
+    """Largest x over the ranks of a replica run (the slowest rank sets the
+    job's time); x itself when there is one rank.  All ranks must call it."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -351,11 +364,7 @@ def run_gpu(args, workload):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
         barrier()
-    ms = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(np.mean(times)), world, dev)
     value = world * n / (ms * 1e-3)
 
     # mixed precision (float32 iterations + float64 polish) on the same
@@ -432,7 +441,7 @@ def run_gpu(args, workload):
             e2e_times.append(el)
         h2d = ts_host.nbytes + y0_host.nbytes
         d2h = m_host.nbytes + c_host.nbytes + 8
-    e2e_s = float(np.mean(e2e_times))
+    e2e_s = max_over_ranks(float(np.mean(e2e_times)), world, dev)
     e2e_value = world * n / e2e_s
 
     if rank != 0:
@@ -577,11 +586,7 @@ def run_gpu_batch(args, workload):
     with ClockSampler(local) as clk:
         times = timed(solve, args.steps)  # inputs (G x D means, ~0.5 GB) exceed L2
         barrier()
-    ms = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(np.mean(times)), world, dev)
     its = info[:, _lib.I_ITERATIONS].cpu().numpy()
     step_iters = int((n_steps * its).sum())
     value = world * total_steps / (ms * 1e-3)
@@ -675,7 +680,7 @@ def run_gpu_batch(args, workload):
             e2e_times.append(el)
     h2d = sum(len(p[3]) * 8 + 16 + 24 for p in problems)
     d2h = ym.nbytes + yc.nbytes
-    e2e_s = float(np.mean(e2e_times))
+    e2e_s = max_over_ranks(float(np.mean(e2e_times)), world, dev)
 
     if rank != 0:
         return
