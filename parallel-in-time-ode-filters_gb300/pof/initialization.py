@@ -107,14 +107,16 @@ def _prior_init(*, x0, dtm):
     return MVNSqrt(torch.cat([x0.mean[None], pm]), torch.cat([x0.chol[None], pL]))
 
 
-def prior_init(*, f, y0, order, ts):
+def prior_init(*, f, y0, order, ts, device=None):
     """pof/initialization.py:83-89: transitions at step sizes ts[1:] (absolute
-    times, as in the reference), not preconditioned, result not scaled by PI."""
-    x0 = taylor_mode_init(f, y0, order)
+    times, as in the reference), not preconditioned, result not scaled by PI.
+    ``device``: where the trajectory is built (default: the current CUDA
+    device)."""
+    x0 = taylor_mode_init(f, y0, order, device=device)
     d = torch.as_tensor(y0).shape[0]
     iwp = IWP(num_derivatives=order, wiener_process_dimension=d)
     ts = torch.as_tensor(ts, dtype=torch.float64)
-    dtm = discretize_transitions(iwp, steps=ts[1:])
+    dtm = discretize_transitions(iwp, steps=ts[1:], device=device)
     return _prior_init(x0=x0, dtm=dtm)
 
 

@@ -1,0 +1,191 @@
+"""The torch host code of `pof` against the oracle, on CPU tensors.
+
+Everything here runs in the drop-in package on the GPU path too: the
+linear-algebra helpers of pof/utils.py, the convergence criterion, the
+sequential one-step predict/update used by the initial trajectories, the
+initial trajectories themselves ("prior" is the default `init` of
+`pof.solver.solve`), and the EK1 / EK0 / regularized linearizations of user
+vector fields (torch.func.jacfwd).  torch runs the same operations on CPU
+and CUDA tensors, so these are checked here on the CPU.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import core as oc, filtsmooth as ofs, ivp as oivp, solver as osolver
+from pof import convergence_criteria as pcc, initialization as pinit, ivp as pivp, observations as pobs
+from pof import transitions as ptr, utils as pu
+from pof.sequential_filtsmooth.filter import _sqrt_predict, _sqrt_update
+from pof.utils import MVNSqrt
+
+CPU = torch.device("cpu")
+
+
+def T(x):
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64)
+
+
+def lower(rng, *shape):
+    return np.tril(rng.standard_normal(shape)) + 3.0 * np.eye(shape[-1])
+
+
+def gram(L):
+    return L @ np.swapaxes(L, -1, -2)
+
+
+@pytest.fixture
+def rng():
+    return np.random.default_rng(20261204)
+
+
+def test_tria_is_lapack_qr(rng):
+    A = rng.standard_normal((7, 6, 13))
+    L = pu.tria(T(A)).numpy()
+    assert np.allclose(np.triu(L, 1), 0.0)
+    assert np.allclose(L, oc.tria(A), rtol=1e-12, atol=1e-12)  # same signs, not just the same L L^T
+    assert np.allclose(gram(L), gram(A), rtol=1e-12, atol=1e-12)
+
+
+def test_whiten_solves_with_the_transpose(rng):
+    """whiten(m, L) = L^-T m (the reference's solve_triangular(L.T, m) with
+    lower=False), not L^-1 m."""
+    L = lower(rng, 5, 4, 4)
+    m = rng.standard_normal((5, 4))
+    w = pu.whiten(T(m), T(L)).numpy()
+    assert np.allclose(w, oc.whiten(m, L), rtol=1e-13, atol=1e-13)
+    assert np.allclose(np.einsum("kji,kj->ki", L, w), m, rtol=1e-12, atol=1e-12)
+    assert not np.allclose(w, np.linalg.solve(L, m[..., None])[..., 0])
+
+
+def test_loglikelihood_objective_and_helpers(rng):
+    L = lower(rng, 6, 3, 3)
+    x = rng.standard_normal((6, 3))
+    assert np.allclose(pu.mvn_loglikelihood(T(x), T(L)).numpy(), oc.mvn_loglikelihood(x, L), rtol=1e-13)
+    F = rng.standard_normal((6, 3, 3))
+    QL = lower(rng, 6, 3, 3)
+    mn, m = rng.standard_normal((6, 3)), rng.standard_normal((6, 3))
+    a = pu.objective_function_value(T(mn), T(m), (T(F), T(QL))).numpy()
+    assert np.allclose(a, oc.objective_function_value(mn, m, F, QL), rtol=1e-13)
+    z = rng.standard_normal((3, 2))
+    assert np.array_equal(pu.append_zeros_along_new_axis(T(z), 4).numpy(), oc.append_zeros_along_new_axis(z, 4))
+    A = rng.standard_normal((2, 3))
+    g = pu.gmul_stack(T(A), MVNSqrt(T(m), T(L)))
+    assert np.allclose(g.mean.numpy(), m @ A.T) and np.allclose(g.chol.numpy(), A @ L)
+
+
+@pytest.mark.parametrize("case", range(12))
+def test_crit_matches_oracle(rng, case):
+    means_old = rng.standard_normal((9, 4))
+    means = means_old + (0.0 if case % 3 == 0 else 10.0 ** -(4 + 3 * (case % 4))) * rng.standard_normal((9, 4))
+    obj_old = float(rng.uniform(1, 1e3))
+    obj = obj_old * (1 + (1e-7 if case % 2 else 1e-3))
+    nll, nll_old = float(rng.standard_normal()), float(rng.standard_normal())
+    if case == 5:
+        nll = float("nan")
+    if case == 7:
+        obj = float("nan")
+    kw = {} if case < 8 else {"rtol": 1e-2, "atol": 1e-2}
+    want = osolver.crit(obj, obj_old, nll, nll_old, means, means_old, **kw)
+    got = pcc.crit(obj, obj_old, nll, nll_old, MVNSqrt(T(means), None), MVNSqrt(T(means_old), None), **kw)
+    assert bool(got) == bool(want)
+
+
+@pytest.mark.parametrize("with_R", [False, True])
+def test_sqrt_predict_and_update_match_oracle(rng, with_R):
+    D, d, B = 6, 2, 5
+    F = rng.standard_normal((B, D, D))
+    QL = lower(rng, B, D, D)
+    m = rng.standard_normal((B, D))
+    L = lower(rng, B, D, D)
+    pm, pL = _sqrt_predict(T(F), T(QL), MVNSqrt(T(m), T(L)))
+    om, oL = ofs.sqrt_predict(F, QL, m, L)
+    assert np.allclose(pm.numpy(), om, rtol=1e-13) and np.allclose(gram(pL.numpy()), gram(oL), rtol=1e-12)
+    for k in range(B):  # the torch helper is one step at a time
+        H = rng.standard_normal((d, D))
+        c = rng.standard_normal(d)
+        R = lower(rng, d, d) if with_R else np.zeros((d, d))
+        (um, uL), ell, ssq = _sqrt_update(T(H), T(R), T(c), MVNSqrt(T(om[k]), T(oL[k])))
+        (vm, vL), vell, vssq = ofs.sqrt_update(H, R, c, om[k], oL[k])
+        assert np.allclose(um.numpy(), vm, rtol=1e-11, atol=1e-12)
+        assert np.allclose(gram(uL.numpy()), gram(vL), rtol=1e-11, atol=1e-12)
+        assert np.isclose(float(ell), vell, rtol=1e-12) and np.isclose(float(ssq), vssq, rtol=1e-11)
+
+
+CASES = [("logistic", {"r": 3.0}, 10.0, 2), ("fhn_classic", {}, 100.0, 3), ("lotkavolterra", {}, 7.0, 4),
+         ("vanderpol", {"stiffness_constant": 1.0}, 6.3, 3)]
+
+
+@pytest.mark.parametrize("name,kw,t1,q", CASES)
+def test_constant_and_prior_init_match_oracle(name, kw, t1, q):
+    """The "constant" trajectory, and the default "prior" one with the
+    reference's quirks: transitions at step sizes ts[1:] (absolute times),
+    not preconditioned, not scaled by PI."""
+    p, o = getattr(pivp, name)(**kw), getattr(oivp, name)(**kw)
+    ts = np.linspace(0.0, t1, 40)
+    c = pinit.constant_init(y0=p.y0, order=q, ts=ts, f=p.f, device=CPU)
+    om, oL = osolver.constant_init(o, q, ts)
+    assert np.allclose(c.mean.numpy(), om, rtol=1e-14) and np.array_equal(c.chol.numpy(), oL)
+    pr = pinit.prior_init(f=p.f, y0=p.y0, order=q, ts=ts, device=CPU)
+    om, oL = osolver.prior_init(o, q, ts)
+    scale = np.abs(om).max(axis=0) + 1e-300
+    assert np.allclose(pr.mean.numpy() / scale, om / scale, rtol=1e-12, atol=1e-12)
+    G, oG = gram(pr.chol.numpy()), gram(oL)
+    assert np.allclose(G, oG, rtol=1e-10, atol=1e-10 * np.abs(oG).max())
+
+
+@pytest.mark.parametrize("name,kw,t1,q", CASES)
+def test_ek1_linearization_of_a_user_field_matches_oracle(rng, name, kw, t1, q):
+    """torch.func.jacfwd EK1 of the residual E1 P x - f(E0 P x) at a batch of
+    states (pof/observations.py:35-40) == the oracle's analytic Jacobians."""
+    p, o = getattr(pivp, name)(**kw), getattr(oivp, name)(**kw)
+    ts = np.linspace(0.0, t1, 33)
+    st = osolver.set_up_solver(o, ts, q)
+    d = st.d
+    iwp = ptr.IWP(wiener_process_dimension=d, num_derivatives=q)
+    P, _ = ptr.nordsieck_preconditioner(iwp, ts[1] - ts[0], device=CPU)
+    E0 = ptr.projection_matrix(iwp, 0, device=CPU) @ P
+    E1 = ptr.projection_matrix(iwp, 1, device=CPU) @ P
+    assert np.allclose(E0.numpy(), st.E0, rtol=1e-15) and np.allclose(E1.numpy(), st.E1, rtol=1e-15)
+
+    def om_fn(x):
+        return E1 @ x - p.f(None, E0 @ x)
+
+    means, _ = osolver.get_initial_trajectory(st, "constant")
+    means = means[1:] * (1 + 0.1 * rng.standard_normal(means[1:].shape))
+    D = means.shape[1]
+    H, b, R = pobs.linearize(om_fn, MVNSqrt(T(means), torch.zeros(len(means), D, D, dtype=torch.float64)))
+    oH, oc_, oR = osolver.linearize(st, means)
+    assert np.allclose(H.numpy(), oH, rtol=1e-12, atol=1e-12 * np.abs(oH).max())
+    assert np.allclose(b.numpy(), oc_, rtol=1e-10, atol=1e-10 * np.abs(oc_).max())
+    assert np.array_equal(R.numpy(), oR)
+
+
+def test_ek0_and_regularized_linearizations(rng):
+    """EK0: H = E1, b = f(m) - E1 m (pof/observations.py:52-61); the
+    Levenberg-Marquardt form stacks the EK1 rows on (I, -m) with noise
+    chol blockdiag(0, I / sqrt(l)) (pof/observations.py:64-83)."""
+    p = pivp.lotkavolterra()
+    q, d = 3, 2
+    D = d * (q + 1)
+    iwp = ptr.IWP(wiener_process_dimension=d, num_derivatives=q)
+    E0 = ptr.projection_matrix(iwp, 0, device=CPU)
+    E1 = ptr.projection_matrix(iwp, 1, device=CPU)
+
+    def om_fn(x):
+        return E1 @ x - p.f(None, E0 @ x)
+
+    m = T(rng.uniform(0.5, 1.5, D))
+    x = MVNSqrt(m, torch.eye(D, dtype=torch.float64))
+    H0, b0, R0 = pobs.linearize_ek0(om_fn, x)
+    assert torch.equal(H0, E1) and torch.allclose(b0, om_fn(m) - E1 @ m) and not R0.any()
+    H, b, R = pobs.linearize(om_fn, x)
+    lam = 4.0
+    Hr, br, Rr = pobs.linearize_regularized(om_fn, x, lam)
+    assert Hr.shape == (d + D, D) and br.shape == (d + D,) and Rr.shape == (d + D, d + D)
+    assert torch.allclose(Hr[:d], H) and torch.equal(Hr[d:], torch.eye(D, dtype=torch.float64))
+    assert torch.allclose(br[:d], om_fn(m)) and torch.equal(br[d:], -m)
+    assert not Rr[:d].any() and not Rr[:, :d].any()
+    assert torch.allclose(Rr[d:, d:], torch.eye(D, dtype=torch.float64) / lam**0.5)
+    # b of the EK1 rows is f(m) - H m there, f(m) in the regularized form (the reference's full_b = [res, -m])
+    assert torch.allclose(b, om_fn(m) - H @ m)
