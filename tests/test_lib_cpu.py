@@ -139,3 +139,56 @@ def test_taylor_mode_matches_oracle(name, ctor, q):
     a = initialization.taylor_derivatives(p.f, p.y0, q).numpy()
     b = taylor.taylor_derivatives(o.components, o.y0, q)
     assert np.allclose(a, b, rtol=1e-13, atol=1e-13)
+
+
+def test_sizes_strides_and_workspace_checked_before_any_cuda_call(lib):
+    """Empty inputs (n_steps = 0), strides that are neither 0 nor one
+    matrix, a workspace below the query's size, a negative maxiters and a
+    field of the wrong dimension are refused on the host with their status,
+    before any pointer is used (the pointers here are placeholders)."""
+    import ctypes as C
+
+    from pof import _lib
+
+    ARG, WORKSPACE, FIELD, DTYPE = -1, -3, -5, -6  # POF_ERR_* of include/pof.h
+    P = 256  # never dereferenced: every call below returns before any CUDA call
+    dp = C.cast(C.c_void_p(P), C.POINTER(C.c_double))
+    n, D, d = 100, 8, 2
+    ws = lib.pof_filtsmooth_workspace_bytes(0, n, D, d)
+
+    def fs(n=n, fts=0, rs=0, wsb=ws, R=P):
+        return lib.pof_linear_filtsmooth(0, n, D, d, P, P, P, P, fts, P, P, R, rs, P, P, dp, P, wsb, None)
+
+    assert fs(n=0) == ARG
+    assert fs(n=-5) == ARG
+    assert fs(fts=D) == ARG
+    assert fs(rs=d) == ARG
+    assert fs(wsb=ws - 1) == WORKSPACE
+    assert lib.pof_linear_noiseless_filtering(0, n, D, d, P, P, P, P, 0, P, P, None, 0, P, P, dp, P, ws - 1,
+                                              None) == WORKSPACE
+    sws = lib.pof_filtsmooth_workspace_bytes(0, n, D, 1)
+    assert lib.pof_smoothing(0, 0, D, P, P, 0, P, P, P, P, dp, P, sws, None) == ARG
+    assert lib.pof_smoothing(0, n, D, P, P, 7, P, P, P, P, dp, P, sws, None) == ARG
+
+    iws = lib.pof_ieks_workspace_bytes(0, n, D, d)
+    fhn = _lib.FIELDS["fhn_classic"]
+
+    def solve(n=n, field=fhn, maxiters=10, wsb=iws, dtype=0):
+        return lib.pof_ieks_solve(dtype, n, D, d, field, P, 0.1, P, P, P, P, P, P, maxiters, 1, dp, P, wsb, None)
+
+    assert solve(n=0) == ARG
+    assert solve(maxiters=-1) == ARG
+    assert solve(wsb=iws - 1) == WORKSPACE
+    assert solve(field=_lib.FIELDS["logistic"]) == FIELD
+    assert solve(field=999) == FIELD
+    assert solve(dtype=3) == DTYPE
+
+    mws = lib.pof_ieks_mixed_workspace_bytes(n, D, d)
+
+    def mixed(rtol=1e-5, settle=1.0, wsb=mws):
+        return lib.pof_ieks_solve_mixed(n, D, d, fhn, P, 0.1, P, P, P, P, P, P, 10, rtol, settle, 10, 1, dp, P, wsb,
+                                        None)
+
+    assert mixed(rtol=0.0) == ARG
+    assert mixed(settle=float("nan")) == ARG
+    assert mixed(wsb=mws - 1) == WORKSPACE
