@@ -235,3 +235,92 @@ def ieks_iterator(ivp, ts, order, init="prior"):
                 break
 
     return gen(), setup
+
+
+# --------------------------------------------------------------------------
+# regularized IEKS iterators, iterators.py:44-133
+# --------------------------------------------------------------------------
+
+
+def qpm_ieks_iterator(ivp, ts, order, init="prior", reg_start=1e20, reg_final=1e-20, steps=40, tau_start=None,
+                      tau_final=None):
+    """``iterators.py:44-106``, quadratic-penalty IEKS: the EK1 model with
+    noise chol ``reg * I / N`` (N = number of steps); each time ``crit``
+    holds at tolerance tau, reg and tau shrink geometrically, reg snaps to 0
+    below reg_final and the loop ends once crit holds at reg = 0 (or on NaN).
+    No calibration (the filter/smoother is called directly).  Yields
+    (states, nll, obj, reg).  The reference's ``init_covs`` lines compute a
+    value nothing reads and are left out."""
+    setup = set_up_solver(ivp, ts, order)
+    states = get_initial_trajectory(setup, method=init)
+    dtm = (setup.F, setup.QL)
+    N = setup.F.shape[0]
+    if tau_start is None:
+        tau_start, tau_final = 1e5, 1e-5
+    reg_fact = (reg_final / reg_start) ** (1 / steps)
+    tau_fact = (tau_final / tau_start) ** (1 / steps)
+
+    def gen():
+        reg, tau = reg_start, tau_start
+        H, c, R = linearize_at_previous_states(setup, states[0])
+        eye = np.broadcast_to(np.eye(R.shape[-1]), R.shape)
+        st, nll, obj, _ = filtsmooth.linear_filtsmooth(setup.x0, dtm, (H, c, reg * eye / N))
+        yield st, nll, obj, reg
+        while True:
+            nll_old, obj_old, st_old = nll, obj, st
+            H, c, _ = linearize_at_previous_states(setup, st[0])
+            st, nll, obj, _ = filtsmooth.linear_filtsmooth(setup.x0, dtm, (H, c, reg * eye / N))
+            yield st, nll, obj, reg
+            if crit(obj, obj_old, nll, nll_old, st[0], st_old[0], rtol=tau, atol=tau):
+                reg *= reg_fact
+                tau *= tau_fact
+                if reg == 0:
+                    break
+                elif reg < reg_final:
+                    reg = 0.0
+                    tau = min(tau_final, 1e-5)
+            if np.isnan(nll) or np.isnan(obj):
+                break
+
+    return gen(), setup
+
+
+def linearize_regularized(setup, m, lam):
+    """``observations.py:64-83`` at a batch of states: the EK1 rows
+    (Jacobian H, offset = the residual itself, as the reference stacks
+    ``res`` and not ``res - H m``) over the rows (I, -m) with noise chol
+    blockdiag(0, I / sqrt(lam))."""
+    d = setup.d
+    D = m.shape[-1]
+    y = filtsmooth.mv(setup.E0, m)
+    H = setup.E1 - setup.ivp.jac(y) @ setup.E0
+    res = filtsmooth.mv(setup.E1, m) - setup.ivp.f(None, y)
+    lead = m.shape[:-1]
+    full_H = np.concatenate([H, np.broadcast_to(np.eye(D), lead + (D, D))], axis=-2)
+    full_b = np.concatenate([res, -m], axis=-1)
+    R = np.zeros(lead + (d + D, d + D))
+    R[..., d:, d:] = np.eye(D) / np.sqrt(lam)
+    return full_H, full_b, R
+
+
+def lm_ieks_iterator(setup, init_means, reg=1e0, nu=10.0):
+    """``iterators.py:109-133``, Levenberg-Marquardt-regularized IEKS
+    (arguments: the set-up's dtm, om and x0, and the trajectory to linearize
+    at first, one state per step).  The reference's step-size adaptation
+    (``nu``) is commented out, so reg stays fixed; the loop ends when nll and
+    obj both stall (``jnp.isclose`` defaults rtol 1e-5, atol 1e-8) or on
+    NaN.  Yields (states, nll, obj, reg)."""
+    dtm = (setup.F, setup.QL)
+
+    def gen():
+        st, nll, obj, _ = filtsmooth.linear_filtsmooth(setup.x0, dtm, linearize_regularized(setup, init_means, reg))
+        yield st, nll, obj, reg
+        while True:
+            nll_old, obj_old = nll, obj
+            st, nll, obj, _ = filtsmooth.linear_filtsmooth(setup.x0, dtm,
+                                                           linearize_regularized(setup, st[0][1:], reg))
+            yield st, nll, obj, reg
+            if (np.isclose(nll_old, nll) and np.isclose(obj_old, obj)) or np.isnan(nll) or np.isnan(obj):
+                break
+
+    return gen()

@@ -1,0 +1,133 @@
+"""The Python control loops of the drop-in package on CPU, with the one
+device call they make -- libpof's filter/smoother -- replaced by the
+oracle's.
+
+`pof.solver.solve` for a user vector field (the loop of pof/solver.py:24-57
+in Python: EK1 by torch.func, filter/smoother in libpof, crit read back each
+iteration), `pof.iterators.ieks_iterator`, the quadratic-penalty iterator
+(its regularization and tolerance schedule) and the Levenberg-Marquardt
+iterator are compared iteration by iteration with the oracle's
+restatements of the reference (oracle/solver.py).  What the substitution
+leaves out -- libpof's own filter/smoother -- is what the GPU tests check.
+"""
+
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+import pof.convenience  # noqa: F401  (every module that reads default_device is patched below)
+import pof.initialization  # noqa: F401
+import pof.observations  # noqa: F401
+import pof.transitions  # noqa: F401
+from oracle import filtsmooth as ofs, ivp as oivp, solver as osolver
+from pof import iterators as pit, solver as psolver, step as pstep
+from pof.utils import MVNSqrt
+
+CPU = torch.device("cpu")
+
+
+def _np(x):
+    return np.ascontiguousarray(x.detach().cpu().numpy())
+
+
+def oracle_filtsmooth(x0, dtm, dom):
+    """pof.parallel_filtsmooth.linear_filtsmooth's contract, computed by the
+    oracle on CPU tensors."""
+    (m, L), nll, obj, ssq = ofs.linear_filtsmooth((_np(x0.mean), _np(x0.chol)), (_np(dtm.F), _np(dtm.QL)),
+                                                  tuple(_np(a) for a in dom))
+
+    def T(a):
+        return torch.as_tensor(np.array(a, dtype=np.float64, copy=True), dtype=torch.float64)
+
+    return MVNSqrt(T(m), T(L)), T(nll), T(obj), T(ssq)
+
+
+@pytest.fixture
+def host_only(monkeypatch):
+    for name, mod in list(sys.modules.items()):
+        if mod is not None and (name == "pof" or name.startswith("pof.")) and hasattr(mod, "default_device"):
+            monkeypatch.setattr(mod, "default_device", lambda: CPU)
+    monkeypatch.setattr(pstep, "parallel_linear_filtsmooth", oracle_filtsmooth)
+    monkeypatch.setattr(pit, "fs", oracle_filtsmooth)
+
+
+def user_field(name):
+    """The same vector field as a plain torch function (no built-in tag: the
+    package linearizes it with torch.func and loops in Python)."""
+    if name == "logistic":
+        return lambda t, y: 3.0 * y * (1.0 - y), [0.01], oivp.logistic(r=3.0), 10.0
+    if name == "vanderpol":
+        return (lambda t, y: torch.stack([y[1], 1.0 * ((1.0 - y[0] ** 2) * y[1] - y[0])]), [2.0, 0.0],
+                oivp.vanderpol(stiffness_constant=1.0), 6.3)
+    raise KeyError(name)
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("name,q,N,init", [("logistic", 2, 60, "constant"), ("logistic", 3, 120, "prior"),
+                                           ("vanderpol", 3, 80, "constant")])
+def test_solve_loop_for_a_user_field(host_only, name, q, N, init):
+    f, y0, o, t1 = user_field(name)
+    ts = np.linspace(0.0, t1, N)
+    ys, info = psolver.solve(f=f, y0=y0, ts=ts, order=q, init=init)
+    (om, oL), oinfo = osolver.solve(o, ts, q, init=init)
+    assert int(info["iterations"]) == oinfo["iterations"]
+    assert rel(_np(ys.mean), om) <= 1e-10
+    C, oC = _np(ys.chol @ ys.chol.transpose(-1, -2)), oL @ np.swapaxes(oL, -1, -2)
+    assert rel(C, oC) <= 1e-9
+    for k in ("nll", "obj", "sigma_squared"):
+        assert np.isclose(float(info[k]), oinfo[k], rtol=1e-9), k
+    assert info["calibrated"] is True
+
+
+def test_ieks_iterator_yields_the_same_iterations(host_only):
+    f, y0, o, t1 = user_field("vanderpol")
+    ts = np.linspace(0.0, t1, 70)
+    it, _ = pit.ieks_iterator(f=f, y0=y0, ts=ts, order=2, init="constant")
+    got = [(_np(s.mean), float(nll), float(obj)) for s, nll, obj, _ in it]
+    oit, _ = osolver.ieks_iterator(o, ts, 2, init="constant")
+    want = [(s[0], nll, obj) for s, nll, obj, _ in oit]
+    assert len(got) == len(want) > 2
+    for (m, nll, obj), (om, onll, oobj) in zip(got, want):
+        assert rel(m, om) <= 1e-10 and np.isclose(nll, onll, rtol=1e-9) and np.isclose(obj, oobj, rtol=1e-9)
+
+
+def test_quadratic_penalty_iterator_follows_the_schedule(host_only):
+    """reg from 1e20 down by a factor per converged stage, snapped to 0
+    below 1e-20, loop end once crit holds at reg = 0: the same regs, the same
+    number of iterations and the same iterates as the oracle."""
+    f, y0, o, t1 = user_field("logistic")
+    ts = np.linspace(0.0, t1, 60)
+    it, _ = pit.qpm_ieks_iterator(f=f, y0=y0, ts=ts, order=2, init="constant")
+    got = [(_np(s.mean), float(obj), reg) for s, _, obj, reg in it]
+    oit, setup = osolver.qpm_ieks_iterator(o, ts, 2, init="constant")
+    want = [(s[0], obj, reg) for s, _, obj, reg in oit]
+    assert len(got) == len(want) >= 42
+    assert [r for _, _, r in got] == [r for _, _, r in want]
+    assert want[-1][2] == 0.0
+    for (m, obj, _), (om, oobj, _) in zip(got, want):
+        assert rel(m, om) <= 1e-8 and np.isclose(obj, oobj, rtol=1e-8)
+
+
+def test_levenberg_marquardt_iterator(host_only):
+    """The regularized observation (d + D rows) runs through the same
+    filter/smoother contract; the first iterations agree with the oracle."""
+    f, y0, o, t1 = user_field("logistic")
+    ts = np.linspace(0.0, t1, 40)
+    setup = pof.convenience.set_up_solver(f=f, y0=y0, ts=ts, order=2)
+    states = pof.convenience.get_initial_trajectory(setup, "constant")
+    it = pit.lm_ieks_iterator(setup["dtm"], setup["om"], setup["x0"], MVNSqrt(states.mean[1:], states.chol[1:]),
+                              reg=1.0)
+    ost = osolver.set_up_solver(o, ts, 2)
+    om0, _ = osolver.get_initial_trajectory(ost, "constant")
+    oit = osolver.lm_ieks_iterator(ost, om0[1:], reg=1.0)
+    for k in range(6):
+        s, nll, obj, reg = next(it)
+        os_, onll, oobj, oreg = next(oit)
+        assert reg == oreg == 1.0
+        assert rel(_np(s.mean), os_[0]) <= 1e-9
+        assert np.isclose(float(nll), onll, rtol=1e-9) and np.isclose(float(obj), oobj, rtol=1e-9)

@@ -233,3 +233,26 @@ def test_sigma_squared_envelope_contains_reference_orders(ivpf, N, q):
     lo, hi = ofs.sigma_squared_envelope(dtm, dom, fm, fL)
     for v in (t, s, b):
         assert lo * (1 - 1e-9) <= v <= hi * (1 + 1e-9)
+
+
+def test_quadratic_penalty_iterator_escapes_a_spurious_fixed_point():
+    """What the quadratic-penalty IEKS is for (iterators.py:44-106): on the
+    logistic ODE y' = 3 y (1 - y), y(0) = 0.01, on 60 grid points over
+    [0, 10], q = 2, the plain IEKS from the constant start stops after four
+    iterations at the fixed point y = 0, while the penalty continuation
+    (reg 1e20 -> 0 over 40 stages) ends on the solution."""
+    from oracle import ivp as oivp, solver as osolver
+
+    o = oivp.logistic(r=3.0)
+    ts = np.linspace(0.0, 10.0, 60)
+    exact = 1.0 / (1.0 + (1.0 / 0.01 - 1.0) * np.exp(-3.0 * ts))
+    (om, _), info = osolver.solve(o, ts, 2, init="constant")
+    assert info["iterations"] == 4 and abs(om[-1, 0]) < 1e-6
+    it, st = osolver.qpm_ieks_iterator(o, ts, 2, init="constant")
+    regs = []
+    for s, _, _, reg in it:
+        regs.append(reg)
+        last = s
+    ys = last[0] @ st.E0.T
+    assert regs[0] == 1e20 and regs[-1] == 0.0 and len(regs) >= 42
+    assert np.abs(ys[:, 0] - exact).max() < 1e-4
