@@ -96,3 +96,30 @@ def test_batch_argument_errors_without_gpu(lib):
     assert call(h=pz) == -1
     neg, pneg = _arr([10, -1], np.int64)
     assert call(n=pneg) == -1
+
+
+def test_projection_and_per_problem_results():
+    """project() applies each problem's E0 P to its rows (as pof.solver.solve
+    returns gmul_stack(E0 P, states)) and BatchResult.problem(b) slices
+    problem b's rows and info out of the concatenation."""
+    import torch
+
+    from pof import batch as pbatch
+
+    q = 3
+    prep = pbatch.prepare_batch(PROBLEMS, q, device=torch.device("cpu"))
+    G, D = prep["means0"].shape
+    g = torch.Generator().manual_seed(5)
+    means = torch.randn((G, D), dtype=torch.float64, generator=g)
+    chols = torch.randn((G, D, D), dtype=torch.float64, generator=g)
+    ym, yc = pbatch.project(prep, means, chols)
+    info = {"iterations": torch.arange(len(PROBLEMS)), "nll": torch.zeros(len(PROBLEMS)), "calibrated": True}
+    res = pbatch.BatchResult(ym, yc, prep["offsets"], info)
+    off = prep["offsets"]
+    for b, (nm, p, y0, ts) in enumerate(PROBLEMS):
+        E0 = osolver.set_up_solver(oracle_of(nm, p, y0, ts), ts, q).E0
+        s, e = off[b], off[b + 1]
+        (mb, cb), ib = res.problem(b)
+        np.testing.assert_allclose(mb.numpy(), means[s:e].numpy() @ E0.T, rtol=1e-14, atol=1e-300)
+        np.testing.assert_allclose(cb.numpy(), E0 @ chols[s:e].numpy(), rtol=1e-14, atol=1e-300)
+        assert int(ib["iterations"]) == b and ib["calibrated"] is True
