@@ -13,6 +13,19 @@ from .utils import MVNSqrt
 fs = linear_filtsmooth
 
 
+def lom(om, traj):
+    """EK1 of the observation model at every state of a trajectory
+    (pof/iterators.py:14: jit(vmap(linearize)))."""
+    return linearize(om, traj)
+
+
+def lom_reg(om, traj, reg):
+    """Levenberg-Marquardt-regularized linearization at every state of a
+    trajectory (pof/iterators.py:15-17: jit(vmap(linearize_regularized)))."""
+    outs = [linearize_regularized(om, MVNSqrt(traj.mean[k], traj.chol[k]), reg) for k in range(traj.mean.shape[0])]
+    return AffineModel(*(torch.stack(z) for z in zip(*outs)))
+
+
 def ieks_iterator(*, f, y0, ts, order, init="prior"):
     """Generator of IEKS iterations until ``crit`` (pof/iterators.py:20-24)."""
     setup = set_up_solver(f=f, y0=y0, ts=ts, order=order)
@@ -75,17 +88,12 @@ def _qpm_ieks_iterator(dtm, om, x0, init_traj, reg_start=1e20, reg_final=1e-20, 
 
 def lm_ieks_iterator(dtm, om, x0, init_traj, reg=1e0, nu=10.0):
     """Levenberg-Marquardt-regularized IEKS (pof/iterators.py:109-133)."""
-
-    def lom_reg(traj):
-        outs = [linearize_regularized(om, MVNSqrt(traj.mean[k], traj.chol[k]), reg) for k in range(traj.mean.shape[0])]
-        return AffineModel(*(torch.stack(z) for z in zip(*outs)))
-
-    dom = lom_reg(init_traj)
+    dom = lom_reg(om, init_traj, reg)
     out, nll, obj, ssq = fs(x0, dtm, dom)
     yield out, nll, obj, reg
     while True:
         nll_old, obj_old = nll, obj
-        dom = lom_reg(MVNSqrt(out.mean[1:], out.chol[1:]))
+        dom = lom_reg(om, MVNSqrt(out.mean[1:], out.chol[1:]), reg)
         out, nll, obj, ssq = fs(x0, dtm, dom)
         yield out, nll, obj, reg
         if (bool(torch.isclose(nll_old, nll)) and bool(torch.isclose(obj_old, obj))) or bool(torch.isnan(nll)) \

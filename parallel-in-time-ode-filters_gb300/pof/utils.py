@@ -85,3 +85,48 @@ def _gmul(A, x: MVNSqrt):
 def gmul_stack(A, states: MVNSqrt):
     """vmap(_gmul, in_axes=[None, 0])(A, states)."""
     return MVNSqrt(states.mean @ A.transpose(-1, -2), A @ states.chol)
+
+
+def linearize(f, x):
+    """First-order Taylor model of f at x: AffineModel(J, f(x) - J x), J by
+    forward-mode differentiation (pof/utils.py:86-90)."""
+    J = torch.func.jacfwd(f)(x)
+    return AffineModel(J, f(x) - J @ x)
+
+
+def _cholesky_update(chol, update_vector, multiplier=1.0):
+    """Lower-triangular L' with L' L'^T = L L^T + multiplier v v^T, column by
+    column (Krause and Igel, 2015, Algorithm 3.1, as pof/utils.py:123-172
+    states it): omega starts at v and b at 1; for column j,
+        L'_jj = sqrt(L_jj^2 + multiplier / b * omega_j^2),
+        gamma = L_jj^2 b + multiplier omega_j^2,
+        omega <- omega - (omega_j / L_jj) L[:, j],
+        L'[:, j] = L'_jj (L[:, j] / L_jj + multiplier omega_j / gamma * omega),
+        b <- b + multiplier (omega_j / L_jj)^2;
+    then the strict upper triangle is zeroed and non-finite entries set to 0."""
+    n = chol.shape[-1]
+    omega = update_vector.clone()
+    b = torch.ones((), dtype=chol.dtype, device=chol.device)
+    cols, diag = [], []
+    for j in range(n):
+        ljj = chol[j, j]
+        wj = omega[j]
+        new_d = torch.sqrt(ljj * ljj + multiplier / b * wj * wj)
+        gamma = ljj * ljj * b + multiplier * wj * wj
+        col = chol[:, j]
+        omega = omega - (wj / ljj) * col
+        cols.append(new_d * (col / ljj + (multiplier * wj / gamma) * omega))
+        diag.append(new_d)
+        b = b + multiplier * (wj / ljj) ** 2
+    out = torch.stack(cols, dim=1)
+    out = torch.tril(out, -1) + torch.diag(torch.stack(diag))
+    return torch.where(torch.isfinite(out), out, torch.zeros_like(out))
+
+
+def cholesky_update_many(chol_init, update_vectors, multiplier):
+    """Successive rank-one updates of a Cholesky factor by the rows of
+    update_vectors (pof/utils.py:115-120)."""
+    chol = chol_init
+    for v in update_vectors:
+        chol = _cholesky_update(chol, v, multiplier=multiplier)
+    return chol

@@ -4,9 +4,10 @@ Everything here runs in the drop-in package on the GPU path too: the
 linear-algebra helpers of pof/utils.py, the convergence criterion, the
 sequential one-step predict/update used by the initial trajectories, the
 initial trajectories themselves ("prior" is the default `init` of
-`pof.solver.solve`), and the EK1 / EK0 / regularized linearizations of user
-vector fields (torch.func.jacfwd).  torch runs the same operations on CPU
-and CUDA tensors, so these are checked here on the CPU.
+`pof.solver.solve`), the EK1 / EK0 / regularized linearizations of user
+vector fields (torch.func.jacfwd), and the element-level operators of the
+reference's parallel filter and smoother.  torch runs the same operations on
+CPU and CUDA tensors, so these are checked here on the CPU.
 """
 
 import numpy as np
@@ -189,3 +190,94 @@ def test_ek0_and_regularized_linearizations(rng):
     assert torch.allclose(Rr[d:, d:], torch.eye(D, dtype=torch.float64) / lam**0.5)
     # b of the EK1 rows is f(m) - H m there, f(m) in the regularized form (the reference's full_b = [res, -m])
     assert torch.allclose(b, om_fn(m) - H @ m)
+
+
+def _filter_elements(rng, B, D, d):
+    """B filter elements of random models with the reference's element
+    construction (the oracle's get_element, filter.py:50-81)."""
+    F = rng.standard_normal((B, D, D)) / np.sqrt(D)
+    QL = lower(rng, B, D, D) * 0.3
+    H = rng.standard_normal((B, d, D))
+    c = rng.standard_normal((B, d))
+    R = np.zeros((B, d, d))
+    return ofs.get_element(F, QL, H, c, R, np.zeros((B, D)), np.zeros((B, D, D)))
+
+
+def _same_element(a, b, tol):
+    A, bb, U, eta, Z = (x.numpy() if isinstance(x, torch.Tensor) else x for x in a)
+    oA, ob, oU, oeta, oZ = b
+    for x, y in ((A, oA), (bb, ob), (eta, oeta), (gram(U), gram(oU)), (gram(Z), gram(oZ))):
+        assert np.allclose(x, y, rtol=tol, atol=tol * max(np.abs(y).max(), 1.0))
+
+
+def test_filtering_operator_matches_oracle_and_is_associative(rng):
+    from pof.parallel_filtsmooth.filter import sqrt_filtering_operator
+
+    B, D, d = 6, 6, 2
+    e1, e2, e3 = (_filter_elements(rng, B, D, d) for _ in range(3))
+    t = lambda e: tuple(T(x) for x in e)  # noqa: E731
+    got = sqrt_filtering_operator(t(e1), t(e2))
+    _same_element(got, ofs.sqrt_filtering_operator(e1, e2), 1e-11)
+    left = sqrt_filtering_operator(sqrt_filtering_operator(t(e1), t(e2)), t(e3))
+    right = sqrt_filtering_operator(t(e1), sqrt_filtering_operator(t(e2), t(e3)))
+    _same_element(left, tuple(x.numpy() for x in right), 1e-9)
+
+
+def test_smoother_elements_and_operator_match_oracle(rng):
+    from pof.parallel_filtsmooth.smoother import get_elements, sqrt_smoothing_operator
+
+    N, D = 9, 5
+    F = rng.standard_normal((N - 1, D, D)) / np.sqrt(D)
+    QL = lower(rng, N - 1, D, D) * 0.3
+    ms = rng.standard_normal((N, D))
+    Ls = lower(rng, N, D, D)
+    g, E, L = get_elements((T(F), T(QL)), MVNSqrt(T(ms), T(Ls)))
+    og, oE, oL = ofs.get_smoother_elements((F, QL), (ms, Ls))
+    assert np.allclose(g.numpy(), og, rtol=1e-11, atol=1e-11) and np.allclose(E.numpy(), oE, rtol=1e-11, atol=1e-11)
+    assert np.allclose(gram(L.numpy()), gram(oL), rtol=1e-11, atol=1e-11)
+    a = (g[1:], E[1:], L[1:])
+    b = (g[:-1], E[:-1], L[:-1])
+    cg, cE, cD = sqrt_smoothing_operator(a, b)
+    og, oE, oD = ofs.sqrt_smoothing_operator((og[1:], oE[1:], oL[1:]), (og[:-1], oE[:-1], oL[:-1]))
+    assert np.allclose(cg.numpy(), og, rtol=1e-11, atol=1e-11) and np.allclose(cE.numpy(), oE, rtol=1e-11, atol=1e-11)
+    assert np.allclose(gram(cD.numpy()), gram(oD), rtol=1e-11, atol=1e-11)
+
+
+def test_utils_linearize_is_the_first_order_model():
+    f = lambda x: torch.stack([x[0] * x[1], torch.sin(x[0]) + x[1] ** 3])  # noqa: E731
+    x = torch.tensor([0.3, -1.2], dtype=torch.float64)
+    A, b = pu.linearize(f, x)
+    J = torch.tensor([[x[1], x[0]], [torch.cos(x[0]), 3 * x[1] ** 2]], dtype=torch.float64)
+    assert torch.allclose(A, J) and torch.allclose(b, f(x) - J @ x)
+    assert torch.allclose(pu.AffineModel(A, b)(x), f(x))
+
+
+@pytest.mark.parametrize("multiplier", [1.0, 0.25])
+def test_cholesky_update_many(rng, multiplier):
+    """L' L'^T = L L^T + multiplier sum_k v_k v_k^T, L' lower-triangular."""
+    n = 5
+    L = lower(rng, n, n)
+    V = rng.standard_normal((3, n))
+    out = pu.cholesky_update_many(T(L), T(V), multiplier).numpy()
+    assert np.array_equal(out, np.tril(out))
+    assert np.allclose(gram(out), gram(L) + multiplier * V.T @ V, rtol=1e-12, atol=1e-12)
+
+
+def test_trajectory_linearizers_of_the_iterators(rng):
+    """lom / lom_reg (pof/iterators.py:14-17) stack the one-state
+    linearizations over a trajectory."""
+    from pof import iterators as pit
+
+    E1 = T(np.kron(np.eye(2), np.eye(1, 3, 1)))
+    E0 = T(np.kron(np.eye(2), np.eye(1, 3, 0)))
+    p = pivp.lotkavolterra()
+    om = pobs.NonlinearModel(lambda x: E1 @ x - p.f(None, E0 @ x))
+    traj = MVNSqrt(T(rng.uniform(0.5, 1.5, (4, 6))), torch.zeros(4, 6, 6, dtype=torch.float64))
+    H, b, R = pit.lom(om, traj)
+    Hr, br, Rr = pit.lom_reg(om, traj, 2.0)
+    for k in range(4):
+        x = MVNSqrt(traj.mean[k], traj.chol[k])
+        h, bb, r = pobs.linearize(om, x)
+        assert torch.allclose(H[k], h) and torch.allclose(b[k], bb) and torch.equal(R[k], r)
+        h, bb, r = pobs.linearize_regularized(om, x, 2.0)
+        assert torch.allclose(Hr[k], h) and torch.allclose(br[k], bb) and torch.equal(Rr[k], r)
