@@ -192,3 +192,42 @@ def test_sizes_strides_and_workspace_checked_before_any_cuda_call(lib):
     assert mixed(rtol=0.0) == ARG
     assert mixed(settle=float("nan")) == ARG
     assert mixed(wsb=mws - 1) == WORKSPACE
+
+
+REFERENCE_API = {
+    # the reference's public names per module (pof/*.py), as this package provides them
+    "pof.solver": ["solve", "sequential_eks_solve"],
+    "pof.parallel_filtsmooth": ["linear_filtsmooth", "linear_noiseless_filtering", "smoothing"],
+    "pof.parallel_filtsmooth.filter": ["linear_noiseless_filtering", "sqrt_filtering_operator"],
+    "pof.parallel_filtsmooth.smoother": ["smoothing", "get_elements", "sqrt_smoothing_operator"],
+    "pof.sequential_filtsmooth": ["filtsmooth", "linear_filtsmooth"],
+    "pof.sequential_filtsmooth.filter": ["extended_kalman_filter", "linear_noiseless_filter"],
+    "pof.sequential_filtsmooth.smoother": ["smoothing"],
+    "pof.step": ["linearize_at_previous_states", "inflate", "ieks_step"],
+    "pof.iterators": ["fs", "lom", "lom_reg", "ieks_iterator", "qpm_ieks_iterator", "lm_ieks_iterator"],
+    "pof.observations": ["NonlinearModel", "AffineModel", "linearize", "uncertain_linearize", "linearize_ek0",
+                         "linearize_regularized"],
+    "pof.transitions": ["TransitionModel", "IWP", "hilbert", "pascal", "preconditioned_discretize_1d",
+                        "preconditioned_discretize", "nordsieck_preconditioner_1d", "nordsieck_preconditioner",
+                        "non_preconditioned_discretize", "projection_matrix_1d", "projection_matrix",
+                        "get_transition_model", "discretize_transitions"],
+    "pof.convergence_criteria": ["crit"],
+    "pof.convenience": ["linearize_observation_model", "set_up_solver", "set_up_solver_no_precond",
+                        "get_initial_trajectory"],
+    "pof.initialization": ["taylor_mode_init", "uncertain_init", "constant_init", "classic_to_init", "prior_init",
+                           "updated_prior_init", "coarse_ekf_init"],
+    "pof.ivp": ["logistic", "lotkavolterra", "vanderpol", "fitzhughnagumo", "rober", "rigid_body", "seir",
+                "threebody", "henonheiles"],
+    "pof.utils": ["MVNSqrt", "AffineModel", "mvn_loglikelihood", "tria", "qr", "linearize",
+                  "append_zeros_along_new_axis", "objective_function_value", "_gmul", "whiten",
+                  "cholesky_update_many"],
+}
+
+
+@pytest.mark.parametrize("module", sorted(REFERENCE_API))
+def test_reference_api_names_exist(module):
+    import importlib
+
+    mod = importlib.import_module(module)
+    missing = [n for n in REFERENCE_API[module] if not hasattr(mod, n)]
+    assert not missing, missing
