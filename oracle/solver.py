@@ -63,6 +63,21 @@ def set_up_solver(ivp, ts, order):
     return Setup(ivp, ts, d, q, F, QLs, P, PI, E0, E1, x0)
 
 
+def set_up_solver_no_precond(ivp, ts, order):
+    """``convenience.py:48-73``: per-step NON-preconditioned transitions at
+    the grid's own step sizes (so a non-uniform grid is honoured), P = PI =
+    I, plain projections, x0 by Taylor mode."""
+    ts = np.asarray(ts, dtype=np.float64)
+    d = ivp.y0.shape[0]
+    q = order
+    F, QL = core.discretize_transitions(d, q, ts[1:] - ts[:-1])
+    D = d * (q + 1)
+    I = np.eye(D)
+    E0 = core.projection_matrix(d, q, 0)
+    E1 = core.projection_matrix(d, q, 1)
+    return Setup(ivp, ts, d, q, F, QL, I, I, E0, E1, taylor_mode_init(ivp, q))
+
+
 def observation_residual(setup, x):
     """The ``NonlinearModel`` of ``convenience.py:28``: E1 x - f(E0 x)."""
     y = filtsmooth.mv(setup.E0, x)

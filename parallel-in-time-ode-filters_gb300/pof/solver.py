@@ -4,7 +4,7 @@ import torch
 
 from . import _lib
 from . import convergence_criteria
-from .convenience import get_initial_trajectory, set_up_solver
+from .convenience import get_initial_trajectory, set_up_solver, set_up_solver_no_precond
 from .sequential_filtsmooth import filtsmooth as seq_fs
 from .step import ieks_step
 from .utils import MVNSqrt, gmul_stack
@@ -79,7 +79,6 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     info["iterations"] counts the float64 ones, info["iterations_float32"]
     the others."""
     setup = set_up_solver(f=f, y0=y0, ts=ts, order=order)
-    dtm = setup["dtm"]
     om = setup["om"]
     x0 = setup["x0"]
     states = get_initial_trajectory(setup, method=init)
@@ -90,7 +89,14 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
         return gmul_stack(setup["E0"], states), info_dict
     if precision != "float64":
         raise NotImplementedError("precision=%r needs a built-in field (pof.ivp)" % (precision,))
+    return _solve_loop(setup, states, calibrate, maxiters, sequential)
 
+
+def _solve_loop(setup, states, calibrate, maxiters, sequential):
+    """The IEKS loop of pof/solver.py:24-73 in Python: each iteration
+    linearizes (libpof for built-in fields, torch.func otherwise) and runs
+    libpof's filter/smoother; crit is read back each iteration."""
+    dtm, om, x0 = setup["dtm"], setup["om"], setup["x0"]
     dev = x0.mean.device
     z = torch.zeros((), dtype=torch.float64, device=dev)
     nll = obj = ssq = z
@@ -110,6 +116,19 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
         states = MVNSqrt(states.mean, ssq**0.5 * states.chol)
         info_dict["calibrated"] = True
     return gmul_stack(setup["E0"], states), info_dict
+
+
+def solve_nonuniform(*, f, y0, ts, order, init="constant", calibrate=True, maxiters=10_000, sequential=False):
+    """Parallel-in-time IEKS on a grid with its own step sizes (an addition
+    to the reference, whose solve takes every step as ts[1] - ts[0],
+    pof/convenience.py:14-16).  The set-up is the reference's
+    set_up_solver_no_precond (pof/convenience.py:48-73): one
+    non-preconditioned IWP transition per step, plain projections; the loop
+    and the returned values are those of solve (pof/solver.py:24-73).  The
+    per-step transitions go to libpof as (n, D, D) stacks."""
+    setup = set_up_solver_no_precond(f=f, y0=y0, ts=ts, order=order)
+    states = get_initial_trajectory(setup, method=init)
+    return _solve_loop(setup, states, calibrate, maxiters, sequential)
 
 
 def sequential_eks_solve(*, f, y0, ts, order, return_full_states=False, calibrate=True):

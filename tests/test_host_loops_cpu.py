@@ -131,3 +131,48 @@ def test_levenberg_marquardt_iterator(host_only):
         assert reg == oreg == 1.0
         assert rel(_np(s.mean), os_[0]) <= 1e-9
         assert np.isclose(float(nll), onll, rtol=1e-9) and np.isclose(float(obj), oobj, rtol=1e-9)
+
+
+def _oracle_loop(st, init="constant", maxiters=10_000):
+    """The reference's IEKS loop (solver.py:24-57) over any oracle set-up."""
+    states = osolver.get_initial_trajectory(st, init)
+    nll = obj = 0.0
+    old, nll_old, obj_old = states, 0.0, 0.0
+    k = 0
+    while k < 1 or (not osolver.crit(obj, obj_old, nll, nll_old, states[0], old[0]) and k <= maxiters):
+        old, nll_old, obj_old = states, nll, obj
+        states, nll, obj, _ = osolver.ieks_step(st, old)
+        k += 1
+    return states, k
+
+
+def test_non_uniform_grid_solve(host_only):
+    """pof.solver.solve_nonuniform: per-step non-preconditioned transitions
+    (the reference's set_up_solver_no_precond) on a grid refined towards
+    t = 0.  Same iterations and means as the oracle's loop over the same
+    set-up, and the solution of y' = y (1 - y), y(0) = 0.01, to 1e-6, where
+    the reference's solve, taking every step as ts[1] - ts[0], is far off."""
+    f = lambda t, y: y * (1.0 - y)  # noqa: E731
+    o = oivp.logistic(r=1.0)
+    u = np.linspace(0.0, 1.0, 50)
+    ts = 10.0 * (1.0 - (1.0 - u) ** 2)
+    exact = 1.0 / (1.0 + 99.0 * np.exp(-ts))
+    ys, info = psolver.solve_nonuniform(f=f, y0=[0.01], ts=ts, order=3)
+    st = osolver.set_up_solver_no_precond(o, ts, 3)
+    (om, _), k = _oracle_loop(st)
+    assert int(info["iterations"]) == k
+    assert rel(_np(ys.mean), om @ st.E0.T) <= 1e-10
+    assert np.abs(_np(ys.mean)[:, 0] - exact).max() < 1e-6
+    (wrong, _), _ = osolver.solve(o, ts, 3, init="constant")
+    assert np.abs(wrong[:, 0] - exact).max() > 1e-2
+
+
+def test_non_preconditioned_set_up_on_a_uniform_grid(host_only):
+    """On a uniform grid the Nordsieck preconditioning is only a change of
+    coordinates: the same IEKS iterations and the same solution."""
+    f = lambda t, y: y * (1.0 - y)  # noqa: E731
+    ts = np.linspace(0.0, 10.0, 80)
+    a, ia = psolver.solve(f=f, y0=[0.01], ts=ts, order=3, init="constant")
+    b, ib = psolver.solve_nonuniform(f=f, y0=[0.01], ts=ts, order=3)
+    assert int(ia["iterations"]) == int(ib["iterations"])
+    assert rel(_np(b.mean), _np(a.mean)) <= 1e-11
