@@ -281,3 +281,57 @@ def test_trajectory_linearizers_of_the_iterators(rng):
         assert torch.allclose(H[k], h) and torch.allclose(b[k], bb) and torch.equal(R[k], r)
         h, bb, r = pobs.linearize_regularized(om, x, 2.0)
         assert torch.allclose(Hr[k], h) and torch.allclose(br[k], bb) and torch.equal(Rr[k], r)
+
+
+def test_uncertain_and_classic_inits():
+    """uncertain_init (initialization.py:25-39): mean [y0, f(y0), 0, ...] per
+    dimension, chol sqrt(var) except 0 on each dimension's first two
+    derivatives; classic_to_init (:59-72): [y, f(y), 0, ...] rows, chol 0."""
+    p = pivp.lotkavolterra()
+    q, d = 3, 2
+    x = pinit.uncertain_init(p.f, p.y0, q, var=4.0, device=CPU)
+    f0 = p.f(None, p.y0)
+    want = torch.zeros(d, q + 1, dtype=torch.float64)
+    want[:, 0], want[:, 1] = p.y0, f0
+    assert torch.allclose(x.mean, want.reshape(-1))
+    diag = torch.full((d, q + 1), 2.0, dtype=torch.float64)
+    diag[:, :2] = 0.0
+    assert torch.equal(x.chol, torch.diag(diag.reshape(-1)))
+    ys = torch.tensor([[1.0, 1.0], [0.5, 2.0], [3.0, 0.1]], dtype=torch.float64)
+    c = pinit.classic_to_init(ys=ys, order=q, f=p.f)
+    for k in range(3):
+        row = torch.zeros(d, q + 1, dtype=torch.float64)
+        row[:, 0], row[:, 1] = ys[k], p.f(None, ys[k])
+        assert torch.allclose(c.mean[k], row.reshape(-1))
+    assert not c.chol.any()
+
+
+def test_updated_prior_init_matches_oracle():
+    """updated_prior_init (initialization.py:92-100): the one-step prior
+    predictions from x0, each updated by the noiseless EK1 observation at
+    its own mean."""
+    q = 2
+    p, o = pivp.vanderpol(stiffness_constant=1.0), oivp.vanderpol(stiffness_constant=1.0)
+    ts = np.linspace(0.0, 6.3, 12)
+    st = osolver.set_up_solver(o, ts, q)
+    iwp = ptr.IWP(wiener_process_dimension=2, num_derivatives=q)
+    P, PI = ptr.nordsieck_preconditioner(iwp, ts[1] - ts[0], device=CPU)
+    E0 = ptr.projection_matrix(iwp, 0, device=CPU) @ P
+    E1 = ptr.projection_matrix(iwp, 1, device=CPU) @ P
+    om = pobs.NonlinearModel(lambda x: E1 @ x - p.f(None, E0 @ x))
+    x0 = MVNSqrt(T(st.x0[0]), T(st.x0[1]) + T(0.1 * np.eye(6)))
+    dtm = (T(st.F), T(st.QL))
+    got = pinit.updated_prior_init(x0=x0, dtm=dtm, om=om)
+    pm, pL = ofs.sqrt_predict(st.F, st.QL, np.broadcast_to(_np_(x0.mean), (len(ts) - 1, 6)),
+                              np.broadcast_to(_np_(x0.chol), (len(ts) - 1, 6, 6)))
+    pm = np.concatenate([_np_(x0.mean)[None], pm])
+    pL = np.concatenate([_np_(x0.chol)[None], pL])
+    H, c, R = osolver.linearize(st, pm)
+    for k in range(len(ts)):
+        (m, L), _, _ = ofs.sqrt_update(H[k], R[k], c[k], pm[k], pL[k])
+        assert np.allclose(got.mean[k].numpy(), m, rtol=1e-10, atol=1e-12)
+        assert np.allclose(gram(got.chol[k].numpy()), gram(L), rtol=1e-9, atol=1e-12)
+
+
+def _np_(t):
+    return t.detach().numpy()
