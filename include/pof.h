@@ -204,9 +204,10 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
 
 /* pof_linear_filtsmooth without a workspace argument.  It has no
  * counterpart in the reference: it exists for callers that cannot allocate
- * device memory -- code that runs while a CUDA graph is being captured,
- * hosts whose device allocator belongs to someone else, real-time loops that
- * forbid cudaMalloc after start-up -- and can only pass inputs and outputs.
+ * device memory -- plugin hosts that hand a library only its input and
+ * output buffers, programs whose device memory belongs to another allocator
+ * (a framework's caching pool), real-time loops that must not call
+ * cudaMalloc after start-up -- and can only pass inputs and outputs.
  * Arguments and results are those of pof_linear_filtsmooth.
  *  - Scratch is a fixed 16 MiB device array inside libpof, held by every GPU
  *    that loads the library until the process exits.  Problems whose

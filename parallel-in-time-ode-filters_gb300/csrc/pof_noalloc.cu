@@ -1,8 +1,8 @@
 // pof_linear_filtsmooth_noalloc: the filter + smoother pass without a
 // caller-provided workspace, for callers that cannot allocate device memory
-// (code running inside a CUDA graph capture or under an allocator that is
-// owned by someone else, real-time loops that forbid cudaMalloc after
-// start-up, plugin hosts that only hand out input and output buffers).
+// (plugin hosts that only hand out input and output buffers, programs whose
+// device memory is owned by another allocator, real-time loops that must
+// not call cudaMalloc after start-up).
 //
 // The scratch memory lives in one file-scope device array of
 // POF_NOALLOC_SCRATCH_BYTES, which every GPU that loads libpof holds until

@@ -1,7 +1,8 @@
 """The allocation-free filter/smoother entry point (collected last).
 
 pof_linear_filtsmooth_noalloc serves callers that cannot allocate device
-memory (graph capture in progress, a foreign allocator, real-time loops):
+memory (plugin hosts that pass only inputs and outputs, a foreign
+allocator, real-time loops that must not call cudaMalloc):
 its scratch is a fixed array inside libpof.  Called twice in a row through
 the C ABI, it must give the results of pof_linear_filtsmooth, which uses a
 caller-provided workspace, and it must refuse problems larger than its
