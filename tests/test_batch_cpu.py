@@ -123,3 +123,30 @@ def test_projection_and_per_problem_results():
         np.testing.assert_allclose(mb.numpy(), means[s:e].numpy() @ E0.T, rtol=1e-14, atol=1e-300)
         np.testing.assert_allclose(cb.numpy(), E0 @ chols[s:e].numpy(), rtol=1e-14, atol=1e-300)
         assert int(ib["iterations"]) == b and ib["calibrated"] is True
+
+
+def test_server_and_mixed_workspace_queries_and_refusals(lib):
+    """The serving engine's and the mixed-precision batch's size queries, and
+    pof_server_create's refusals, which all happen on the host before any
+    CUDA call (placeholder pointers are never used)."""
+    w = lib.pof_server_workspace_bytes(8, 2, 16, 100_000, 1 << 20)
+    assert w > 0
+    assert lib.pof_server_workspace_bytes(8, 2, 32, 100_000, 1 << 20) > w
+    assert lib.pof_server_workspace_bytes(8, 2, 16, 200_000, 1 << 20) > w
+    assert lib.pof_server_workspace_bytes(8, 2, 16, 100_000, 1 << 24) > w
+    assert lib.pof_server_workspace_bytes(7, 2, 16, 100_000, 1 << 20) == 0  # shape not compiled
+    assert lib.pof_server_workspace_bytes(8, 2, 0, 100_000, 1 << 20) == 0
+    assert lib.pof_server_workspace_bytes(8, 2, 16, 1, 1 << 20) == 0
+    P = 256
+    h = ctypes.c_void_p()
+    assert lib.pof_server_create(8, 2, 16, 100_000, 1 << 20, P, P, 1, P, w, None) == -1  # no out pointer
+    assert lib.pof_server_create(7, 2, 16, 100_000, 1 << 20, P, P, 1, P, w, ctypes.byref(h)) == -2
+    assert lib.pof_server_create(8, 2, 0, 100_000, 1 << 20, P, P, 1, P, w, ctypes.byref(h)) == -1
+    assert lib.pof_server_create(8, 2, 16, 100_000, 1 << 20, P, P, 1, P, w - 1, ctypes.byref(h)) == -3
+    assert h.value is None
+
+    ns, pns = _arr([299, 1000, 32, 63], np.int64)
+    w64 = lib.pof_batch_workspace_bytes(0, 4, pns, 8, 2, 0, 0)
+    wmx = lib.pof_batch_mixed_workspace_bytes(4, pns, 8, 2, 0, 0)
+    assert wmx > w64 > 0
+    assert lib.pof_batch_mixed_workspace_bytes(4, pns, 7, 2, 0, 0) == 0
