@@ -1,0 +1,189 @@
+"""Host side of the continuous-batching server (pof.serve) on CPU.
+
+`pof.serve.Server` queues requests, keeps one engine per (d, q), admits
+requests in arrival order while an engine has a free slot and memory, runs
+ticks and collects finished requests.  Here libpof's engine (pof_server_*,
+which the GPU tests exercise) is replaced by a host fake with the same
+contract: a slot table, a grid-point budget, and requests that finish after
+a number of iterations fixed at admission.  The tests check the Server's
+own logic: FIFO admission within a shape, shapes that do not block one
+another, queueing under the memory budget, and the results each request
+gets back.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from pof import _lib, batch as pbatch, serve
+
+CPU = torch.device("cpu")
+BUSY = -7
+
+
+class FakeEngines:
+    """pof_server_* on the host.  A request of n steps holds n + 1 grid
+    points from admission until its result is fetched, and finishes after
+    `iterations(n)` IEKS iterations."""
+
+    def __init__(self, iterations):
+        self.iterations = iterations
+        self.servers = {}
+        self.log = []  # (event, engine (D, d), slot, n_steps)
+
+    def _s(self, h):
+        return self.servers[h.value if isinstance(h, ctypes.c_void_p) else h]
+
+    def pof_status_string(self, rc):
+        return b"fake status %d" % rc
+
+    def pof_server_workspace_bytes(self, D, d, max_requests, max_points, level_bytes):
+        return 4096
+
+    def pof_server_create(self, D, d, max_requests, max_points, level_bytes, F, QL, calibrate, ws, wsb, out):
+        h = len(self.servers) + 1
+        self.servers[h] = {"D": D, "d": d, "maxB": max_requests, "maxG": max_points, "used": 0, "slots": {},
+                           "done": []}
+        out._obj.value = h
+        return 0
+
+    def pof_server_destroy(self, h):
+        return 0
+
+    def pof_server_submit(self, h, n_steps, field, params, step, x0m, x0L, row, maxiters, rtol):
+        s = self._s(h)
+        free = [i for i in range(s["maxB"]) if i not in s["slots"]]
+        if not free or s["used"] + n_steps + 1 > s["maxG"]:
+            return BUSY
+        slot = free[0]
+        s["slots"][slot] = {"n": n_steps, "it": 0, "target": self.iterations(n_steps), "done": False}
+        s["used"] += n_steps + 1
+        self.log.append(("admit", (s["D"], s["d"]), slot, n_steps))
+        return slot
+
+    def pof_server_launch(self, h, k):
+        s = self._s(h)
+        for slot, r in sorted(s["slots"].items()):
+            if not r["done"]:
+                r["it"] = min(r["it"] + k, r["target"])
+                if r["it"] == r["target"]:
+                    r["done"] = True
+                    s["done"].append(slot)
+        return 0
+
+    def pof_server_sync(self, h, nref):
+        nref._obj.value = sum(1 for r in self._s(h)["slots"].values() if not r["done"])
+        return 0
+
+    def pof_server_poll(self, h, buf, cap):
+        s = self._s(h)
+        out, s["done"] = s["done"][:cap], s["done"][cap:]
+        arr = (ctypes.c_int64 * cap).from_address(buf.value)
+        for i, slot in enumerate(out):
+            arr[i] = slot
+        return len(out)
+
+    def pof_server_fetch(self, h, slot, m, L, info):
+        s = self._s(h)
+        r = s["slots"].pop(slot)
+        s["used"] -= r["n"] + 1
+        N, D = r["n"] + 1, s["D"]
+        # every state's mean holds (n_steps, slot) so the test can tell results apart
+        mean = np.tile(np.array([r["n"], slot] * D, dtype=np.float64)[:D], (N, 1))
+        chol = np.zeros((N, D, D))
+        inf = np.array([r["it"], 1.0, 2.0, 3.0])
+        for ptr, a in ((m, mean), (L, chol), (info, inf)):
+            ctypes.memmove(ptr.value, a.ctypes.data, a.nbytes)
+        self.log.append(("fetch", (s["D"], s["d"]), slot, r["n"]))
+        return 0
+
+
+@pytest.fixture
+def fake(monkeypatch):
+    f = FakeEngines(iterations=lambda n: 2 + n // 100)
+    monkeypatch.setattr(_lib, "lib", lambda: f)
+    # the fake engine takes host tensors (the real pointer helper refuses them)
+    monkeypatch.setattr(_lib, "ptr", lambda t: None if t is None else ctypes.c_void_p(t.data_ptr()))
+    monkeypatch.setattr(serve, "default_device", lambda: CPU)
+    return f
+
+
+def _run(srv, limit=1000):
+    ticks = 0
+    while srv.busy():
+        srv.tick()
+        ticks += 1
+        assert ticks < limit
+    return ticks
+
+
+def logistic(n):
+    return ("logistic", (3.0,), [0.01], np.linspace(0.0, 10.0, n + 1))
+
+
+def vdp(n):
+    return ("vanderpol", (1.0,), [2.0, 0.0], np.linspace(0.0, 6.3, n + 1))
+
+
+def test_fifo_admission_with_two_slots(fake):
+    srv = serve.Server(max_requests=2, max_points=10**6)
+    ns = [450, 120, 300, 50, 220]
+    rids = [srv.submit(*logistic(n), order=2) for n in ns]
+    _run(srv)
+    admitted = [n for ev, _, _, n in fake.log if ev == "admit"]
+    assert admitted == ns  # arrival order
+    live = 0
+    for ev, _, _, _ in fake.log:  # never more than two requests hold a slot
+        live += 1 if ev == "admit" else -1
+        assert 0 <= live <= 2
+    for rid, n in zip(rids, ns):
+        (m, L), info = srv.result(rid)
+        assert m.shape == (n + 1, 1) and L.shape == (n + 1, 1, 3)
+        assert int(info["iterations"]) == 2 + n // 100
+        assert info["calibrated"] is True
+        assert srv.t_done[rid] >= srv.t_submit[rid]
+
+
+def test_results_are_projected_per_request(fake):
+    """result() applies the request's own E0 P: mean[:, 0] * p0, p0 the
+    Nordsieck scale of its step."""
+    srv = serve.Server(max_requests=4, max_points=10**6)
+    ns = [100, 333]
+    rids = [srv.submit(*logistic(n), order=2) for n in ns]
+    _run(srv)
+    for rid, n in zip(rids, ns):
+        (m, _), _ = srv.result(rid)
+        p0 = float(pbatch.prepare_rows([logistic(n)], 2)["p0"][0])
+        assert torch.allclose(m[:, 0], torch.full((n + 1,), n * p0, dtype=torch.float64))
+
+
+def test_memory_budget_keeps_fifo_within_a_shape(fake):
+    """A request that does not fit waits, and later requests of the same
+    shape wait behind it even if they would fit; other shapes go ahead."""
+    srv = serve.Server(max_requests=8, max_points=1000)
+    a = srv.submit(*logistic(600), order=2)
+    b = srv.submit(*logistic(700), order=2)   # does not fit next to a
+    c = srv.submit(*logistic(10), order=2)    # would fit, but b is first in line
+    v = srv.submit(*vdp(500), order=3)        # another engine: admitted at once
+    srv.tick()
+    admitted = [(shape, n) for ev, shape, _, n in fake.log if ev == "admit"]
+    assert admitted == [((3, 1), 600), ((8, 2), 500)]
+    _run(srv)
+    admitted = [n for ev, shape, _, n in fake.log if ev == "admit" and shape == (3, 1)]
+    assert admitted == [600, 700, 10]
+    for rid in (a, b, c, v):
+        assert rid in srv.results
+    assert not srv.busy()
+
+
+def test_engines_per_shape_and_close(fake):
+    srv = serve.Server(max_requests=4, max_points=10**5)
+    srv.submit(*logistic(50), order=2)
+    srv.submit(*logistic(50), order=3)
+    srv.submit(*vdp(50), order=3)
+    _run(srv)
+    assert sorted(srv.engines) == [(1, 2), (1, 3), (2, 3)]
+    srv.close()
+    assert srv.engines == {}
