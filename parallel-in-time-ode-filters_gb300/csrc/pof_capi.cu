@@ -597,8 +597,8 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
   k_d2f<<<g1d(D * D), 256, 0, st>>>(QL, fQL, D * D);
   k_init_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(w32 + m.p32.scalars));
   StepModel sm32{fF, fQL, 0, fH, fc, nullptr, 0};
-  // float32 phase: linearize in float64, filter/smooth in float32, judge the
-  // step in float64
+  // float32 phase: linearize in float64, filter/smooth in float32, measure
+  // each step's change in float64
   int64_t it32 = 0;
   double prev = 1e300, best = 1e300;
   int worse = 0;
