@@ -256,3 +256,33 @@ def test_quadratic_penalty_iterator_escapes_a_spurious_fixed_point():
     ys = last[0] @ st.E0.T
     assert regs[0] == 1e20 and regs[-1] == 0.0 and len(regs) >= 42
     assert np.abs(ys[:, 0] - exact).max() < 1e-4
+
+
+@pytest.mark.parametrize("D,d,n", [(8, 2, 61), (6, 3, 40), (4, 1, 33)])
+@pytest.mark.parametrize("C0,Cs,segmented,ks_max", [(4, (2,) * 8, False, 0), (3, (3, 2), False, 0),
+                                                     (5, (2,), True, 0), (1, (2,) * 8, False, 16)])
+def test_blocked_schedules_on_unstructured_per_step_models(D, d, n, C0, Cs, segmented, ks_max):
+    """The kernels' schedules (chunked tree, batched segmentation, parallel
+    top) restated in oracle/blocked.py, on models with none of the IWP
+    prior's zero patterns: a dense F and a full lower Q_L per step, a nonzero
+    observation noise per step, x0 with a full chol.  Same filtered and
+    smoothed marginals, NLL and objectives as the reference scan."""
+    rng = np.random.default_rng(1000 * D + n)
+    F = rng.standard_normal((n, D, D)) / np.sqrt(D) + 0.5 * np.eye(D)
+    QL = np.tril(rng.standard_normal((n, D, D))) * 0.2 + 0.5 * np.eye(D)
+    H = rng.standard_normal((n, d, D))
+    c = rng.standard_normal((n, d))
+    R = np.tril(rng.standard_normal((n, d, d))) * 0.1 + 0.3 * np.eye(d)
+    x0 = (rng.standard_normal(D), np.tril(rng.standard_normal((D, D))) * 0.3 + np.eye(D))
+    dtm, dom = (F, QL), (H, c, R)
+    (fm, fL), nll, obj, _ = ofs.linear_noiseless_filtering(x0, dtm, dom)
+    (bm, bL), bnll, bobj, _, _ = blocked.filter_blocked(x0, dtm, dom, C0=C0, Cs=Cs, segmented=segmented,
+                                                         ks_max=ks_max)
+    assert np.abs(fm - bm).max() <= 1e-10 * np.abs(fm).max()
+    assert _covd(bL, fL) <= 1e-10
+    assert abs(nll - bnll) <= 1e-10 * abs(nll) and abs(obj - bobj) <= 1e-10 * abs(obj)
+    (sm, sL), sobj = ofs.smoothing(dtm, (fm, fL))
+    (bsm, bsL), bsobj = blocked.smoother_blocked(dtm, (bm, bL), C0=C0, Cs=Cs, segmented=segmented, ks_max=ks_max)
+    assert np.abs(sm - bsm).max() <= 1e-10 * np.abs(sm).max()
+    assert _covd(bsL, sL) <= 1e-10
+    assert abs(sobj - bsobj) <= 1e-10 * abs(sobj)
