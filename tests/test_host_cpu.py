@@ -335,3 +335,25 @@ def test_updated_prior_init_matches_oracle():
 
 def _np_(t):
     return t.detach().numpy()
+
+
+FIELDS = [("logistic", {}), ("logistic", {"r": 3.0}), ("lotkavolterra", {}), ("vanderpol", {}),
+          ("fitzhughnagumo", {}), ("fhn_classic", {}), ("rober", {}), ("rigid_body", {}), ("seir", {}),
+          ("threebody", {}), ("henonheiles", {})]
+
+
+@pytest.mark.parametrize("name,kw", FIELDS)
+def test_builtin_fields_match_the_oracle(rng, name, kw):
+    """Every pof.ivp field (torch) against the oracle's restatement of
+    pof/ivp.py: values and Jacobians (torch.func.jacfwd against the oracle's
+    forward-mode Jacobian) at perturbed initial values, and the same y0,
+    time span and parameters."""
+    p, o = getattr(pivp, name)(**kw), getattr(oivp, name)(**kw)
+    assert np.array_equal(p.y0.numpy(), o.y0) and (p.t0, p.tmax) == (o.t0, o.tmax)
+    assert p.f.pof_field == (o.name, tuple(float(x) for x in o.params))
+    for _ in range(3):
+        y = o.y0 * (1 + 0.1 * rng.standard_normal(o.y0.shape)) + 0.01 * rng.standard_normal(o.y0.shape)
+        fy = p.f(None, T(y)).numpy()
+        assert np.allclose(fy, o.f(None, y), rtol=1e-13, atol=1e-13 * max(1.0, np.abs(fy).max()))
+        J = torch.func.jacfwd(lambda yy: p.f(None, yy))(T(y)).numpy()
+        assert np.allclose(J, o.jac(y), rtol=1e-12, atol=1e-12 * max(1.0, np.abs(J).max()))
