@@ -176,3 +176,28 @@ def test_non_preconditioned_set_up_on_a_uniform_grid(host_only):
     b, ib = psolver.solve_nonuniform(f=f, y0=[0.01], ts=ts, order=3)
     assert int(ia["iterations"]) == int(ib["iterations"])
     assert rel(_np(b.mean), _np(a.mean)) <= 1e-11
+
+
+def test_loops_stop_on_nan(host_only, monkeypatch):
+    """The reference stops on NaN (convergence_criteria.py:6,
+    iterators.py:105-106): a filter/smoother that returns a NaN objective on
+    its second call ends the solve loop and the QPM loop there, and the NaN
+    reaches info."""
+    calls = []
+
+    def poisoned(x0, dtm, dom):
+        calls.append(1)
+        out, nll, obj, ssq = oracle_filtsmooth(x0, dtm, dom)
+        if len(calls) >= 2:
+            obj = torch.tensor(float("nan"), dtype=torch.float64)
+        return out, nll, obj, ssq
+
+    monkeypatch.setattr(pstep, "parallel_linear_filtsmooth", poisoned)
+    monkeypatch.setattr(pit, "fs", poisoned)
+    f, y0, _, t1 = user_field("vanderpol")
+    ts = np.linspace(0.0, t1, 50)
+    _, info = psolver.solve(f=f, y0=y0, ts=ts, order=2, init="constant")
+    assert int(info["iterations"]) == 2 and torch.isnan(info["obj"])
+    calls.clear()
+    it, _ = pit.qpm_ieks_iterator(f=f, y0=y0, ts=ts, order=2, init="constant")
+    assert len(list(it)) == 2
