@@ -85,6 +85,9 @@ enum {
   POF_FIELD_HENONHEILES = 10    /* (p)                pof/ivp.py:137-152 */
 };
 
+/* Text of a POF_* status; the last CUDA runtime error seen by libpof (for
+ * POF_ERR_CUDA); the library's interface version.  No reference
+ * counterpart (the reference raises Python exceptions). */
 const char* pof_status_string(int status);
 const char* pof_last_cuda_error(void);
 int pof_version(void);
@@ -92,6 +95,9 @@ int pof_version(void);
 /* 1 if the (D, d) pair is compiled into this build, else 0. */
 int pof_shape_supported(int32_t D, int32_t d);
 
+/* Bytes of the workspace of pof_linear_filtsmooth, pof_linear_noiseless_filtering
+ * and pof_smoothing (0 when n_steps < 1 or D < 1).  The reference needs none:
+ * XLA allocates the scan's intermediates (pof/parallel_filtsmooth/filter.py:35). */
 size_t pof_filtsmooth_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32_t d);
 
 /* pof.parallel_filtsmooth.linear_filtsmooth(x0, dtm, dom)
@@ -152,6 +158,7 @@ int pof_sequential_eks(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int
                        int64_t ft_stride, int32_t smooth, void* out_mean, void* out_chol, double* out_scalars,
                        void* stream);
 
+/* Bytes of the workspace of pof_ieks_solve (0 when n_steps < 1 or D < 1). */
 size_t pof_ieks_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32_t d);
 
 /* pof.solver.solve(f, y0, ts, order, init, calibrate, maxiters)
@@ -168,6 +175,7 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
                    void* chols, int64_t maxiters, int32_t calibrate, double* info, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* Bytes of the workspace of pof_ieks_solve_mixed (0 when n_steps < 1 or D < 1). */
 size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
 
 /* pof.solver.solve with precision="mixed".  Float32 iterations first: each
