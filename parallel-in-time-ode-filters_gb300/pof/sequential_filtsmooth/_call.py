@@ -36,9 +36,8 @@ def sequential(x0, dtm, dom=None, om=None, smooth=True, stream=None):
     else:
         field = getattr(om, "field", None)
         if field is None:
-            raise NotImplementedError(
-                "sequential EKF of a user vector field: libpof linearizes built-in fields inside the "
-                "sequential kernel; pass a field from pof.ivp (or use solve(sequential=True))")
+            raise ValueError("libpof's sequential EKF linearizes built-in fields only (pof.ivp); "
+                             "pof.sequential_filtsmooth.filtsmooth runs other fields step by step in torch")
         setup = om.setup
         fid, params = field_params(field, dtype, device)
         d = setup["iwp"].wiener_process_dimension

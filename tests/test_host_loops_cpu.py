@@ -201,3 +201,29 @@ def test_loops_stop_on_nan(host_only, monkeypatch):
     calls.clear()
     it, _ = pit.qpm_ieks_iterator(f=f, y0=y0, ts=ts, order=2, init="constant")
     assert len(list(it)) == 2
+
+
+def test_sequential_eks_of_a_user_field(host_only, monkeypatch):
+    """pof.solver.sequential_eks_solve for a plain torch field: the EKF
+    step by step in torch (filter.py:9-30, linearized at each predicted mean)
+    and the RTS smoother (here the oracle's in place of libpof's) give the
+    oracle's sequential EKS (solver.py:76-96)."""
+    import pof.parallel_filtsmooth as ppfs
+
+    def oracle_smoothing(dtm, filt):
+        (m, L), obj = ofs.sequential_smoothing((_np(dtm[0]), _np(dtm[1])), (_np(filt[0]), _np(filt[1])))
+        return MVNSqrt(torch.as_tensor(m.copy()), torch.as_tensor(L.copy())), torch.tensor(obj)
+
+    monkeypatch.setattr(ppfs, "smoothing", oracle_smoothing)
+    f, y0, o, t1 = user_field("vanderpol")
+    ts = np.linspace(0.0, t1, 60)
+    ys, info = psolver.sequential_eks_solve(f=f, y0=y0, ts=ts, order=3)
+    (om, oL), oinfo = osolver.sequential_eks_solve(o, ts, 3)
+    assert rel(_np(ys.mean), om) <= 1e-10
+    C, oC = _np(ys.chol @ ys.chol.transpose(-1, -2)), oL @ np.swapaxes(oL, -1, -2)
+    assert rel(C, oC) <= 1e-9
+    for k in ("nll", "obj", "sigma_squared"):
+        assert np.isclose(float(info[k]), oinfo[k], rtol=1e-9), k
+    full, _ = psolver.sequential_eks_solve(f=f, y0=y0, ts=ts, order=3, return_full_states=True)
+    (ofull, _), _ = osolver.sequential_eks_solve(o, ts, 3, return_full_states=True)
+    assert rel(_np(full.mean), ofull) <= 1e-10
