@@ -634,7 +634,7 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
     if (rel < rtol_f32) break;       // converged as far as float32 goes
     // non-shrinking changes count once the change is below `settle` (the
     // IEKS's first iterations from a crude initial trajectory are not
-    // monotone); 0 counts every one
+    // monotone); HUGE_VAL counts every one
     worse = (rel >= prev && best < settle) ? worse + 1 : (rel >= prev ? worse : 0);
     if (worse >= 3) break;           // float32 stopped helping
     prev = rel;
