@@ -1,9 +1,10 @@
 """Problem set-up, EK1 linearization, initial trajectories, convergence
 criterion and the IEKS loop, restated in NumPy float64 (test infrastructure).
 
-Restates ``pof/convenience.py``, ``pof/initialization.py``,
-``pof/observations.py``, ``pof/step.py``, ``pof/convergence_criteria.py`` and
-``pof/solver.py``, including the reference's quirks:
+Restates ``pof/convenience.py`` (both set-ups), ``pof/initialization.py``,
+``pof/observations.py``, ``pof/step.py``, ``pof/convergence_criteria.py``,
+``pof/solver.py`` and the IEKS, quadratic-penalty and Levenberg-Marquardt
+iterators of ``pof/iterators.py``, including the reference's quirks:
 
 * double calibration of the returned chol (``step.py:42-44`` and
   ``solver.py:66-69``);
