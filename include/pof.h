@@ -6,7 +6,7 @@
  * is a JAX library with no FFI of its own; its hot path is a set of Python
  * functions over JAX arrays.  Each entry point below replaces one of those
  * functions and keeps its argument meaning; a JAX-FFI or ctypes binding
- * passes device pointers straight through (see INTEGRATION.md).
+ * passes device pointers straight through.
  *
  * Conventions
  *  - All array arguments are DEVICE pointers, row-major, C-contiguous, of the
@@ -61,13 +61,28 @@ enum {
   POF_S_COUNT = 8
 };
 
-/* Layout of the `info` block written by pof_ieks_solve (device doubles). */
+/* Layout of the `info` block written by pof_ieks_solve, per problem by the
+ * batched solves and by pof_server_fetch (device doubles). */
 enum {
   POF_I_ITERATIONS = 0,
   POF_I_NLL = 1,
   POF_I_OBJ = 2,
   POF_I_SSQ = 3,
-  POF_I_COUNT = 4
+  POF_I_STATUS = 4, /* POF_SOLVE_*: why the IEKS loop of this problem stopped */
+  POF_I_COUNT = 5
+};
+
+/* Per-problem outcome of an IEKS loop (info[POF_I_STATUS]).  The loop stops
+ * as the reference's does (pof/solver.py:36-45 with crit,
+ * pof/convergence_criteria.py:4-13: on NaN, on convergence, or after
+ * maxiters + 1 iterations); the status says which.  NaN and infinities stay
+ * in the outputs -- nothing traps.  No reference counterpart (the reference
+ * returns only the iteration count). */
+enum {
+  POF_SOLVE_CONVERGED = 0, /* crit held with finite objective and NLL */
+  POF_SOLVE_MAXITERS = 1,  /* stopped after maxiters + 1 iterations without crit */
+  POF_SOLVE_NONFINITE = 2, /* objective or NLL NaN or infinite (poisoned input, 0 pivot) */
+  POF_SOLVE_CANCELLED = 3  /* pof_server_cancel before it stopped */
 };
 
 /* Built-in vector fields for on-device EK1 linearization (pof/ivp.py). */
@@ -169,11 +184,34 @@ size_t pof_ieks_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32
  *        F = QL-pair of the preconditioned IWP prior (constant, (D, D)).
  *   out: means (N, D), chols (N, D, D) -- the final states, calibrated twice
  *        when `calibrate` (solver.py:66-69); info[POF_I_*].
- * The call waits on `stream` once per iteration to read the loop condition. */
+ * The loop runs as one CUDA graph with a while node (one iteration per pass
+ * of its body, the loop condition set on the device), enqueued on `stream`
+ * without waiting; the instantiated graph is kept for the next call with
+ * the same arguments (per host thread).  With libpof's event profiler on,
+ * POF_SOLVE_NO_GRAPH set, or maxiters above 100000 the iterations are
+ * launched from the host instead, which waits on `stream` once per
+ * iteration to read the loop condition. */
 int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field, const void* params,
                    double h, const void* x0_mean, const void* x0_chol, const void* F, const void* QL, void* means,
                    void* chols, int64_t maxiters, int32_t calibrate, double* info, void* workspace,
                    size_t workspace_bytes, void* stream);
+
+/* Bytes of the workspace of pof_ieks_solve_sequential (0 when n_steps < 1 or D < 1). */
+size_t pof_ieks_sequential_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32_t d);
+
+/* pof.solver.solve(..., sequential=True) for a built-in field
+ *   (pof/solver.py:11-73 with pof/step.py:37-40 dispatching to
+ *   pof/sequential_filtsmooth/__init__.py:13-16): the IEKS loop of
+ * pof_ieks_solve with the sequential square-root Kalman filter
+ * (sequential_filtsmooth/filter.py:33-92) and RTS smoother (smoother.py:8-48)
+ * in place of the parallel scans -- the same team kernels as the parallel
+ * path's level 0, run over one chunk that spans the trajectory.  Arguments,
+ * outputs and info as in pof_ieks_solve (nll with the parallel filter's
+ * sign).  The loop is enqueued as pof_ieks_solve's is. */
+int pof_ieks_solve_sequential(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field,
+                              const void* params, double h, const void* x0_mean, const void* x0_chol, const void* F,
+                              const void* QL, void* means, void* chols, int64_t maxiters, int32_t calibrate,
+                              double* info, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Bytes of the workspace of pof_ieks_solve_mixed (0 when n_steps < 1 or D < 1). */
 size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
@@ -200,7 +238,8 @@ size_t pof_ieks_mixed_workspace_bytes(int64_t n_steps, int32_t D, int32_t d);
  * in pof_ieks_solve; info has POF_I_COUNT + 2 entries: [POF_I_COUNT] the
  * number of kept float32 iterations (POF_I_ITERATIONS counts the float64
  * ones), [POF_I_COUNT + 1] the smallest relative change the float32 phase
- * reached.  Waits on `stream` once per iteration. */
+ * reached.  Waits on `stream` once per float32 iteration; the float64
+ * loop is enqueued as pof_ieks_solve's is. */
 int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, const double* params, double h,
                          const double* x0_mean, const double* x0_chol, const double* F, const double* QL,
                          double* means, double* chols, int64_t maxiters_f32, double rtol_f32, double settle_f32,
@@ -220,10 +259,15 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
  *  - Scratch is a fixed 16 MiB device array inside libpof, held by every GPU
  *    that loads the library until the process exits.  Problems whose
  *    pof_filtsmooth_workspace_bytes exceeds POF_NOALLOC_SCRATCH_BYTES are
- *    refused with POF_ERR_WORKSPACE before any GPU work (about 13k steps at
- *    D = 8, d = 2 in float64).
+ *    refused with POF_ERR_WORKSPACE before any GPU work.  The largest
+ *    n_steps that fit, float64 (float32): D = 3: 34212 (100400); D = 4:
+ *    20296 (40112); D = 5: 13408 (26618); D = 6: 5778 (11482); D = 8: 3344
+ *    (6660); D = 9: 2664 (5316); D = 10: 2176 (4341).  Bad dtypes, shapes
+ *    and sizes get pof_linear_filtsmooth's statuses first.
  *  - The first call on a device looks up the array's address on that device
  *    (the current device); make that first call before any stream capture.
+ *    The address is kept until the process exits: resetting the device
+ *    (cudaDeviceReset) after that first call is not supported.
  *  - Every call shares the array: calls whose work overlaps on the GPU
  *    (other streams, other host threads) race and must be serialized by the
  *    caller.  Nothing needs clearing between calls.
@@ -339,6 +383,13 @@ int64_t pof_server_submit(pof_server* s, int64_t n_steps, int32_t field, const d
 int pof_server_launch(pof_server* s, int64_t iterations);
 int pof_server_sync(pof_server* s, int64_t* n_running);
 int pof_server_step(pof_server* s, int64_t iterations, int64_t* n_running);
+/* Host-set cancel flag of an admitted request: the engine reads it at each
+ * of its ticks (mapped host memory, no CUDA call here), so a request stops
+ * at the first tick that runs after this call -- also one enqueued earlier
+ * by pof_server_launch -- and finishes with info[POF_I_STATUS] =
+ * POF_SOLVE_CANCELLED and its last iterate.  Fetch it like any finished
+ * request.  POF_ERR_ARG for a free or finished slot. */
+int pof_server_cancel(pof_server* s, int64_t slot);
 /* Up to cap slots that finished since the last poll. */
 int64_t pof_server_poll(pof_server* s, int64_t* slots_out, int64_t cap);
 /* Copy a finished request's result -- means (N, D), calibrated chols

@@ -146,6 +146,7 @@ struct BatchCtx {
     v.fld = reinterpret_cast<const int32_t*>(w + P.fld);
     v.rtol = nullptr;
     v.maxit = nullptr;
+    v.cancel = nullptr;
     v.p01 = reinterpret_cast<const double*>(w + P.p01);
     v.frozen = a.frozen;
     v.ap = reinterpret_cast<const int32_t*>(lw + L.ap);

@@ -24,6 +24,7 @@ struct BView {
   const int32_t* cp;      // (n1)
   const double* rtol;     // (B) objective rtol of crit per problem, or null (a shared value)
   const int64_t* maxit;   // (B) maxiters per problem, or null (a shared value)
+  const volatile int32_t* cancel;  // (B) host-set cancel flags (mapped host memory), or null
   int64_t n;              // grid points of the index space (SoA stride of the smoother elements)
   int64_t n1;             // level-0 chunks
   int64_t Ba;             // problems of the plan
@@ -462,10 +463,12 @@ static __global__ void kb_control(BView v, const double* __restrict__ partials, 
   else
     objc = (oo == obj);
   const bool conv = nan || objc || nc == 0.0;
-  const bool cont = !conv && it <= (double)maxiters;
+  const bool cancelled = v.cancel && v.cancel[b] != 0;
+  const bool cont = !conv && it <= (double)maxiters && !cancelled;
   sc[S_OBJ_OLD] = obj;
   sc[S_NLL_OLD] = nll;
   sc[S_CONT] = cont ? 1.0 : 0.0;
+  sc[S_STATUS] = (cancelled && !conv) ? (double)POF_SOLVE_CANCELLED : stop_status(conv, obj, nll);
   if (cont)
     atomicAdd(nactive, 1);
   else
@@ -492,10 +495,12 @@ __global__ void kb_finish(const int64_t* __restrict__ gb, const int64_t* __restr
     for (int64_t i = g0 * D * D + threadIdx.x; i < g1 * D * D; i += blockDim.x) chols[i] *= s;
   }
   if (info && threadIdx.x == 0) {
-    info[4 * b + 0] = sc[S_ITER];
-    info[4 * b + 1] = sc[S_NLL];
-    info[4 * b + 2] = sc[S_OBJ];
-    info[4 * b + 3] = sc[S_SSQ];
+    double* o = info + (int64_t)POF_I_COUNT * b;
+    o[POF_I_ITERATIONS] = sc[S_ITER];
+    o[POF_I_NLL] = sc[S_NLL];
+    o[POF_I_OBJ] = sc[S_OBJ];
+    o[POF_I_SSQ] = sc[S_SSQ];
+    o[POF_I_STATUS] = sc[S_STATUS];
   }
 }
 

@@ -43,7 +43,7 @@ namespace {
 
 const Ops* find_ops(int dtype, int D, int DY) {
   if (dtype != POF_F64 && dtype != POF_F32) return nullptr;
-  if (DY < 1 || D % DY != 0) return nullptr;
+  if (DY < 1 || D < 1) return nullptr;
   return find_shape(dtype, D, DY);
 }
 
@@ -63,12 +63,21 @@ int env_int(const char* name, int dflt = 0) {
 
 Plan plan_for(int dtype, int64_t n, int D, int DY, bool solver) {
   return make_plan(n, D, DY, esz(dtype), solver, env_int("POF_C0"), env_int("POF_CG"),
-                   env_int("POF_TEAM_WIDE_L0") != 0, env_int("POF_KS", 0));
+                   env_int("POF_TEAM_WIDE_L0") != 0, env_int("POF_KS", 0), env_int("POF_L0_TEAM", 0));
+}
+
+// The sequential filter/smoother as a plan: one level-0 chunk spanning all
+// n steps, so one team runs the square-root Kalman filter and the RTS
+// smoother step after step (the level-0 kernels' recursion, from x0 and
+// from the terminal state), nothing above it.
+Plan sequential_plan(int dtype, int64_t n, int D, int DY) {
+  const int C0 = n < (int64_t)0x7fffffff ? (int)n : 0x7fffffff;
+  return make_plan(n, D, DY, esz(dtype), true, C0, 0, false, 0);
 }
 
 int check_common(int dtype, int64_t n, int D, int DY, const Ops** ops) {
   if (dtype != POF_F64 && dtype != POF_F32) return POF_ERR_DTYPE;
-  if (n < 1 || D < 1 || DY < 1 || DY > D) return POF_ERR_ARG;
+  if (n < 1 || D < 1 || DY < 1) return POF_ERR_ARG;
   *ops = find_ops(dtype, D, DY);
   if (!*ops) return POF_ERR_SHAPE;
   return POF_OK;
@@ -215,7 +224,7 @@ const char* pof_status_string(int status) {
 
 const char* pof_last_cuda_error(void) { return g_cuda_error.c_str(); }
 
-int pof_version(void) { return 1; }
+int pof_version(void) { return 2; }
 
 int pof_shape_supported(int32_t D, int32_t d) { return find_ops(POF_F64, D, d) != nullptr ? 1 : 0; }
 
@@ -397,10 +406,131 @@ struct Loop {
   double rtol, atol;  // objective test of crit
 };
 
-// The IEKS loop of pof/solver.py:36-57 on the device (one host read of the
-// loop condition per iteration).  Leaves the result in l.means and the
-// scalars (nll, obj, ssq, iterations) in the plan's scalar block.
+// The IEKS loop as one CUDA graph: a while node whose body is one iteration
+// -- linearize at the iterate in l.means, filter and smooth into the second
+// buffer, loop control (k_ieks_control_graph sets the while condition),
+// copy the new iterate back into l.means -- so the whole loop runs on the
+// device without a host round trip per iteration.  The instantiated graph
+// is kept for the next call with the same arguments (one per host thread).
+struct GraphLoopKey {
+  const Ops* ops;
+  int64_t n, maxiters;
+  int D, DY, C0, Cg, nlev, field, dev;
+  bool ks, calibrate;
+  const void *params, *x0m, *x0L, *F, *QL, *means, *chols;
+  char* w;
+  double p0, p1, rtol, atol;
+  bool same(const GraphLoopKey& o) const {
+    return ops == o.ops && n == o.n && maxiters == o.maxiters && D == o.D && DY == o.DY && C0 == o.C0 &&
+           Cg == o.Cg && nlev == o.nlev && field == o.field && dev == o.dev && ks == o.ks &&
+           calibrate == o.calibrate && params == o.params && x0m == o.x0m && x0L == o.x0L && F == o.F &&
+           QL == o.QL && means == o.means && chols == o.chols && w == o.w && p0 == o.p0 && p1 == o.p1 &&
+           rtol == o.rtol && atol == o.atol;
+  }
+};
+
+// No destructor: an instantiated graph kept at process exit is released
+// with the context (a CUDA call during static destruction may find the
+// runtime gone).
+struct GraphLoopCache {
+  bool valid = false;
+  GraphLoopKey key{};
+  cudaGraphExec_t exec = nullptr;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    valid = false;
+  }
+};
+thread_local GraphLoopCache g_loop_graph;
+
+// The graph's while loop ends by itself after maxiters + 1 iterations at the
+// latest; loops allowed more than kGraphMaxIters iterations are launched from
+// the host instead, so a process can always be interrupted between launches.
+constexpr int64_t kGraphMaxIters = 100000;
+
+bool loop_graphs_on(int64_t maxiters) {
+  return !g_prof.on && env_int("POF_SOLVE_NO_GRAPH") == 0 && maxiters <= kGraphMaxIters;
+}
+
+int build_loop_graph(const Loop& l, cudaStream_t st, cudaGraphExec_t* out) {
+  const Plan& p = *l.p;
+  char* w = l.w;
+  double* scal = reinterpret_cast<double*>(w + p.scalars);
+  void* Hb = w + p.H;
+  void* cb = w + p.c;
+  void* mnew = w + p.means2;
+  StepModel sm{l.F, l.QL, 0, Hb, cb, nullptr, 0};
+  cudaGraph_t g = nullptr;
+  int rc = cuda_status(cudaGraphCreate(&g, 0));
+  if (rc) return rc;
+  cudaGraphConditionalHandle handle;
+  rc = cuda_status(cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (!rc) rc = cuda_status(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+  if (!rc) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    // a private stream for the capture, so nothing else of the caller's
+    // stream joins the body
+    cudaStream_t cs = nullptr;
+    rc = cuda_status(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    if (!rc) rc = cuda_status(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal));
+    if (!rc) {
+      l.ops->linearize(p.n, l.field, l.params, l.p0, l.p1, l.means, Hb, cb, cs);
+      l.ops->filter(p, w, sm, l.x0m, l.x0L, mnew, l.chols, cs);
+      l.ops->smoother(p, w, l.F, l.QL, 0, mnew, l.chols, l.calibrate, l.means, cs);
+      k_ieks_control_graph<<<1, 32, 0, cs>>>(scal, l.maxiters, l.rtol, l.atol, handle);
+      cudaMemcpyAsync(l.means, mnew, l.esz * p.D * (p.n + 1), cudaMemcpyDeviceToDevice, cs);
+      cudaGraph_t captured = nullptr;
+      const int rc2 = cuda_status(cudaStreamEndCapture(cs, &captured));
+      rc = launch_status();
+      if (!rc) rc = rc2;
+    }
+    if (cs) cudaStreamDestroy(cs);
+  }
+  if (!rc) rc = cuda_status(cudaGraphInstantiate(out, g, 0));
+  cudaGraphDestroy(g);
+  (void)st;
+  return rc;
+}
+
+int ieks_loop_graph(const Loop& l, cudaStream_t st) {
+  const Plan& p = *l.p;
+  int dev = 0;
+  int rc = cuda_status(cudaGetDevice(&dev));
+  if (rc) return rc;
+  GraphLoopKey key{l.ops, p.n, l.maxiters, p.D, p.DY, p.C0, p.Cg, p.nlev, l.field, dev, p.ks, l.calibrate,
+                   l.params, l.x0m, l.x0L, l.F, l.QL, l.means, l.chols, l.w, l.p0, l.p1, l.rtol, l.atol};
+  GraphLoopCache& c = g_loop_graph;
+  if (!(c.valid && c.key.same(key))) {
+    c.reset();
+    rc = build_loop_graph(l, st, &c.exec);
+    if (rc) {
+      c.reset();
+      return rc;
+    }
+    c.key = key;
+    c.valid = true;
+  }
+  k_init_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(l.w + p.scalars));
+  rc = launch_status();
+  if (!rc) rc = cuda_status(cudaGraphLaunch(c.exec, st));
+  return rc;
+}
+
+// The IEKS loop of pof/solver.py:36-57 on the device: as one CUDA graph
+// (ieks_loop_graph), or -- with the event profiler on, or POF_SOLVE_NO_GRAPH
+// set -- launched from the host with one read of the loop condition per
+// iteration.  Leaves the result in l.means and the scalars (nll, obj, ssq,
+// iterations, status) in the plan's scalar block.
 int ieks_loop(const Loop& l, cudaStream_t st) {
+  if (loop_graphs_on(l.maxiters)) return ieks_loop_graph(l, st);
   const Plan& p = *l.p;
   char* w = l.w;
   double* scal = reinterpret_cast<double*>(w + p.scalars);
@@ -533,6 +663,37 @@ int pof_ieks_solve(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t
   if (!params || !x0_mean || !x0_chol || !F || !QL || !means || !chols || !workspace || maxiters < 0)
     return POF_ERR_ARG;
   Plan p = plan_for(dtype, n_steps, D, d, true);
+  if (workspace_bytes < p.total) return POF_ERR_WORKSPACE;
+  double p0, p1;
+  rc = nordsieck_p01(D, d, h, &p0, &p1);
+  if (rc) return rc;
+  char* w = aligned_ws(workspace);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  Loop l{ops, &p, w, field, params, p0, p1, x0_mean, x0_chol, F, QL, means, chols, (size_t)esz(dtype),
+         maxiters, calibrate != 0, 1e-6, 1e-9};
+  rc = ieks_loop(l, st);
+  if (rc) return rc;
+  if (calibrate) ops->scale_inplace(chols, (int64_t)D * D * (n_steps + 1), w + p.scale, st);
+  if (info) k_copy_scalars<<<1, 32, 0, st>>>(reinterpret_cast<double*>(w + p.scalars), info, 1);
+  return launch_status();
+}
+
+size_t pof_ieks_sequential_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32_t d) {
+  if (n_steps < 1 || D < 1) return 0;
+  return sequential_plan(dtype, n_steps, D, d).total;
+}
+
+int pof_ieks_solve_sequential(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field,
+                              const void* params, double h, const void* x0_mean, const void* x0_chol, const void* F,
+                              const void* QL, void* means, void* chols, int64_t maxiters, int32_t calibrate,
+                              double* info, void* workspace, size_t workspace_bytes, void* stream) {
+  const Ops* ops = nullptr;
+  int rc = check_common(dtype, n_steps, D, d, &ops);
+  if (rc) return rc;
+  if (field <= 0 || field >= FIELD_COUNT || field_dim(field) != d) return POF_ERR_FIELD;
+  if (!params || !x0_mean || !x0_chol || !F || !QL || !means || !chols || !workspace || maxiters < 0)
+    return POF_ERR_ARG;
+  Plan p = sequential_plan(dtype, n_steps, D, d);
   if (workspace_bytes < p.total) return POF_ERR_WORKSPACE;
   double p0, p1;
   rc = nordsieck_p01(D, d, h, &p0, &p1);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "../../include/pof.h"
 #include "pof_kernels.cuh"
 #include "pof_team_kernels.cuh"
 #include "pof_plan.h"
@@ -14,8 +15,16 @@ namespace pof {
 
 enum Scalar : int {
   S_NLL = 0, S_OBJ = 1, S_SSQ = 2, S_FOBJ = 3, S_NOTCLOSE = 4,
-  S_OBJ_OLD = 5, S_NLL_OLD = 6, S_ITER = 7, S_CONT = 8, S_COUNT = 16
+  S_OBJ_OLD = 5, S_NLL_OLD = 6, S_ITER = 7, S_CONT = 8, S_STATUS = 9, S_COUNT = 16
 };
+
+// Why a loop that stops now stops (POF_SOLVE_*): the reference's stopping
+// rule is unchanged, this only labels it.  Infinite values stop the
+// reference's loop through isclose(inf, inf), so they are reported with NaN.
+__device__ __forceinline__ double stop_status(bool conv, double obj, double nll) {
+  if (!isfinite(obj) || !isfinite(nll)) return (double)POF_SOLVE_NONFINITE;
+  return conv ? (double)POF_SOLVE_CONVERGED : (double)POF_SOLVE_MAXITERS;
+}
 
 template <typename T>
 __global__ void k_finalize_filter(const double* __restrict__ partials, int64_t n1, int64_t n, int DY,
@@ -46,8 +55,8 @@ static __global__ void k_finalize_smoother(const double* __restrict__ partials, 
 // isclose(obj_old, obj, rtol, atol) or when every mean is
 // isclose(old, new, mrtol, matol); the reference's values are rtol = 1e-6,
 // atol = 1e-9, mrtol = 1e-13, matol = 1e-8.
-static __global__ void k_ieks_control(double* __restrict__ scalars, int64_t maxiters, double rtol, double atol) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ bool ieks_control(double* __restrict__ scalars, int64_t maxiters, double rtol,
+                                             double atol) {
   const double k = scalars[S_ITER] + 1.0;
   scalars[S_ITER] = k;
   const double obj = scalars[S_OBJ], nll = scalars[S_NLL];
@@ -62,8 +71,26 @@ static __global__ void k_ieks_control(double* __restrict__ scalars, int64_t maxi
   const bool conv = nan || objc || meansc;
   const bool cont = (k < 1.0) || (!conv && k <= (double)maxiters);
   scalars[S_CONT] = cont ? 1.0 : 0.0;
+  scalars[S_STATUS] = stop_status(conv, obj, nll);
   scalars[S_OBJ_OLD] = obj;
   scalars[S_NLL_OLD] = nll;
+  return cont;
+}
+
+static __global__ void k_ieks_control(double* __restrict__ scalars, int64_t maxiters, double rtol, double atol) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  ieks_control(scalars, maxiters, rtol, atol);
+}
+
+// The same control as the last node of the body of a CUDA graph's while
+// loop: the loop goes on while the handle is non-zero.  Every iteration adds
+// one to the iteration count and the loop stops once it exceeds maxiters + 1
+// at the latest, so the while loop ends.
+static __global__ void k_ieks_control_graph(double* __restrict__ scalars, int64_t maxiters, double rtol,
+                                            double atol, cudaGraphConditionalHandle handle) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const bool cont = ieks_control(scalars, maxiters, rtol, atol);
+  cudaGraphSetConditional(handle, cont ? 1u : 0u);
 }
 
 static __global__ void k_init_scalars(double* __restrict__ scalars) {
@@ -85,10 +112,11 @@ static __global__ void k_copy_scalars(const double* __restrict__ src, double* __
     dst[3] = src[S_FOBJ];
     dst[4] = src[S_NOTCLOSE];
   } else {  // info of the solver
-    dst[0] = src[S_ITER];
-    dst[1] = src[S_NLL];
-    dst[2] = src[S_OBJ];
-    dst[3] = src[S_SSQ];
+    dst[POF_I_ITERATIONS] = src[S_ITER];
+    dst[POF_I_NLL] = src[S_NLL];
+    dst[POF_I_OBJ] = src[S_OBJ];
+    dst[POF_I_SSQ] = src[S_SSQ];
+    dst[POF_I_STATUS] = src[S_STATUS];
   }
 }
 
@@ -127,6 +155,10 @@ struct Driver {
   static constexpr int TSW = TeamSize<D>::v;                     // wide teams
   static constexpr int TSN = TSW / 2 >= 4 ? TSW / 2 : 4;          // narrow teams
   static constexpr int TSX = TSW < 32 ? 2 * TSW : 32;             // widest teams (latency-bound levels)
+  // quarter teams (4 lanes) at level 0, D = 8 only (tuning: POF_L0_TEAM=4):
+  // one warp instruction serves twice as many chunks' one-lane reflector
+  // chains, each lane updates twice as many rows
+  static constexpr int TSQ = (D == 8 && TSN > 4) ? 4 : TSN;
   static constexpr bool kTeamL0 = D >= 6;  // pof_plan.h l0_lanes
   using FWS = FiltTeamWs<T, D>;
   using SWS = SmoTeamWs<T, D>;
@@ -142,14 +174,18 @@ struct Driver {
 
   static void filter(const Plan& p, char* ws, const StepModel& sm, const T* x0m, const T* x0L, T* means, T* chols,
                      cudaStream_t st) {
-    if (p.team == TSN && TSN != TSW)
+    if (p.team == TSQ && TSQ != TSN)
+      filter_ts<TSQ, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
+    else if (p.team == TSN && TSN != TSW)
       filter_ts<TSN, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
     else
       filter_ts<TSW, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
   }
   static void smoother(const Plan& p, char* ws, const T* F, const T* QL, int64_t ft_stride, T* means, T* chols,
                        bool calibrate, const T* means_old, cudaStream_t st) {
-    if (p.team == TSN && TSN != TSW)
+    if (p.team == TSQ && TSQ != TSN)
+      smoother_ts<TSQ, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);
+    else if (p.team == TSN && TSN != TSW)
       smoother_ts<TSN, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);
     else
       smoother_ts<TSW, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);
@@ -172,7 +208,10 @@ struct Driver {
     Bufs b{ws, &p};
     const int64_t n = p.n;
     const int64_t n1 = p.cnt[1];
-    {
+    // One chunk (a plan whose level 0 spans the trajectory: the sequential
+    // filter): its start state is x0, which the top writes without reading
+    // any element, so the chunk's element is not built.
+    if (n1 > 1 || p.ks) {
       ProfScope ps(PK_FILT_L0_REDUCE, st);
       if constexpr (kTeamL0) {
         if (sm.ft_stride)
@@ -257,7 +296,9 @@ struct Driver {
     Bufs b{ws, &p};
     const int64_t n = p.n;
     const int64_t n1 = p.cnt[1];
-    {
+    // one chunk: its end state is the terminal state, written by the top
+    // without reading the chunk's composite, which is therefore not built
+    if (n1 > 1 || p.ks) {
       ProfScope ps(PK_SMO_L0_REDUCE, st);
       if constexpr (kTeamL0)
         launch_team<SWS, TS>(k_smo_reduce_team<T, D, TS>, n1, st, (const T*)b.template at<T>(p.selem), n, p.C0,

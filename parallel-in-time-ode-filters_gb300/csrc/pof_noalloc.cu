@@ -30,6 +30,9 @@ void* g_ptr[kMaxDevices] = {nullptr};
 
 // Device address of the scratch array on the current device, looked up once
 // per device (the lookup also makes the runtime load the module there).
+// The address is kept for the life of the process, so resetting a device
+// (cudaDeviceReset) after the first call on it is not supported: the module
+// and its array are gone and the kept address is stale.
 int scratch_address(void** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -53,7 +56,13 @@ extern "C" int pof_linear_filtsmooth_noalloc(int32_t dtype, int64_t n_steps, int
                                              const void* QL, int64_t ft_stride, const void* H, const void* c,
                                              const void* R, int64_t r_stride, void* out_mean, void* out_chol,
                                              double* out_scalars, void* stream) {
-  // Too large for the fixed scratch: refuse before touching the GPU.
+  // The argument checks of pof_linear_filtsmooth come first, in its order,
+  // so both entry points return the same status for the same bad inputs;
+  // then a problem too large for the fixed scratch is refused before
+  // touching the GPU.
+  if (dtype != POF_F64 && dtype != POF_F32) return POF_ERR_DTYPE;
+  if (n_steps < 1 || D < 1 || d < 1) return POF_ERR_ARG;
+  if (!pof_shape_supported(D, d)) return POF_ERR_SHAPE;
   const size_t need = pof_filtsmooth_workspace_bytes(dtype, n_steps, D, d);
   if (need == 0) return POF_ERR_ARG;
   if (need > (size_t)POF_NOALLOC_SCRATCH_BYTES) return POF_ERR_WORKSPACE;

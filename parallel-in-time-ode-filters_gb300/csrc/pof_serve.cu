@@ -90,7 +90,7 @@ __global__ void ks_admit(int32_t b, const AdmitBlock* __restrict__ blk, const do
 
 // A finished request's result: the latest iterate (buffer by the parity of
 // its iteration count), the calibrated chol (pof/solver.py:66-69) and
-// info = (iterations, nll, obj, sigma^2).
+// info = (iterations, nll, obj, sigma^2, status).
 __global__ void ks_fetch(int32_t b, int parity0, const int64_t* __restrict__ gb, const int64_t* __restrict__ ns,
                          const double* __restrict__ m0, const double* __restrict__ m1,
                          const double* __restrict__ chols, const double* __restrict__ pscal,
@@ -106,10 +106,11 @@ __global__ void ks_fetch(int32_t b, int parity0, const int64_t* __restrict__ gb,
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N * D * D; i += stride)
     out_L[i] = chols[g0 * D * D + i] * s;
   if (info && blockIdx.x == 0 && threadIdx.x == 0) {
-    info[0] = sc[S_ITER];
-    info[1] = sc[S_NLL];
-    info[2] = sc[S_OBJ];
-    info[3] = sc[S_SSQ];
+    info[POF_I_ITERATIONS] = sc[S_ITER];
+    info[POF_I_NLL] = sc[S_NLL];
+    info[POF_I_OBJ] = sc[S_OBJ];
+    info[POF_I_SSQ] = sc[S_SSQ];
+    info[POF_I_STATUS] = sc[S_STATUS];
   }
 }
 
@@ -143,6 +144,10 @@ struct pof_server {
   std::vector<int32_t> h_c0, h_frozen;
   Arena arena;
   void* bufs[2] = {nullptr, nullptr};
+  // Cancel flags, one per slot, in mapped pinned host memory: the host sets
+  // them (pof_server_cancel) and kb_control reads them at every tick.
+  volatile int32_t* h_cancel = nullptr;
+  int32_t* d_cancel = nullptr;
   int cur = 0;  // bufs[cur] holds the current iterates
   bool dirty = true;
   int64_t ticks = 0;
@@ -216,6 +221,17 @@ int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_po
   s->h_frozen.assign(max_requests, 1);
   s->arena.init(max_points);
   int rc = cuda_status(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+  if (!rc) {
+    void* hc = nullptr;
+    rc = cuda_status(cudaHostAlloc(&hc, sizeof(int32_t) * max_requests, cudaHostAllocMapped));
+    if (!rc) {
+      memset(hc, 0, sizeof(int32_t) * max_requests);
+      s->h_cancel = static_cast<volatile int32_t*>(hc);
+      void* dc = nullptr;
+      rc = cuda_status(cudaHostGetDevicePointer(&dc, hc, 0));
+      s->d_cancel = static_cast<int32_t*>(dc);
+    }
+  }
   const BatchPersist& P = s->P;
   char* w = s->w;
   if (!rc) rc = cuda_status(cudaMemsetAsync(w + P.frozen, 0xff, sizeof(int32_t) * max_requests, s->st));
@@ -225,6 +241,7 @@ int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_po
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s->st));
   if (rc) {
     if (s->st) cudaStreamDestroy(s->st);
+    if (s->h_cancel) cudaFreeHost(const_cast<int32_t*>(s->h_cancel));
     delete s;
     return rc;
   }
@@ -259,6 +276,7 @@ int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_po
   v.frozen = a.frozen;
   v.rtol = reinterpret_cast<const double*>(x + s->X.rtol);
   v.maxit = reinterpret_cast<const int64_t*>(x + s->X.maxit);
+  v.cancel = s->d_cancel;
   v.n = max_points;
   s->bufs[0] = x + s->X.means;
   s->bufs[1] = w + P.means2;
@@ -270,6 +288,7 @@ int pof_server_destroy(pof_server* s) {
   if (!s) return POF_ERR_ARG;
   cudaStreamSynchronize(s->st);
   cudaStreamDestroy(s->st);
+  if (s->h_cancel) cudaFreeHost(const_cast<int32_t*>(s->h_cancel));
   delete s;
   return POF_OK;
 }
@@ -350,6 +369,7 @@ int64_t pof_server_submit(pof_server* s, int64_t n_steps, int32_t field, const d
     return rc;
   }
   Slot& sl = s->slots[b];
+  s->h_cancel[b] = 0;  // no tick reads slot b's flag before the next re-plan
   sl.used = true;
   sl.finished = false;
   sl.g0 = g0;
@@ -402,6 +422,14 @@ int pof_server_step(pof_server* s, int64_t iterations, int64_t* n_running) {
   int rc = pof_server_launch(s, iterations);
   if (!rc) rc = pof_server_sync(s, n_running);
   return rc;
+}
+
+int pof_server_cancel(pof_server* s, int64_t slot) {
+  if (!s || slot < 0 || slot >= s->maxB) return POF_ERR_ARG;
+  const Slot& sl = s->slots[slot];
+  if (!sl.used || sl.finished) return POF_ERR_ARG;
+  s->h_cancel[slot] = 1;
+  return POF_OK;
 }
 
 int64_t pof_server_poll(pof_server* s, int64_t* slots_out, int64_t cap) {

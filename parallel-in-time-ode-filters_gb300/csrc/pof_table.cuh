@@ -41,8 +41,11 @@ struct OpsImpl {
   }
   static void linearize(int64_t n, int field, const void* params, double p0, double p1, const void* means, void* H,
                         void* c, cudaStream_t st) {
-    Driver<T, D, DY>::linearize(n, field, static_cast<const T*>(params), (T)p0, (T)p1,
-                                static_cast<const T*>(means), static_cast<T*>(H), static_cast<T*>(c), st);
+    // a field's EK1 model has d = D / (q + 1) rows; shapes with more rows
+    // than states exist for given (H, c, R) only and never get here
+    if constexpr (D % DY == 0)
+      Driver<T, D, DY>::linearize(n, field, static_cast<const T*>(params), (T)p0, (T)p1,
+                                  static_cast<const T*>(means), static_cast<T*>(H), static_cast<T*>(c), st);
   }
   static void scale_inplace(void* x, int64_t count, const void* scale, cudaStream_t st) {
     k_scale_inplace<T><<<grid_for(count, 256), 256, 0, st>>>(static_cast<T*>(x), count,

@@ -203,3 +203,24 @@ def reference_step_flops(D, d):
     Cs = 22 / 3 * D ** 3 + 2 * D ** 2
     O = 16 / 3 * D ** 3 + 2 * d * D ** 2 + tr(d, D + d) + 4 * D ** 2
     return Ef + 2 * Cf + Es + 2 * Cs + O
+
+
+def kernel_bytes(n, D, d, esz=8):
+    """Compulsory DRAM bytes of one launch of the level-0 kernels over a
+    problem of n steps (each input read once, each output written once, in
+    the workspace layout of csrc/pof_plan.h): the `algorithmic` traffic the
+    roofline compares ncu's dram bytes with."""
+    C0, cnt = plan_levels(n, D)
+    n1 = cnt[1]
+    elem = 3 * D * D + 2 * D  # filter element (A, b, U, eta, Z)
+    state = D + D * D  # (mean, chol)
+    selem = D + 2 * D * D  # smoother element (g, E, D)
+    return {
+        "linearize": esz * n * (D + d * D + d),
+        "filt_l0_reduce": esz * (n * (d * D + d) + n1 * elem),
+        # H, c in; chunk start states in; means, chols, smoother elements out
+        "filt_l0_down": esz * (n * (d * D + d + state + selem) + n1 * state),
+        "smo_l0_reduce": esz * (n * selem + n1 * selem),
+        # smoother elements, previous means in; chunk end states in; means, chols out
+        "smo_l0_down": esz * (n * (selem + D + state) + n1 * state),
+    }

@@ -19,8 +19,10 @@ POF_F64, POF_F32 = 0, 1
 S_NLL, S_OBJ, S_SSQ, S_FOBJ, S_NOTCLOSE = 0, 1, 2, 3, 4
 S_COUNT = 8
 # info layout (POF_I_*)
-I_ITERATIONS, I_NLL, I_OBJ, I_SSQ = 0, 1, 2, 3
-I_COUNT = 4
+I_ITERATIONS, I_NLL, I_OBJ, I_SSQ, I_STATUS = 0, 1, 2, 3, 4
+I_COUNT = 5
+# info[I_STATUS]: why a problem's IEKS loop stopped (POF_SOLVE_*)
+SOLVE_STATUS = {0: "converged", 1: "maxiters", 2: "nonfinite", 3: "cancelled"}
 
 FIELDS = {
     "user": 0,
@@ -79,6 +81,11 @@ _SIGS = {
         _c.c_int,
         [_i32, _i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _dp, _vp, _sz, _vp],
     ),
+    "pof_ieks_sequential_workspace_bytes": (_sz, [_i32, _i64, _i32, _i32]),
+    "pof_ieks_solve_sequential": (
+        _c.c_int,
+        [_i32, _i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _dp, _vp, _sz, _vp],
+    ),
     "pof_ieks_mixed_workspace_bytes": (_sz, [_i64, _i32, _i32]),
     "pof_ieks_solve_mixed": (
         _c.c_int,
@@ -102,6 +109,7 @@ _SIGS = {
     "pof_server_launch": (_c.c_int, [_vp, _i64]),
     "pof_server_sync": (_c.c_int, [_vp, _vp]),
     "pof_server_step": (_c.c_int, [_vp, _i64, _vp]),
+    "pof_server_cancel": (_c.c_int, [_vp, _i64]),
     "pof_server_poll": (_i64, [_vp, _vp, _i64]),
     "pof_server_fetch": (_c.c_int, [_vp, _i64, _vp, _vp, _dp]),
     "pof_server_stream": (_vp, [_vp]),
@@ -190,6 +198,12 @@ def stream_handle(stream=None):
 
 def workspace(nbytes, device):
     return torch.empty(int(nbytes), dtype=torch.uint8, device=device)
+
+
+def solve_status(code):
+    """Name of an info[I_STATUS] value ("converged", "maxiters", "nonfinite",
+    "cancelled")."""
+    return SOLVE_STATUS.get(int(code), "unknown")
 
 
 def shape_supported(D, d):

@@ -227,34 +227,145 @@ def run_batch(prep, means, chols, info, maxiters=10_000, calibrate=True, C0=0, C
     return workspace
 
 
-def autotune(prep, C0s=(8, 16, 32, 64, 128), Cgs=(2, 4), iterations=3, repeats=2):
-    """Chunk length C0 and group size Cg for a prepared batch, by timing: each
-    candidate runs `iterations` IEKS iterations of the whole batch (maxiters
-    caps the solve; the work per iteration is what differs between
-    candidates), best of `repeats`, CUDA events on the current stream.
-    Returns (C0, Cg, {(C0, Cg): ms}).  A problem's result depends on (C0, Cg)
-    only through rounding; pass the same values again to reproduce it."""
-    dev = prep["x0m"].device
-    means = torch.empty_like(prep["means0"])
-    G, D = means.shape
-    chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
-    info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
+class _TeamWidth:
+    """Level-0 team width of the batched kernels for the calls inside the
+    block (lanes per chunk: the narrow teams by default, the wide ones with
+    POF_BATCH_TEAM_WIDE=1, read by libpof at each call)."""
+
+    def __init__(self, wide):
+        self.wide = wide
+
+    def __enter__(self):
+        import os
+
+        self.old = os.environ.get("POF_BATCH_TEAM_WIDE")
+        if self.wide is not None:
+            os.environ["POF_BATCH_TEAM_WIDE"] = "1" if self.wide else "0"
+        return self
+
+    def __exit__(self, *a):
+        import os
+
+        if self.wide is None:
+            return
+        if self.old is None:
+            os.environ.pop("POF_BATCH_TEAM_WIDE", None)
+        else:
+            os.environ["POF_BATCH_TEAM_WIDE"] = self.old
+
+
+def autotune_key(prep, device=None):
+    """Cache key of a batch's tuning: the GPU, the state shape (D, d) and
+    the total step count to a factor of two."""
+    dev = device if device is not None else prep["x0m"].device
+    name = torch.cuda.get_device_name(dev) if torch.cuda.is_available() else "cpu"
+    steps = int(np.asarray(prep["n_steps"]).sum())
+    return "%s|D%d|d%d|steps2^%d" % (name, prep["D"], prep["d"], int(round(math.log2(max(steps, 1)))))
+
+
+def _cache_path(path=None):
+    import os
+
+    if path:
+        return path
+    env = os.environ.get("POF_AUTOTUNE_CACHE")
+    if env:
+        return env
+    return os.path.join(os.path.expanduser("~"), ".cache", "pof_gb300", "autotune.json")
+
+
+def load_tuning(prep, path=None):
+    """(C0, Cg, wide) cached for this batch's key, or None."""
+    import json
+    import os
+
+    p = _cache_path(path)
+    if not os.path.exists(p):
+        return None
+    try:
+        with open(p) as f:
+            entry = json.load(f).get(autotune_key(prep))
+    except (OSError, ValueError):
+        return None
+    if not entry:
+        return None
+    return int(entry["C0"]), int(entry["Cg"]), bool(entry["wide"])
+
+
+def store_tuning(prep, C0, Cg, wide, times=None, path=None):
+    """Write (C0, Cg, wide) under this batch's key (other keys are kept)."""
+    import json
+    import os
+
+    p = _cache_path(path)
+    os.makedirs(os.path.dirname(p) or ".", exist_ok=True)
+    data = {}
+    if os.path.exists(p):
+        try:
+            with open(p) as f:
+                data = json.load(f)
+        except (OSError, ValueError):
+            data = {}
+    data[autotune_key(prep)] = {"C0": int(C0), "Cg": int(Cg), "wide": bool(wide),
+                                "ms": None if times is None else min(times.values())}
+    tmp = p + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, p)
+
+
+def autotune(prep, C0s=(8, 16, 32, 64, 128), Cgs=(2, 4), widths=(False, True), iterations=3, repeats=2,
+             timer=None):
+    """Chunk length C0, group size Cg and level-0 team width (narrow or wide
+    teams: lanes per chunk) for a prepared batch, by timing: each candidate
+    runs `iterations` IEKS iterations of the whole batch (maxiters caps the
+    solve; the work per iteration is what differs between candidates), best
+    of `repeats`, CUDA events on the current stream.  Returns
+    (C0, Cg, wide, {(C0, Cg, wide): ms}).  A problem's result depends on
+    these only through rounding; pass the same values again to reproduce it.
+    `timer(C0, Cg, wide)` (ms) replaces the measurement."""
     times = {}
-    ws = None
-    for C0 in C0s:
-        for Cg in Cgs:
+    if timer is None:
+        dev = prep["x0m"].device
+        means = torch.empty_like(prep["means0"])
+        G, D = means.shape
+        chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
+        info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
+        ws = [None]
+
+        def timer(C0, Cg, wide):
             best = float("inf")
-            for _ in range(repeats):
-                means.copy_(prep["means0"])
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                ws = run_batch(prep, means, chols, info, maxiters=iterations - 1, C0=C0, Cg=Cg, workspace=ws)
-                e1.record()
-                e1.synchronize()
-                best = min(best, e0.elapsed_time(e1))
-            times[(C0, Cg)] = best
-    C0, Cg = min(times, key=times.get)
-    return C0, Cg, times
+            with _TeamWidth(wide):
+                for _ in range(repeats):
+                    means.copy_(prep["means0"])
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    ws[0] = run_batch(prep, means, chols, info, maxiters=iterations - 1, C0=C0, Cg=Cg,
+                                      workspace=ws[0])
+                    e1.record()
+                    e1.synchronize()
+                    best = min(best, e0.elapsed_time(e1))
+            return best
+
+    for wide in widths:
+        for C0 in C0s:
+            for Cg in Cgs:
+                times[(C0, Cg, wide)] = timer(C0, Cg, wide)
+    C0, Cg, wide = min(times, key=times.get)
+    return C0, Cg, wide, times
+
+
+def tuned(prep, cache=True, path=None, **kwargs):
+    """(C0, Cg, wide) for a batch: from the autotune cache when it has the
+    batch's key (autotune_key), else by autotune, then stored (cache=True)."""
+    if cache:
+        hit = load_tuning(prep, path)
+        if hit is not None:
+            return hit
+    C0, Cg, wide, times = autotune(prep, **kwargs)
+    if cache:
+        store_tuning(prep, C0, Cg, wide, times, path)
+    return C0, Cg, wide
 
 
 def project(prep, means, chols):
@@ -273,24 +384,83 @@ def solve_batch(problems, order, init="constant", calibrate=True, maxiters=10_00
     parallel IEKS of pof.solver.solve (built-in fields, constant init).
     precision="mixed": float32 iterations first, float64 polish after, per
     problem (as pof.solver.solve's precision="mixed").  C0="auto" picks the
-    chunk length and group size by timing (autotune).  Returns a
+    chunk length, group size and level-0 team width by timing (autotune),
+    or from the autotune cache file (POF_AUTOTUNE_CACHE, default
+    ~/.cache/pof_gb300/autotune.json) for a batch of the same key.  Returns a
     BatchResult; ``result.problem(b)`` gives problem b's
     ((means (N_b, d), chol_covs (N_b, d, D)), info) as pof.solver.solve."""
     dev = default_device()
     prep = prepare_batch(problems, order, device=dev, init=init)
+    wide = None
     if C0 == "auto":
-        C0, Cg, _ = autotune(prep)
+        C0, Cg, wide = tuned(prep)
     means = prep["means0"].clone()
     G, D = means.shape
     chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
     info = torch.zeros((prep["B"], _lib.I_COUNT), dtype=torch.float64, device=dev)
     info32 = torch.zeros((prep["B"], 2), dtype=torch.float64, device=dev) if precision == "mixed" else None
-    run_batch(prep, means, chols, info, maxiters=maxiters, calibrate=calibrate, C0=C0, Cg=Cg, precision=precision,
-              maxiters_f32=maxiters_f32, rtol_f32=rtol_f32, info_f32=info32, settle_f32=settle_f32)
+    with _TeamWidth(wide):
+        run_batch(prep, means, chols, info, maxiters=maxiters, calibrate=calibrate, C0=C0, Cg=Cg,
+                  precision=precision, maxiters_f32=maxiters_f32, rtol_f32=rtol_f32, info_f32=info32,
+                  settle_f32=settle_f32)
     ym, yc = project(prep, means, chols)
     info_d = {"iterations": info[:, _lib.I_ITERATIONS].to(torch.int64), "nll": info[:, _lib.I_NLL],
-              "obj": info[:, _lib.I_OBJ], "sigma_squared": info[:, _lib.I_SSQ], "calibrated": bool(calibrate)}
+              "obj": info[:, _lib.I_OBJ], "sigma_squared": info[:, _lib.I_SSQ],
+              "status": info[:, _lib.I_STATUS].to(torch.int64), "calibrated": bool(calibrate)}
     if info32 is not None:
         info_d["iterations_float32"] = info32[:, 0].to(torch.int64)
         info_d["best_change_float32"] = info32[:, 1]
     return BatchResult(ym, yc, prep["offsets"], info_d)
+
+
+def shard(n_steps, world):
+    """Split a batch across `world` ranks by work: problems are taken
+    longest first and each goes to the rank holding the fewest steps so far
+    (ties: the lower rank).  Returns one sorted index array per rank.  The
+    partition depends only on the step counts, so every rank computes the
+    same one without talking to the others."""
+    n_steps = np.asarray(n_steps, dtype=np.int64)
+    load = np.zeros(world, dtype=np.int64)
+    parts = [[] for _ in range(world)]
+    for b in np.argsort(-n_steps, kind="stable"):
+        r = int(np.argmin(load))
+        parts[r].append(int(b))
+        load[r] += int(n_steps[b])
+    return [np.array(sorted(p), dtype=np.int64) for p in parts]
+
+
+def solve_batch_sharded(problems, order, rank, world, group=None, solver=None, **kwargs):
+    """solve_batch of one fixed batch split over the ranks of a
+    torch.distributed process group: rank `rank` solves its share
+    (pof.batch.shard), then the per-problem results are all-gathered (one
+    collective after the solve; the solve itself exchanges nothing) and every
+    rank returns the whole batch's BatchResult on the host, in the original
+    problem order.  A problem's result depends only on its own inputs, so it
+    is the one a single-rank solve gives.  `solver(problems, order,
+    **kwargs)` replaces solve_batch (it must return a BatchResult)."""
+    import torch.distributed as dist
+
+    solver = solver or solve_batch
+    n_steps = [len(p[3]) - 1 for p in problems]
+    mine = shard(n_steps, world)[rank]
+    local = []
+    if len(mine):
+        res = solver([problems[b] for b in mine], order, **kwargs)
+        for i, b in enumerate(mine):
+            (m, L), info = res.problem(i)
+            info = {k: (v.detach().cpu() if torch.is_tensor(v) else v) for k, v in info.items()}
+            local.append((int(b), m.detach().cpu(), L.detach().cpu(), info))
+    gathered = [None] * world
+    dist.all_gather_object(gathered, local, group=group)
+    per = {}
+    for part in gathered:
+        for b, m, L, info in part:
+            per[b] = (m, L, info)
+    order_b = range(len(problems))
+    mean = torch.cat([per[b][0] for b in order_b])
+    chol = torch.cat([per[b][1] for b in order_b])
+    offsets = np.concatenate([[0], np.cumsum([per[b][0].shape[0] for b in order_b])]).astype(np.int64)
+    keys = [k for k in per[0][2] if k != "calibrated"]
+    info = {k: torch.stack([torch.as_tensor(per[b][2][k]) for b in order_b]) for k in keys}
+    info["calibrated"] = per[0][2].get("calibrated", True)
+    return BatchResult(mean, chol, offsets, info)

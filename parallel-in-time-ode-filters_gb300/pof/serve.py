@@ -34,6 +34,7 @@ class Request(NamedTuple):
     order: int
     rtol: float
     maxiters: int
+    deadline: float = float("inf")  # perf_counter time after which the request is cancelled
 
 
 class Engine:
@@ -88,6 +89,17 @@ class Engine:
         self.slots[int(slot)] = (req, p0)
         return True
 
+    def cancel(self, rid):
+        """Set the engine's cancel flag of request rid (admitted, unfinished):
+        it stops at the engine's next tick with status "cancelled" and its
+        last iterate, and is collected by finished() like any other.  False
+        when rid is not in this engine."""
+        for slot, (req, _) in self.slots.items():
+            if req.rid == rid:
+                _lib.check(_lib.lib().pof_server_cancel(self.h, int(slot)), "pof_server_cancel")
+                return True
+        return False
+
     def launch(self, k=1):
         _lib.check(_lib.lib().pof_server_launch(self.h, int(k)), "pof_server_launch")
 
@@ -138,6 +150,7 @@ class Server:
         self.t_submit = {}
         self.t_done = {}
         self.prepared = {}
+        self.stop_reason = {}  # rid -> "cancelled" | "timeout" for requests stopped by the host
 
     def engine(self, d, q):
         key = (d, q)
@@ -145,13 +158,52 @@ class Server:
             self.engines[key] = Engine(d, q, self.max_requests, self.max_points, device=self.dev)
         return self.engines[key]
 
-    def submit(self, field, params, y0, ts, order, rtol=1e-6, maxiters=10_000, t_arrival=None):
+    def submit(self, field, params, y0, ts, order, rtol=1e-6, maxiters=10_000, t_arrival=None, timeout=None):
+        """Queue a request; returns its id.  timeout (seconds from arrival):
+        a request still unfinished then is cancelled -- taken out of the queue,
+        or stopped by its engine at the next tick -- and reported with status
+        "timeout"."""
         rid = self.next_rid
         self.next_rid += 1
+        t0 = time.perf_counter() if t_arrival is None else t_arrival
+        deadline = float("inf") if timeout is None else t0 + float(timeout)
         self.queue.append(Request(rid, field, tuple(float(p) for p in params), np.asarray(y0, dtype=np.float64),
-                                  np.asarray(ts, dtype=np.float64), int(order), float(rtol), int(maxiters)))
-        self.t_submit[rid] = time.perf_counter() if t_arrival is None else t_arrival
+                                  np.asarray(ts, dtype=np.float64), int(order), float(rtol), int(maxiters), deadline))
+        self.t_submit[rid] = t0
         return rid
+
+    def cancel(self, rid, reason="cancelled"):
+        """Stop request rid: a queued one leaves the queue at once (its
+        result is (None, info) with no iterations); an admitted one stops at
+        its engine's next tick with its last iterate.  Either way its status
+        is `reason`.  False when rid has already finished."""
+        if rid in self.results:
+            return False
+        for r in self.queue:
+            if r.rid == rid:
+                self.queue = deque(q for q in self.queue if q.rid != rid)
+                self.prepared.pop(rid, None)
+                info = torch.full((_lib.I_COUNT,), float("nan"), dtype=torch.float64)
+                info[_lib.I_ITERATIONS] = 0.0
+                info[_lib.I_STATUS] = 3.0  # POF_SOLVE_CANCELLED
+                self.results[rid] = (None, info)
+                self.t_done[rid] = time.perf_counter()
+                self.stop_reason[rid] = reason
+                return True
+        for e in self.engines.values():
+            if e.cancel(rid):
+                self.stop_reason[rid] = reason
+                return True
+        return False
+
+    def _expire(self):
+        """Cancel the requests whose deadline has passed (status "timeout")."""
+        now = time.perf_counter()
+        late = [r.rid for r in self.queue if r.deadline <= now]
+        for e in self.engines.values():
+            late += [req.rid for req, _ in e.slots.values() if req.deadline <= now and req.rid not in self.stop_reason]
+        for rid in late:
+            self.cancel(rid, reason="timeout")
 
     def _admit(self):
         """Prepare and admit queued requests in arrival order while engines take them."""
@@ -184,8 +236,10 @@ class Server:
         self.queue = kept
 
     def tick(self, k=1):
-        """Admit, run k iterations on every engine (overlapping), collect the
-        finished requests; returns their ids."""
+        """Cancel what is past its deadline, admit, run k iterations on every
+        engine (overlapping), collect the finished requests; returns their
+        ids."""
+        self._expire()
         self._admit()
         live = [e for e in self.engines.values() if e.slots]
         for e in live:
@@ -203,10 +257,18 @@ class Server:
         return bool(self.queue) or any(e.slots for e in self.engines.values())
 
     def result(self, rid):
-        """((means (N, d), chol_covs (N, d, D)), info) as pof.solver.solve returns."""
+        """((means (N, d), chol_covs (N, d, D)), info) as pof.solver.solve
+        returns, with info["status"] the request's outcome: "converged",
+        "maxiters", "nonfinite" (NaN or infinite objective: a poisoned input),
+        "cancelled" or "timeout".  A request cancelled before admission has
+        no result (None)."""
         ys, info = self.results[rid]
+        status = _lib.solve_status(float(info[_lib.I_STATUS]))
+        if status == "cancelled":
+            status = self.stop_reason.get(rid, status)
         return ys, {"iterations": info[_lib.I_ITERATIONS].to(torch.int64), "nll": info[_lib.I_NLL],
-                    "obj": info[_lib.I_OBJ], "sigma_squared": info[_lib.I_SSQ], "calibrated": True}
+                    "obj": info[_lib.I_OBJ], "sigma_squared": info[_lib.I_SSQ], "status": status,
+                    "calibrated": True}
 
     def close(self):
         for e in self.engines.values():

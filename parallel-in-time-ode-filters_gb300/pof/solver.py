@@ -11,11 +11,12 @@ from .utils import MVNSqrt, gmul_stack
 
 
 def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxiters_f32=10_000, rtol_f32=1e-5,
-                   settle_f32=float("inf")):
+                   settle_f32=float("inf"), sequential=False):
     """The whole IEKS loop in libpof (pof_ieks_solve): linearization, chunked
     filter/smoother, calibration and the convergence test all on the device.
     precision="mixed": float32 iterations first, float64 polish after
-    (pof_ieks_solve_mixed)."""
+    (pof_ieks_solve_mixed).  sequential: the sequential filter/smoother in
+    the loop (pof_ieks_solve_sequential)."""
     om = setup["om"]
     name, params = om.field
     x0 = setup["x0"]
@@ -43,18 +44,23 @@ def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxi
                                       _lib.ptr(info), _lib.ptr(ws), wsb, _lib.stream_handle())
         _lib.check(rc, "pof_ieks_solve_mixed")
     else:
-        wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+        wsq = lib.pof_ieks_sequential_workspace_bytes if sequential else lib.pof_ieks_workspace_bytes
+        entry = lib.pof_ieks_solve_sequential if sequential else lib.pof_ieks_solve
+        wsb = wsq(_lib.POF_F64, n, D, d)
         ws = _lib.workspace(wsb, dev)
-        rc = lib.pof_ieks_solve(_lib.POF_F64, n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]),
-                                _lib.ptr(m0), _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means),
-                                _lib.ptr(chols), int(maxiters), int(bool(calibrate)), _lib.ptr(info), _lib.ptr(ws),
-                                wsb, _lib.stream_handle())
-        _lib.check(rc, "pof_ieks_solve")
+        rc = entry(_lib.POF_F64, n, D, d, _lib.FIELDS[name], _lib.ptr(p), float(setup["dt"]),
+                   _lib.ptr(m0), _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL), _lib.ptr(means),
+                   _lib.ptr(chols), int(maxiters), int(bool(calibrate)), _lib.ptr(info), _lib.ptr(ws),
+                   wsb, _lib.stream_handle())
+        _lib.check(rc, "pof_ieks_solve_sequential" if sequential else "pof_ieks_solve")
     info_dict = {
         "iterations": info[_lib.I_ITERATIONS].to(torch.int64),
-        "nll": info[_lib.I_NLL],
+        # the sequential twin reports +sum log-likelihood (quirk of
+        # pof/sequential_filtsmooth/filter.py:23-30), the parallel filter -sum
+        "nll": -info[_lib.I_NLL] if sequential else info[_lib.I_NLL],
         "obj": info[_lib.I_OBJ],
         "sigma_squared": info[_lib.I_SSQ],
+        "status": info[_lib.I_STATUS].to(torch.int64),
         "calibrated": bool(calibrate),
     }
     if precision == "mixed":
@@ -68,10 +74,13 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     """Parallel-in-time IEKS (pof/solver.py:11-73).
 
     Returns (MVNSqrt(means (N, d), chol_covs (N, d, D)), info) with
-    info = {iterations, nll, obj, sigma_squared, calibrated}.  Built-in fields
-    (pof.ivp) run the whole loop on the device; other torch vector fields are
-    linearized with torch.func on the device and filtered/smoothed by libpof,
-    with the loop test read back each iteration.
+    info = {iterations, nll, obj, sigma_squared, status, calibrated}
+    (status: why the loop stopped, 0 converged, 1 maxiters, 2 non-finite).
+    Built-in fields (pof.ivp) run the whole loop on the device, with the
+    parallel or (sequential=True) the sequential filter/smoother; other
+    torch vector fields are linearized with torch.func on the device and
+    filtered/smoothed by libpof, with the loop test read back each
+    iteration.
 
     precision="mixed" (built-in fields, an addition to the reference's
     signature): float32 IEKS iterations until the objective's relative change
@@ -83,9 +92,10 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     x0 = setup["x0"]
     states = get_initial_trajectory(setup, method=init)
 
-    if om.field is not None and not sequential and _lib.shape_supported(x0.mean.shape[0], setup["iwp"].wiener_process_dimension):
+    builtin = om.field is not None and _lib.shape_supported(x0.mean.shape[0], setup["iwp"].wiener_process_dimension)
+    if builtin and (not sequential or precision == "float64"):
         states, info_dict = _solve_builtin(setup, states, calibrate, maxiters, precision, maxiters_f32, rtol_f32,
-                                           settle_f32)
+                                           settle_f32, sequential=sequential)
         return gmul_stack(setup["E0"], states), info_dict
     if precision != "float64":
         raise NotImplementedError("precision=%r needs a built-in field (pof.ivp)" % (precision,))
@@ -102,16 +112,22 @@ def _solve_loop(setup, states, calibrate, maxiters, sequential):
     nll = obj = ssq = z
     states_old, nll_old, obj_old = states, z, z
     k = 0
+    conv = False
     while True:
         # cond (solver.py:36-45)
-        if not (k < 1 or (not bool(convergence_criteria.crit(obj, obj_old, nll, nll_old, states, states_old))
-                          and k <= maxiters)):
+        if k >= 1:
+            conv = bool(convergence_criteria.crit(obj, obj_old, nll, nll_old, states, states_old))
+        if not (k < 1 or (not conv and k <= maxiters)):
             break
         # body (solver.py:47-55)
         states_old, nll_old, obj_old = states, nll, obj
         states, nll, obj, ssq = ieks_step(om=om, dtm=dtm, x0=x0, states=states_old, sequential=sequential)
         k += 1
-    info_dict = {"iterations": torch.tensor(k), "nll": nll, "obj": obj, "sigma_squared": ssq, "calibrated": False}
+    # the stopping reason (POF_SOLVE_*), as libpof's loop reports it
+    finite = bool(torch.isfinite(torch.as_tensor(obj)).item() and torch.isfinite(torch.as_tensor(nll)).item())
+    status = 0 if (finite and conv) else (1 if finite else 2)
+    info_dict = {"iterations": torch.tensor(k), "nll": nll, "obj": obj, "sigma_squared": ssq,
+                 "status": torch.tensor(status), "calibrated": False}
     if calibrate:
         states = MVNSqrt(states.mean, ssq**0.5 * states.chol)
         info_dict["calibrated"] = True
