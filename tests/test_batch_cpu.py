@@ -5,6 +5,7 @@ pof_ieks_solve_batch (which return before any GPU work)."""
 import ctypes
 
 import numpy as np
+import torch
 import pytest
 
 from oracle import ivp as oivp, solver as osolver
@@ -150,3 +151,29 @@ def test_server_and_mixed_workspace_queries_and_refusals(lib):
     wmx = lib.pof_batch_mixed_workspace_bytes(4, pns, 8, 2, 0, 0)
     assert wmx > w64 > 0
     assert lib.pof_batch_mixed_workspace_bytes(4, pns, 7, 2, 0, 0) == 0
+
+
+def test_autotune_cache_round_trip(tmp_path, monkeypatch):
+    """The autotuner's choice is stored under the batch's key (GPU, D, d,
+    total steps to a factor of two) and found again; a batch of another key
+    is tuned anew; other keys of the file are kept."""
+    from pof import batch as pbatch
+
+    monkeypatch.setenv("POF_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    prep = {"D": 8, "d": 2, "n_steps": np.array([1000, 3000]), "x0m": torch.zeros(2, 8)}
+    other = {"D": 8, "d": 2, "n_steps": np.array([100000]), "x0m": torch.zeros(1, 8)}
+    calls = []
+
+    def timer(C0, Cg, wide):
+        calls.append((C0, Cg, wide))
+        return abs(C0 - 32) + (0.5 if Cg == 4 else 0.0) + (0.25 if wide else 0.0)
+
+    assert pbatch.load_tuning(prep) is None
+    assert pbatch.tuned(prep, timer=timer) == (32, 2, False)
+    n = len(calls)
+    assert n == 5 * 2 * 2
+    assert pbatch.tuned(prep, timer=timer) == (32, 2, False) and len(calls) == n  # from the cache
+    assert pbatch.autotune_key(other) != pbatch.autotune_key(prep)
+    pbatch.tuned(other, timer=timer)
+    assert len(calls) == 2 * n
+    assert pbatch.load_tuning(prep) == (32, 2, False) and pbatch.load_tuning(other) is not None

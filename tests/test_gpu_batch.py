@@ -231,11 +231,20 @@ def test_batch_mixed_independent_of_the_mix():
         assert int(full.info["iterations_float32"][b]) == int(alone.info["iterations_float32"][0])
 
 
-def test_autotune_picks_a_candidate_and_keeps_parity():
+def test_autotune_picks_a_candidate_and_keeps_parity(tmp_path, monkeypatch):
+    """Chunk length, group size and level-0 team width by timing; the tuned
+    solve keeps parity; solve_batch(C0="auto") stores the choice in the
+    autotune cache and takes it from there the next time."""
     prep = pbatch.prepare_batch(problems(BATCH_D2), 3)
-    C0, Cg, times = pbatch.autotune(prep, C0s=(4, 16), Cgs=(2, 4), iterations=2, repeats=1)
-    assert (C0, Cg) in times and len(times) == 4 and all(t > 0 for t in times.values())
-    res = pbatch.solve_batch(problems(BATCH_D2), order=3, maxiters=1000, C0=C0, Cg=Cg)
+    C0, Cg, wide, times = pbatch.autotune(prep, C0s=(4, 16), Cgs=(2, 4), iterations=2, repeats=1)
+    assert (C0, Cg, wide) in times and len(times) == 8 and all(t > 0 for t in times.values())
+    with pbatch._TeamWidth(wide):
+        res = pbatch.solve_batch(problems(BATCH_D2), order=3, maxiters=1000, C0=C0, Cg=Cg)
+    monkeypatch.setenv("POF_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    auto = pbatch.solve_batch(problems(BATCH_D2), order=3, maxiters=1000, C0="auto")
+    assert pbatch.load_tuning(prep) is not None
+    again = pbatch.solve_batch(problems(BATCH_D2), order=3, maxiters=1000, C0="auto")
+    assert torch.equal(auto.mean, again.mean)  # the cached choice, the same bits
     ref = pbatch.solve_batch(problems(BATCH_D2), order=3, maxiters=1000, C0=4, Cg=2)
     for b in range(len(BATCH_D2)):
         (ma, _), ia = ref.problem(b)

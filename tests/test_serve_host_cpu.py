@@ -58,7 +58,8 @@ class FakeEngines:
         if not free or s["used"] + n_steps + 1 > s["maxG"]:
             return BUSY
         slot = free[0]
-        s["slots"][slot] = {"n": n_steps, "it": 0, "target": self.iterations(n_steps), "done": False}
+        s["slots"][slot] = {"n": n_steps, "it": 0, "target": self.iterations(n_steps), "done": False,
+                            "cancel": False, "status": 0}
         s["used"] += n_steps + 1
         self.log.append(("admit", (s["D"], s["d"]), slot, n_steps))
         return slot
@@ -66,11 +67,24 @@ class FakeEngines:
     def pof_server_launch(self, h, k):
         s = self._s(h)
         for slot, r in sorted(s["slots"].items()):
-            if not r["done"]:
-                r["it"] = min(r["it"] + k, r["target"])
-                if r["it"] == r["target"]:
+            for _ in range(k):
+                if r["done"]:
+                    break
+                r["it"] += 1
+                if r["cancel"] or r["it"] >= r["target"]:
+                    # a cancelled request stops at the first tick after the flag
+                    r["status"] = 3 if (r["cancel"] and r["it"] < r["target"]) else 0
                     r["done"] = True
                     s["done"].append(slot)
+        return 0
+
+    def pof_server_cancel(self, h, slot):
+        s = self._s(h)
+        r = s["slots"].get(slot)
+        if r is None or r["done"]:
+            return -1
+        r["cancel"] = True
+        self.log.append(("cancel", (s["D"], s["d"]), slot, r["n"]))
         return 0
 
     def pof_server_sync(self, h, nref):
@@ -93,7 +107,7 @@ class FakeEngines:
         # every state's mean holds (n_steps, slot) so the test can tell results apart
         mean = np.tile(np.array([r["n"], slot] * D, dtype=np.float64)[:D], (N, 1))
         chol = np.zeros((N, D, D))
-        inf = np.array([r["it"], 1.0, 2.0, 3.0])
+        inf = np.array([r["it"], 1.0, 2.0, 3.0, r["status"]])
         for ptr, a in ((m, mean), (L, chol), (info, inf)):
             ctypes.memmove(ptr.value, a.ctypes.data, a.nbytes)
         self.log.append(("fetch", (s["D"], s["d"]), slot, r["n"]))
@@ -187,3 +201,50 @@ def test_engines_per_shape_and_close(fake):
     assert sorted(srv.engines) == [(1, 2), (1, 3), (2, 3)]
     srv.close()
     assert srv.engines == {}
+
+
+def test_cancel_queued_and_running_requests(fake):
+    """A queued request leaves the queue at once; an admitted one stops at
+    the engine's next tick with its last iterate; both report "cancelled",
+    and the other requests are unaffected."""
+    srv = serve.Server(max_requests=1, max_points=10**6)
+    a = srv.submit(*logistic(500), order=2)   # admitted, 7 iterations to go
+    b = srv.submit(*logistic(100), order=2)   # waits for a's slot
+    c = srv.submit(*logistic(200), order=2)
+    srv.tick()
+    assert srv.cancel(b)                      # still queued
+    assert srv.cancel(a)                      # running
+    _run(srv)
+    (ma, _), ia = srv.result(a)
+    assert ia["status"] == "cancelled" and int(ia["iterations"]) == 2  # one tick, then stopped at the next
+    assert ma is not None and ma.shape == (501, 1)
+    yb, ib = srv.result(b)
+    assert yb is None and ib["status"] == "cancelled" and int(ib["iterations"]) == 0
+    _, ic = srv.result(c)
+    assert ic["status"] == "converged" and int(ic["iterations"]) == 2 + 200 // 100
+    assert not srv.cancel(c)                  # already finished
+    assert [n for ev, _, _, n in fake.log if ev == "admit"] == [500, 200]
+
+
+def test_stuck_request_times_out(fake, monkeypatch):
+    """A request that never meets its criterion (injected on the host: the
+    fake engine never finishes it) is cancelled once its timeout has
+    passed, reported as "timeout", and frees its slot for the next one."""
+    clock = [0.0]
+    monkeypatch.setattr(serve.time, "perf_counter", lambda: clock[0])
+    fake.iterations = lambda n: 10**9 if n == 777 else 3
+    srv = serve.Server(max_requests=1, max_points=10**6)
+    stuck = srv.submit(*logistic(777), order=2, timeout=5.0)
+    after = srv.submit(*logistic(50), order=2, timeout=5.0)
+    for _ in range(4):
+        srv.tick()
+        clock[0] += 1.0
+    assert stuck not in srv.results and after not in srv.results
+    clock[0] = 5.0                            # both deadlines pass; `after` is still queued
+    _run(srv)
+    (m, _), info = srv.result(stuck)
+    assert info["status"] == "timeout" and m.shape == (778, 1)
+    y, info2 = srv.result(after)
+    assert y is None and info2["status"] == "timeout"
+    ev = [e for e, _, _, _ in fake.log]
+    assert ev.count("cancel") == 1 and ev.count("admit") == 1

@@ -68,11 +68,52 @@ def test_noalloc_matches_workspace_entry_point_twice(name, mk, N, q):
         assert np.allclose(s[:4], s_ref[:4], rtol=1e-10, atol=0)
 
 
+SCRATCH = 16 * 1024 * 1024
+
+
+def _n_max(lib, dtype, D, d):
+    """Largest step count whose workspace fits the fixed scratch."""
+    lo, hi = 1, 10**8
+    while lo < hi:
+        m = (lo + hi + 1) // 2
+        if lib.pof_filtsmooth_workspace_bytes(dtype, m, D, d) <= SCRATCH:
+            lo = m
+        else:
+            hi = m - 1
+    return lo
+
+
 def test_noalloc_refuses_problems_larger_than_its_scratch():
     lib = _lib.lib()
-    n, D, d = 10_000_000, 8, 2
-    assert lib.pof_filtsmooth_workspace_bytes(0, n, D, d) > 16 * 1024 * 1024
     null = ctypes.c_void_p(0)
-    rc = lib.pof_linear_filtsmooth_noalloc(0, n, D, d, null, null, null, null, 0, null, null, null, 0, null, null,
-                                           null, null)
-    assert rc == -3  # POF_ERR_WORKSPACE, refused before any GPU work
+
+    def call(dtype, n, D, d):
+        return lib.pof_linear_filtsmooth_noalloc(dtype, n, D, d, null, null, null, null, 0, null, null, null, 0,
+                                                 null, null, null, null)
+
+    for dtype, D, d, documented in ((0, 8, 2, 3344), (1, 8, 2, 6660), (0, 4, 1, 20296), (0, 3, 1, 34212)):
+        n_max = _n_max(lib, dtype, D, d)
+        assert n_max == documented  # the limits include/pof.h lists
+        assert call(dtype, n_max + 1, D, d) == -3  # POF_ERR_WORKSPACE, refused before any GPU work
+    assert call(0, 10_000_000, 8, 2) == -3
+    # bad inputs get the statuses of the workspace entry point, not the size refusal
+    for args in ((7, 100, 8, 2), (0, 0, 8, 2), (0, 100, 8, 9), (0, 100, 7, 2)):
+        dtype, n, D, d = args
+        ref = lib.pof_linear_filtsmooth(dtype, n, D, d, null, null, null, null, 0, null, null, null, 0, null, null,
+                                        null, null, 0, null)
+        assert call(*args) == ref != 0, (args, ref)
+
+
+def test_noalloc_runs_the_largest_problem_it_accepts():
+    """The boundary itself: n_max steps (D = 8, d = 2, float64) run in the
+    fixed scratch and equal the workspace entry point."""
+    torch.cuda.set_device(0)
+    lib = _lib.lib()
+    n = _n_max(lib, 0, 8, 2)
+    a = _inputs(oivp.fhn_classic(tmax=10.0 * n / 500), n + 1, 3)
+    rc, m_ref, L_ref, s_ref = _run(lib, a, n, 8, 2, noalloc=False)
+    assert rc == 0
+    rc, m, L, s = _run(lib, a, n, 8, 2, noalloc=True)
+    assert rc == 0, lib.pof_status_string(rc)
+    assert np.abs(m - m_ref).max() <= 1e-10 * np.abs(m_ref).max()
+    assert np.allclose(s[:4], s_ref[:4], rtol=1e-10, atol=0)
