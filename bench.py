@@ -56,9 +56,26 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "fhn_q3_N65536"
 MAXITERS = 10_000  # the reference's default (pof/solver.py:12)
 
-# DRAM bytes (read + write) per launch of a workload's dominant kernel from
-# one ncu capture (profiles/k_filt_l0_down_team_fhn_q3_N65536.md)
+# DRAM bytes (read + write) per launch of a workload's dominant kernel
+# (dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
+# k_filt_l0_down_team<double, 8, 2, 8> on this workload; not measured by the
+# bench run itself)
 NCU_TRAFFIC = {("fhn_q3_N65536", "filt_l0_down"): 66.193664e6 + 108.293888e6}
+
+
+def workload_config(workload):
+    """The `config` object of a plain workload's line: the same dict in the
+    GPU arm and in the reference arm (measured quantities such as the
+    iteration count are reported beside it, not in it)."""
+    name, kw, t1, q, N = WORKLOADS[workload]
+    from oracle import ivp as oivp
+
+    ivp = getattr(oivp, name)(**kw)
+    d = ivp.y0.shape[0]
+    return {"workload": workload, "ivp": name, "params": [float(x) for x in ivp.params], "y0": ivp.y0.tolist(),
+            "q": q, "D": d * (q + 1), "N": N, "t1": t1, "init": "constant", "maxiters": MAXITERS,
+            "criterion": "pof/convergence_criteria.py (obj rtol 1e-6, atol 1e-9; means rtol 1e-13)",
+            "l2": "flushed between solves (256 MiB write)"}
 
 
 def jprint(obj):
@@ -78,6 +95,18 @@ def max_over_ranks(x, world, device):
     return float(t.item())
 
 
+def sum_over_ranks(x, world, device):
+    """Sum of x over the ranks (x itself with one rank).  All ranks call it."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -90,15 +119,17 @@ def dist_info():
 # ---------------------------------------------------------------------------
 
 
-def _oracle_iteration_s(workload, M):
-    """Seconds of one oracle IEKS iteration (ieks_step) on the first M steps
-    of the workload's grid (run in a worker process)."""
+def _oracle_iteration_s(workload, M=None):
+    """Seconds of one oracle IEKS iteration (ieks_step, the reference's
+    associative-scan order) on the first M steps of the workload's grid, the
+    whole grid when M is None (run in a worker process)."""
     from oracle import ivp as oivp, solver as osolver
 
     name, kw, t1, q, N = WORKLOADS[workload]
     ivp = getattr(oivp, name)(**kw)
-    dt = (t1 - ivp.t0) / (N - 1)
-    ts = ivp.t0 + dt * np.arange(M + 1)
+    ts = np.linspace(ivp.t0, t1, N)
+    if M is not None:
+        ts = ts[: M + 1]
     st = osolver.set_up_solver(ivp, ts, q)
     states = osolver.get_initial_trajectory(st, "constant")
     t0 = time.perf_counter()
@@ -106,52 +137,64 @@ def _oracle_iteration_s(workload, M):
     return time.perf_counter() - t0
 
 
-def cpu_sample(workload, budget_s=20.0, iterations=None, procs=None):
-    """Cost per step and IEKS iteration of the reference's algorithm (the
-    oracle: the associative-scan tree of jax.lax.associative_scan, NumPy and
-    LAPACK) on the host cores: a contiguous sub-grid of M steps is sized in
-    one process (about budget_s / 8), then `procs` processes (default: every
-    core) each run one iteration on it at once; the aggregate rate is
-    procs x M step-iterations over the wall time.  The full solve's time is
-    that cost x (N - 1) x iterations."""
-    import concurrent.futures as cf
-    import multiprocessing as mp
+class CpuReference:
+    """The reference's algorithm (the NumPy float64 oracle: its
+    associative-scan bracketing, LAPACK QR) on every host core: `procs`
+    worker processes (spawned, one BLAS thread each) each run one IEKS
+    iteration over the WHOLE grid of the workload at the same time, i.e.
+    procs independent solves progressing in parallel.  One round is one
+    timed sample; a solve's time is extrapolated from it as
+    (round time / procs) x the iteration count of the solve."""
 
-    name, kw, t1, q, N = WORKLOADS[workload]
-    M = 256
-    while True:
-        el = _oracle_iteration_s(workload, M)
-        if el > budget_s / 8 or M >= N - 1:
-            break
-        M = min(M * 4, N - 1)
-    procs = procs or os.cpu_count() or 1
-    saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
-    for k in saved:
-        os.environ[k] = "1"  # one core per worker
-    try:
-        with cf.ProcessPoolExecutor(procs, mp_context=mp.get_context("spawn")) as ex:
-            list(ex.map(_oracle_iteration_s, [workload] * procs, [64] * procs))  # start-up, imports
-            t0 = time.perf_counter()
-            list(ex.map(_oracle_iteration_s, [workload] * procs, [M] * procs))
-            wall = time.perf_counter() - t0
-    finally:
-        for k, v in saved.items():
+    def __init__(self, workload, procs=None):
+        import concurrent.futures as cf
+        import multiprocessing as mp
+
+        self.workload = workload
+        self.procs = procs or os.cpu_count() or 1
+        self._saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+        for k in self._saved:
+            os.environ[k] = "1"  # one core per worker
+        self.ex = cf.ProcessPoolExecutor(self.procs, mp_context=mp.get_context("spawn"))
+
+    def warm(self):
+        """Start the workers and import the oracle (a 64-step iteration each)."""
+        list(self.ex.map(_oracle_iteration_s, [self.workload] * self.procs, [64] * self.procs))
+
+    def round(self):
+        """Wall seconds of one round: every worker one whole-grid iteration."""
+        t0 = time.perf_counter()
+        list(self.ex.map(_oracle_iteration_s, [self.workload] * self.procs))
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.ex.shutdown()
+        for k, v in self._saved.items():
             if v is None:
                 os.environ.pop(k, None)
             else:
                 os.environ[k] = v
-    per_step_iter = wall / (procs * M)
-    its = iterations
-    solve_s = per_step_iter * (N - 1) * its
-    return {
-        "per_step_iter_s": per_step_iter,
-        "solve_s": solve_s,
-        "value": (N - 1) / solve_s,
-        "sample": "one IEKS iteration (ieks_step) of the oracle on the first %d steps of the grid in each of %d "
-        "processes at once; solve time extrapolated as cost per step-iteration x (N-1) x %d iterations"
-        % (M, procs, its),
-        "cores": procs,
-    }
+
+    def describe(self, iterations):
+        N = WORKLOADS[self.workload][4]
+        return ("one IEKS iteration (ieks_step) of the oracle over the whole grid (%d steps) in each of %d "
+                "processes at once per sample; a solve's time is extrapolated as sample time / %d x %d iterations "
+                "(the float64 GPU solve's iteration count)" % (N - 1, self.procs, self.procs, iterations))
+
+
+def cpu_sample(workload, iterations, rounds=1):
+    """cpu_baseline of the GPU arm: CpuReference, `rounds` timed rounds."""
+    ref = CpuReference(workload)
+    try:
+        ref.warm()
+        walls = [ref.round() for _ in range(rounds)]
+    finally:
+        ref.close()
+    N = WORKLOADS[workload][4]
+    wall = float(np.median(walls))
+    solve_s = wall / ref.procs * iterations
+    return {"value": (N - 1) / solve_s, "solve_s": solve_s, "round_s": wall, "cores": ref.procs,
+            "sample": ref.describe(iterations)}
 
 
 def run_reference(args, workload):
@@ -163,13 +206,16 @@ def run_reference(args, workload):
         jprint({"impl": "reference", "unavailable": "no measured IEKS iteration count for workload %s to "
                 "extrapolate the CPU sample with" % workload})
         return
-    samples = []
-    for _ in range(args.warmup):
-        cpu_sample(workload, budget_s=4.0, iterations=iters)
-    for _ in range(args.steps):
-        samples.append(cpu_sample(workload, budget_s=8.0, iterations=iters))
     name, kw, t1, q, N = WORKLOADS[workload]
-    solve_s = float(np.median([s["solve_s"] for s in samples]))
+    ref = CpuReference(workload)
+    try:
+        for _ in range(max(args.warmup, 1)):  # worker start-up and imports (64-step iterations)
+            ref.warm()
+        walls = [ref.round() for _ in range(args.steps)]
+    finally:
+        ref.close()
+    wall = float(np.mean(walls))
+    solve_s = wall / ref.procs * iters
     value = (N - 1) / solve_s
     jprint(
         {
@@ -180,16 +226,19 @@ def run_reference(args, workload):
             "n_gpus": args.gpus,
             "steps": args.steps,
             "warmup": args.warmup,
-            "ms_per_step": solve_s * 1e3,
+            "ms_per_step": wall * 1e3,
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": workload, "ivp": name, "q": q, "N": N, "t1": t1, "init": "constant",
-                       "iterations": iters},
-            "cpu_baseline": {"value": value, "unit": "IVP*steps/s", "cores": samples[-1]["cores"], "kind": "port",
-                             "sample": samples[-1]["sample"]},
+            "config": workload_config(workload),
+            "step": "one sample: %d whole-grid IEKS iterations at once (one per core); ms_per_step is its wall "
+                    "time" % ref.procs,
+            "extrapolation": {"iterations_per_solve": iters, "solves_in_parallel": ref.procs,
+                              "solve_s": solve_s},
+            "cpu_baseline": {"value": value, "unit": "IVP*steps/s", "cores": ref.procs, "kind": "port",
+                             "sample": ref.describe(iters)},
             "e2e": {"value": value, "unit": "IVP*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference is JAX (not installed here); this arm times the NumPy float64 restatement of its "
                     "algorithm (oracle/) on every host core",
@@ -444,6 +493,12 @@ def run_gpu(args, workload):
     e2e_s = max_over_ranks(float(np.mean(e2e_times)), world, dev)
     e2e_value = world * n / e2e_s
 
+    extras = {}
+    if not args.no_extras:  # every rank: the batched block splits one batch over the ranks
+        extras["config0"] = config0_block(args)
+        extras["batched"] = batched_block(args)
+        extras["served"] = served_block(args)
+
     if rank != 0:
         return
     out = {
@@ -459,16 +514,22 @@ def run_gpu(args, workload):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": workload, "ivp": name, "params": list(params), "q": q, "D": D, "N": N, "t1": t1,
-                   "init": "constant", "iterations": iterations, "maxiters": MAXITERS,
-                   "l2": "flushed between solves (256 MiB write)", "C0": C0, "levels": cnt[1:]},
+        "config": workload_config(workload),
+        "iterations": iterations,
+        "status": _lib.solve_status(info[_lib.I_STATUS].item()),
+        "ms_per_iteration": ms / iterations,
+        "plan": {"C0": C0, "levels": cnt[1:]},
         "e2e": {"value": e2e_value, "unit": "IVP*steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
                 "path": "pof.solver.solve(numpy y0, ts) -> means/chols .cpu()"},
         "roofline": {"bound": "fp64", "kernel": dom_kind, "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC.get((workload, dom_kind)),
-                     "peak_source": "measured on this GPU by pof_fp64_probe (FP64 FMA chains); "
-                                    "MEASURED_PEAKS.json has no FP64 figure",
+                     "traffic_source": ("ncu capture of this kernel on this workload (dram__bytes_read.sum + "
+                                        "dram__bytes_write.sum per launch), a constant of bench.py, not measured "
+                                        "in this run") if (workload, dom_kind) in NCU_TRAFFIC else None,
+                     "algorithmic_bytes_per_launch": _flops.kernel_bytes(n, D, d).get(dom_kind),
+                     "peak_source": "measured in this run by pof_fp64_probe (8 independent FP64 FMA chains per "
+                                    "thread, all SMs); MEASURED_PEAKS.json has no FP64 figure",
                      "flops_per_launch": dom_flops, "ms_per_launch": dom_ms_per_launch},
         "kernels": {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in prof.items() if v[1]},
         "gpu_launches": int(launches_per_solve * args.steps),
@@ -479,11 +540,263 @@ def run_gpu(args, workload):
     }
     if mixed is not None:
         out["mixed_precision"] = mixed
+    out.update(extras)
     if not args.no_cpu_baseline:
-        cb = cpu_sample(workload, budget_s=20.0, iterations=iterations)
+        cb = cpu_sample(workload, iterations=iterations)
         out["cpu_baseline"] = {"value": cb["value"], "unit": "IVP*steps/s", "cores": cb["cores"], "kind": "port",
-                               "sample": cb["sample"]}
+                               "sample": cb["sample"], "round_s": cb["round_s"]}
     jprint(out)
+
+
+# ---------------------------------------------------------------------------
+# Blocks of the default line: the other configurations, measured briefly
+# ---------------------------------------------------------------------------
+
+BATCH_BUDGET = 24  # maxiters of the default line's batched block: at most 25 IEKS iterations per instance
+
+
+def _events_ms(torch, fn, reps):
+    out = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return out
+
+
+def config0_block(args):
+    """FitzHugh-Nagumo (0.2, 0.2, 3), t in [0, 100], N = 1000, q = 3,
+    constant init, the reference's criterion: whole solves through
+    pof_ieks_solve (inputs resident), 1 warm-up + 3 timed."""
+    import torch
+
+    from pof import _lib, ivp as pivp
+    from pof.convenience import get_initial_trajectory, set_up_solver
+
+    lib = _lib.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    p = pivp.fhn_classic()
+    N, q = 1000, 3
+    ts = np.linspace(0.0, 100.0, N)
+    setup = set_up_solver(f=p.f, y0=p.y0, ts=ts, order=q)
+    means0 = get_initial_trajectory(setup, "constant").mean.contiguous()
+    D, d, n = means0.shape[1], 2, N - 1
+    means = torch.empty_like(means0)
+    chols = torch.empty((N, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+    prm = torch.tensor(setup["om"].field[1], dtype=torch.float64, device=dev)
+    wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+    ws = _lib.workspace(wsb, dev)
+    F, QL = setup["dtm"].F[0].contiguous(), setup["dtm"].QL[0].contiguous()
+    m0, L0 = setup["x0"].mean.contiguous(), setup["x0"].chol.contiguous()
+
+    def one():
+        means.copy_(means0)
+        _lib.check(lib.pof_ieks_solve(_lib.POF_F64, n, D, d, _lib.FIELDS["fhn_classic"], _lib.ptr(prm),
+                                      float(setup["dt"]), _lib.ptr(m0), _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL),
+                                      _lib.ptr(means), _lib.ptr(chols), MAXITERS, 1, _lib.ptr(info), _lib.ptr(ws), wsb,
+                                      _lib.stream_handle()), "pof_ieks_solve")
+
+    one()
+    ms = float(np.mean(_events_ms(torch, one, 3)))
+    it = int(info[_lib.I_ITERATIONS].item())
+    return {"workload": "fhn_q3_N1000 (the reference's CPU configuration)", "ms_per_solve": ms, "iterations": it,
+            "ms_per_iteration": ms / it, "value": n / (ms * 1e-3), "unit": "IVP*steps/s",
+            "status": _lib.solve_status(info[_lib.I_STATUS].item()),
+            "note": "the iteration count is decided by rounding on this problem (the reference's own tree and "
+                    "sequential orders stop at 657 and another count); ms per iteration compares kernels"}
+
+
+def batched_block(args):
+    """The batched configuration's exact instances (4096 FitzHugh-Nagumo,
+    default_rng(0), N log-uniform in [256, 8192], q = 3) under a fixed
+    iteration budget (maxiters = BATCH_BUDGET): step-iterations/s of the
+    plain one-solve-per-launch float64 path (8 instances stratified by N),
+    the batched float64 solve and the batched mixed solve (float32 iterations
+    under the same budget, float64 polish under it), each timed once after a
+    one-iteration warm-up; per-instance error of mixed against batched
+    float64."""
+    import torch
+
+    from pof import _lib, batch as pbatch
+
+    lib = _lib.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rank, world, _ = dist_info()
+    family, B, seed, q, _ = BATCH_WORKLOADS["fhn_batch4096"]
+    problems = batch_problems(family, B, seed)
+    if world > 1:  # one fixed batch split over the ranks by steps
+        problems = [problems[b] for b in pbatch.shard([len(p[3]) - 1 for p in problems], world)[rank]]
+    prep = pbatch.prepare_batch(problems, q, device=dev)
+    Bl = prep["B"]
+    n_steps = prep["n_steps"]
+    D, d = prep["D"], prep["d"]
+    means = torch.empty_like(prep["means0"])
+    G = means.shape[0]
+    chols = torch.empty((G, D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros((Bl, _lib.I_COUNT), dtype=torch.float64, device=dev)
+    info32 = torch.zeros((Bl, 2), dtype=torch.float64, device=dev)
+    ws = [None]
+
+    def solve(precision, maxiters):
+        means.copy_(prep["means0"])
+        ws[0] = pbatch.run_batch(prep, means, chols, info, maxiters=maxiters, workspace=ws[0], precision=precision,
+                                 info_f32=info32, maxiters_f32=maxiters, settle_f32=args.f32_settle)
+
+    out = {"workload": "fhn_batch4096: %d instances%s, a, b, c within +-20%% of (0.2, 0.2, 3), y0 ~ N((-1, 1), "
+                       "0.1^2 I), t in [0, 100], N log-uniform in [256, 8192] (default_rng(0)), q = 3"
+                       % (B, " (this rank's share: %d)" % Bl if world > 1 else ""),
+           "budget": "fixed iteration budget: maxiters = %d (at most %d IEKS iterations per instance; instances "
+                     "that meet the criterion stop earlier)" % (BATCH_BUDGET, BATCH_BUDGET + 1),
+           "total_steps": int(n_steps.sum())}
+    def timed_all(fn):
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return max_over_ranks(_events_ms(torch, fn, 1)[0], world, dev)
+
+    solve("float64", 0)
+    t64 = timed_all(lambda: solve("float64", BATCH_BUDGET))
+    its = info[:, _lib.I_ITERATIONS].cpu().numpy()
+    st = info[:, _lib.I_STATUS].cpu().numpy()
+    si64 = sum_over_ranks(float((n_steps * its).sum()), world, dev)
+    steps_all = sum_over_ranks(float(n_steps.sum()), world, dev)
+    ref = means.clone()
+    out["batched_float64"] = {"ms": t64, "step_iterations_per_s": si64 / (t64 * 1e-3),
+                              "ivp_steps_per_s": steps_all / (t64 * 1e-3),
+                              "converged": int(sum_over_ranks(int((st == 0).sum()), world, dev))}
+    solve("mixed", 0)
+    tmx = timed_all(lambda: solve("mixed", BATCH_BUDGET))
+    it64 = info[:, _lib.I_ITERATIONS].cpu().numpy()
+    it32 = info32[:, 0].cpu().numpy()
+    stm = info[:, _lib.I_STATUS].cpu().numpy()
+    err = _project_err(prep, means, ref)
+    both = (st == 0) & (stm == 0)
+    out["batched_mixed"] = {
+        "ms": tmx,
+        "step_iterations_per_s": sum_over_ranks(float((n_steps * (it64 + it32)).sum()), world, dev) / (tmx * 1e-3),
+        "ivp_steps_per_s": steps_all / (tmx * 1e-3),
+        "iterations_float32_total": int(it32.sum()), "iterations_float64_total": int(it64.sum()),
+        "converged": int((stm == 0).sum()),
+        "rel_err_vs_batched_float64": {"max": float(err.max()), "median": float(np.median(err))},
+        "rel_err_where_both_converged": {"instances": int(both.sum()),
+                                         "max": float(err[both].max()) if both.any() else None,
+                                         "median": float(np.median(err[both])) if both.any() else None,
+                                         "fraction_within_1e-6": float((err[both] <= 1e-6).mean())
+                                         if both.any() else None}}
+    # plain float64 path, one pof_ieks_solve per instance, same budget
+    order = np.argsort(n_steps)
+    sample = [int(order[int(i)]) for i in np.linspace(0, Bl - 1, 8)]
+    plain_ms, plain_si, plain_steps = 0.0, 0.0, 0
+    for b in sample:
+        n = int(n_steps[b])
+        m = torch.empty((n + 1, D), dtype=torch.float64, device=dev)
+        c = torch.empty((n + 1, D, D), dtype=torch.float64, device=dev)
+        inf = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+        wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+        pws = _lib.workspace(wsb, dev)
+        m0 = prep["means0"][prep["offsets"][b]:prep["offsets"][b + 1]]
+        x0m, x0L = prep["x0m"][b].contiguous(), prep["x0L"][b].contiguous()
+
+        def one():
+            m.copy_(m0)
+            _lib.check(lib.pof_ieks_solve(_lib.POF_F64, n, D, d, int(prep["fields"][b]), _lib.ptr(prep["params"][b]),
+                                          float(prep["h"][b]), _lib.ptr(x0m), _lib.ptr(x0L), _lib.ptr(prep["F"]),
+                                          _lib.ptr(prep["QL"]), _lib.ptr(m), _lib.ptr(c), BATCH_BUDGET, 1,
+                                          _lib.ptr(inf), _lib.ptr(pws), wsb, _lib.stream_handle()), "pof_ieks_solve")
+
+        one()
+        t = _events_ms(torch, one, 1)[0]
+        plain_ms += t
+        plain_si += n * int(inf[_lib.I_ITERATIONS].item())
+        plain_steps += n
+    plain_rate = plain_si / (plain_ms * 1e-3)
+    out["plain_float64"] = {"sample": "8 instances stratified by N, one pof_ieks_solve each",
+                            "step_iterations_per_s": plain_rate, "ivp_steps_per_s": plain_steps / (plain_ms * 1e-3)}
+    out["speedup_vs_plain"] = {
+        "batched_float64": out["batched_float64"]["step_iterations_per_s"] / plain_rate,
+        "batched_mixed": out["batched_mixed"]["step_iterations_per_s"] / plain_rate,
+        "unit": "ratio of step-iterations/s under the same budget"}
+    del ws[0]
+    return out
+
+
+def served_block(args):
+    """A short served stream: 48 requests (logistic, FitzHugh-Nagumo,
+    Lotka-Volterra, Van der Pol mu = 10; +-20 % parameters, N log-uniform in
+    [2^8, 2^16], q in {2, 3, 4}, tolerance in {1e-4, 1e-6}, maxiters 100) at
+    16 Poisson arrivals/s, served in real time by pof.serve.Server; latency
+    percentiles and throughput against the plain path serving the same
+    arrivals one request at a time (first come, first served, on each
+    request's measured pof_ieks_solve time)."""
+    import torch
+
+    from pof import _lib, batch as pbatch, serve
+
+    lib = _lib.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    R, rate, maxiters, seed = 48, 16.0, 100, 0
+    reqs = serve_requests(R, seed)
+    steps_total = sum(len(r[3]) - 1 for r in reqs)
+    plain_t = []
+    for (nm, p, y0, ts, q, tol) in reqs:
+        prep = pbatch.prepare_batch([(nm, p, y0, ts)], q, device=dev)
+        n, D, d = int(prep["n_steps"][0]), prep["D"], prep["d"]
+        m = prep["means0"].clone()
+        c = torch.empty((n + 1, D, D), dtype=torch.float64, device=dev)
+        inf = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+        wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+        ws = _lib.workspace(wsb, dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.check(lib.pof_ieks_solve(_lib.POF_F64, n, D, d, int(prep["fields"][0]), _lib.ptr(prep["params"][0]),
+                                      float(prep["h"][0]), _lib.ptr(prep["x0m"][0]), _lib.ptr(prep["x0L"][0]),
+                                      _lib.ptr(prep["F"]), _lib.ptr(prep["QL"]), _lib.ptr(m), _lib.ptr(c),
+                                      maxiters, 1, _lib.ptr(inf), _lib.ptr(ws), wsb, _lib.stream_handle()),
+                   "pof_ieks_solve")
+        torch.cuda.synchronize()
+        plain_t.append(time.perf_counter() - t0)
+        del ws, m, c
+    srv = serve.Server(max_requests=256, max_points=1 << 21, device=dev)
+    for r in reqs[:6]:  # engines built and warmed
+        nm, p, y0, ts, q, tol = r
+        srv.submit(nm, p, y0, ts[: min(len(ts), 300)], q, rtol=tol, maxiters=maxiters)
+    while srv.busy():
+        srv.tick()
+    srv.results.clear()
+    arrivals = np.cumsum(np.random.default_rng(seed + 1000).exponential(1.0 / rate, size=R))
+    fin, lat_plain = 0.0, []
+    for a, t in zip(arrivals, plain_t):
+        fin = max(a, fin) + t
+        lat_plain.append(fin - a)
+    t_start = time.perf_counter()
+    rid_of, k = {}, 0
+    while k < R or srv.busy():
+        now = time.perf_counter() - t_start
+        while k < R and arrivals[k] <= now:
+            nm, p, y0, ts, q, tol = reqs[k]
+            rid_of[srv.submit(nm, p, y0, ts, q, rtol=tol, maxiters=maxiters, t_arrival=t_start + arrivals[k])] = k
+            k += 1
+        if srv.busy():
+            srv.tick()
+        elif k < R:
+            time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t_start))))
+    lat = [srv.t_done[rid] - srv.t_submit[rid] for rid in rid_of]
+    statuses = [srv.result(rid)[1]["status"] for rid in rid_of]
+    makespan = max(srv.t_done[rid] for rid in rid_of) - (t_start + arrivals[0])
+    srv.close()
+    return {"workload": "%d requests at %.0f/s (Poisson), logistic / FitzHugh-Nagumo / Lotka-Volterra / Van der Pol "
+                        "mu = 10, +-20 %% parameters, N log-uniform in [2^8, 2^16], q in {2, 3, 4}, tolerance in "
+                        "{1e-4, 1e-6}, maxiters %d" % (R, rate, maxiters, maxiters),
+            "served": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                       "ivp_steps_per_s": steps_total / makespan, "makespan_s": makespan,
+                       "status_counts": {s: statuses.count(s) for s in sorted(set(statuses))}},
+            "plain_fifo": {"p50_s": float(np.percentile(lat_plain, 50)), "p99_s": float(np.percentile(lat_plain, 99)),
+                           "ivp_steps_per_s": steps_total / (fin - arrivals[0])},
+            "omitted": "reaction-diffusion d = 128 requests (the dense D >= 128 path is not built)"}
 
 
 # ---------------------------------------------------------------------------
@@ -1137,6 +1450,8 @@ def main():
                     + sorted(MIXED_WORKLOADS) + sorted(SWEEP_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default line without its config0 / batched / served blocks")
     ap.add_argument("--f32-settle", type=float, default=0.1,
                     help="mixed precision: count non-shrinking float32 changes only once the smallest change is "
                          "below this (inf: from the first iteration, the library's default)")
