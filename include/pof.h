@@ -277,6 +277,17 @@ int pof_linear_filtsmooth_noalloc(int32_t dtype, int64_t n_steps, int32_t D, int
                                   const void* H, const void* c, const void* R, int64_t r_stride, void* out_mean,
                                   void* out_chol, double* out_scalars, void* stream);
 
+/* Runtime bounds checks (the substitute for a memory sanitizer).  A build
+ * with -DPOF_CHECKS (pof._build.build(checks=True): libpof_checked.so)
+ * tests the element, step and problem indices of the global accesses the
+ * kernels derive from sizes and plan tables; a failing check skips its
+ * access and records the source line (in csrc) of the first failure.
+ * pof_checks_compiled: 1 in such a build, else 0.  pof_checks_read: that
+ * line (0: no failure; always 0 in the normal build), cleared when `reset`.
+ * Waits for the device.  No reference counterpart. */
+int pof_checks_compiled(void);
+int pof_checks_read(uint64_t* line_out, int32_t reset);
+
 /* Per-kernel timing.  When enabled, every libpof launch is bracketed by CUDA
  * events on its stream; pof_profile_read waits for them and returns the
  * summed milliseconds and launch counts per kernel kind (POF_PK_*), in

@@ -155,6 +155,7 @@ struct BatchCtx {
     v.ce = reinterpret_cast<const int64_t*>(lw + L.ce);
     v.cp = reinterpret_cast<const int32_t*>(lw + L.cp);
     v.n = P.G;
+    v.nb = B;
     v.n1 = L.cnt[1];
     v.Ba = L.Ba;
     v.C0 = L.C0max;

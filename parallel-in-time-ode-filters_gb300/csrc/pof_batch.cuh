@@ -26,6 +26,7 @@ struct BView {
   const int64_t* maxit;   // (B) maxiters per problem, or null (a shared value)
   const volatile int32_t* cancel;  // (B) host-set cancel flags (mapped host memory), or null
   int64_t n;              // grid points of the index space (SoA stride of the smoother elements)
+  int64_t nb;             // problem slots of the index space (bound of every problem index)
   int64_t n1;             // level-0 chunks
   int64_t Ba;             // problems of the plan
   int C0;                 // longest chunk
@@ -65,9 +66,9 @@ __global__ void kb_linearize(BView v, const T* __restrict__ params, const T* __r
   const int64_t t = i / v.C0;
   if (t >= v.n1) return;
   const int b = v.cp[t];
-  if (v.frozen[b]) return;
+  if (!POF_IN(b, v.nb) || v.frozen[b]) return;
   const int64_t s = v.cs[t] + i % v.C0;
-  if (s >= v.ce[t]) return;
+  if (s >= v.ce[t] || !POF_IN(s + 1, v.n)) return;
   const T p0 = (T)v.p01[2 * b], p1 = (T)v.p01[2 * b + 1];
   const T* m = means + (s + 1) * D;
   T y[DY], f[DY], J[DY * DY];
@@ -115,6 +116,7 @@ __global__ void kb_filt_l0_reduce(BView v, const T* __restrict__ F, const T* __r
     w.eta[i] = T(0);
   }
   for (int64_t s = s0; s < s1; ++s) {
+    if (!POF_IN(s, v.n)) break;
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     tm.sync();
     t_cond_fold_step<T, TS, D, DY>(tm, w, fq.F, fq.QL, StepStruct{fq.wq, fq.wf, true});
@@ -217,6 +219,7 @@ __global__ void kb_filt_l0_down(BView v, const T* __restrict__ F, const T* __res
   }
   double ssq = 0.0, nll = 0.0, fobj = 0.0;
   for (int64_t s = s0; s < s1; ++s) {
+    if (!POF_IN(s + 1, v.n)) break;  // writes grid point s + 1
     t_load_step<T, TS, D, DY>(tm, w, H + s * DY * D, c + s * DY, nullptr);
     for (int i = tm.r; i < D; i += TS) ws_.mold[i] = w.m[i];
     tm.sync();
@@ -372,6 +375,7 @@ __global__ void kb_smo_l0_down(BView v, const T* __restrict__ F, const T* __rest
       for (int f = tm.r; f < D * D; f += TS) chols[g * D * D + f] = w.D1[(f / D) * L1 + f % D] * sc;
   }
   for (int64_t k = s1 - 1; k >= s0; --k) {
+    if (!POF_IN(k, v.n)) break;
     for (int i = tm.r; i < D; i += TS) ws_.mnext[i] = w.g1[i];
     t_load_smo<T, TS, D>(tm, selems, v.n, k, w.g2, w.E2, w.D2m);
     tm.sync();

@@ -151,7 +151,40 @@ void prof_end(int kind, cudaStream_t st) {
 }
 }  // namespace pof
 
+#ifdef POF_CHECKS
+namespace pof {
+__device__ unsigned long long pof_check_line = 0;
+}
+#endif
+
 extern "C" {
+
+int pof_checks_compiled(void) {
+#ifdef POF_CHECKS
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+int pof_checks_read(uint64_t* line_out, int32_t reset) {
+  if (!line_out) return POF_ERR_ARG;
+  *line_out = 0;
+#ifdef POF_CHECKS
+  unsigned long long v = 0;
+  int rc = cuda_status(cudaMemcpyFromSymbol(&v, pof::pof_check_line, sizeof(v)));
+  if (rc) return rc;
+  *line_out = v;
+  if (reset) {
+    const unsigned long long zero = 0;
+    rc = cuda_status(cudaMemcpyToSymbol(pof::pof_check_line, &zero, sizeof(zero)));
+    if (rc) return rc;
+  }
+#else
+  (void)reset;
+#endif
+  return POF_OK;
+}
 
 // FP64 FMA throughput probe: 8 independent dependency chains per thread.
 __global__ void k_fp64_probe(int64_t iters, double* sink) {

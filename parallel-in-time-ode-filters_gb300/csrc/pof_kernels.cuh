@@ -168,6 +168,7 @@ __global__ void __launch_bounds__(64) k_filt_l0_reduce(int64_t n, int C0, StepMo
 #pragma unroll
     for (int i = 0; i < D; ++i) A[i * D + i] = T(1);
     for (int64_t s = s0; s < s1; ++s) {
+      if (!POF_IN(s, n)) break;
       StepView<T, D, DY> v(sm, s);
       cond_fold_step<T, D, DY>(v.F, v.QL, v.H, v.c, v.R, A, b, U, eta, Z);
     }
@@ -268,6 +269,7 @@ __global__ void __launch_bounds__(64) k_filt_l0_down(int64_t n, int C0, StepMode
   double ssq = 0.0, nll = 0.0, fobj = 0.0;
   T ge[GL::NG];
   for (int64_t s = s0; s < s1; ++s) {
+    if (!POF_IN(s, n)) break;
     StepView<T, D, DY> v(sm, s);
     T mold[D];
     ld<T, D>(m, mold);
@@ -397,6 +399,7 @@ __global__ void __launch_bounds__(64) k_smo_l0_down(int64_t n, int C0, const T* 
   }
   T ge[GL::NG];
   for (int64_t k = s1 - 1; k >= s0; --k) {
+    if (!POF_IN(k, n)) break;
     T mnext[D];
     ld<T, D>(m, mnext);
     ld_soa<T, GL::NG>(selems, n, k, ge);

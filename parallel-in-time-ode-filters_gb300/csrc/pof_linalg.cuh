@@ -19,6 +19,26 @@
 namespace pof {
 
 // ---------------------------------------------------------------------------
+// Runtime bounds checks (the sanitizer substitute): compiled in with
+// -DPOF_CHECKS (a build with relocatable device code, so every translation
+// unit shares one device word), they test the global-memory indices the
+// kernels derive from sizes and plan tables -- element, step and problem
+// indices -- before the access.  A failing check skips its access and
+// records the source line of the first failure in pof_check_line
+// (pof_checks_read).  In the normal build every check is the constant true.
+// ---------------------------------------------------------------------------
+#ifdef POF_CHECKS
+extern __device__ unsigned long long pof_check_line;
+__device__ __forceinline__ bool pof_check_fail(int line) {
+  atomicCAS(&pof_check_line, 0ull, (unsigned long long)line);
+  return false;
+}
+#define POF_IN(i, n) (((i) >= 0 && (i) < (n)) ? true : ::pof::pof_check_fail(__LINE__))
+#else
+#define POF_IN(i, n) true
+#endif
+
+// ---------------------------------------------------------------------------
 // Reciprocal and reciprocal square root of a double, for the scalars of the
 // Householder reflectors and the diagonal solves.
 //

@@ -278,6 +278,7 @@ int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_po
   v.maxit = reinterpret_cast<const int64_t*>(x + s->X.maxit);
   v.cancel = s->d_cancel;
   v.n = max_points;
+  v.nb = max_requests;
   s->bufs[0] = x + s->X.means;
   s->bufs[1] = w + P.means2;
   *out = s;

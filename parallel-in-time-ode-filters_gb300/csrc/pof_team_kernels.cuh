@@ -26,6 +26,7 @@ struct TeamBlock {
 template <typename T, int TS, int D>
 __device__ __forceinline__ void t_load_filt(const Team<TS>& tm, const T* base, int64_t n, int64_t e, T* A, T* b,
                                             T* U, T* eta, T* Z) {
+  if (!POF_IN(e, n)) return;
   using FL = FiltLayout<D>;
   constexpr int L1 = Ld<D>::v;
   for (int f = tm.r; f < FL::NF; f += TS) {
@@ -46,6 +47,7 @@ __device__ __forceinline__ void t_load_filt(const Team<TS>& tm, const T* base, i
 template <typename T, int TS, int D>
 __device__ __forceinline__ void t_store_filt(const Team<TS>& tm, T* base, int64_t n, int64_t e, const T* A,
                                              const T* b, const T* U, const T* eta, const T* Z) {
+  if (!POF_IN(e, n)) return;
   using FL = FiltLayout<D>;
   constexpr int L1 = Ld<D>::v;
   for (int f = tm.r; f < FL::NF; f += TS) {
@@ -67,6 +69,7 @@ __device__ __forceinline__ void t_store_filt(const Team<TS>& tm, T* base, int64_
 // state (m, L) <-> slot
 template <typename T, int TS, int D>
 __device__ __forceinline__ void t_load_state(const Team<TS>& tm, const T* base, int64_t n, int64_t e, T* m, T* L) {
+  if (!POF_IN(e, n)) return;
   constexpr int L1 = Ld<D>::v;
   for (int f = tm.r; f < D + D * D; f += TS) {
     const T v = base[f * n + e];
@@ -79,6 +82,7 @@ __device__ __forceinline__ void t_load_state(const Team<TS>& tm, const T* base, 
 template <typename T, int TS, int D>
 __device__ __forceinline__ void t_store_state(const Team<TS>& tm, T* base, int64_t n, int64_t e, const T* m,
                                               const T* L) {
+  if (!POF_IN(e, n)) return;
   constexpr int L1 = Ld<D>::v;
   for (int f = tm.r; f < D + D * D; f += TS) base[f * n + e] = (f < D) ? m[f] : L[((f - D) / D) * L1 + (f - D) % D];
 }
@@ -97,6 +101,7 @@ __device__ __forceinline__ void t_load_state_plain(const Team<TS>& tm, const T* 
 template <typename T, int TS, int D>
 __device__ __forceinline__ void t_load_smo(const Team<TS>& tm, const T* base, int64_t n, int64_t e, T* g, T* E,
                                            T* Dm) {
+  if (!POF_IN(e, n)) return;
   using GL = SmoLayout<D>;
   constexpr int L1 = Ld<D>::v;
   for (int f = tm.r; f < GL::NG; f += TS) {
@@ -112,6 +117,7 @@ __device__ __forceinline__ void t_load_smo(const Team<TS>& tm, const T* base, in
 template <typename T, int TS, int D>
 __device__ __forceinline__ void t_store_smo(const Team<TS>& tm, T* base, int64_t n, int64_t e, const T* g,
                                             const T* E, const T* Dm) {
+  if (!POF_IN(e, n)) return;
   using GL = SmoLayout<D>;
   constexpr int L1 = Ld<D>::v;
   for (int f = tm.r; f < GL::NG; f += TS) {
@@ -534,6 +540,7 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
   if (t == 0) {
     t_load_state_plain<T, TS, D>(tm, x0m, x0L, w.m, w.L);
     for (int64_t s = s0; s < s1; ++s) {
+      if (!POF_IN(s, n)) break;
       fq_step<PS, T, TS, D>(tm, fq, sm, s, false, D / DY);
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
@@ -554,6 +561,7 @@ __global__ void k_filt_l0_reduce_team(int64_t n, int C0, StepModel sm, const T* 
       w.eta[i] = T(0);
     }
     for (int64_t s = s0; s < s1; ++s) {
+      if (!POF_IN(s, n)) break;
       fq_step<PS, T, TS, D>(tm, fq, sm, s, false, D / DY);
       StepView<T, D, DY> v(sm, s);
       t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
@@ -591,6 +599,7 @@ __global__ void k_filt_l0_down_team(int64_t n, int C0, StepModel sm, const T* __
   }
   double ssq = 0.0, nll = 0.0, fobj = 0.0;
   for (int64_t s = s0; s < s1; ++s) {
+    if (!POF_IN(s, n)) break;
     fq_step<PS, T, TS, D>(tm, fq, sm, s, true, D / DY);
     StepView<T, D, DY> v(sm, s);
     t_load_step<T, TS, D, DY>(tm, w, v.H, v.c, v.R);
@@ -663,6 +672,7 @@ __global__ void k_smo_l0_down_team(int64_t n, int C0, const T* __restrict__ F, c
       for (int f = tm.r; f < D * D; f += TS) chols[n * D * D + f] = w.D1[(f / D) * L1 + f % D] * sc;
   }
   for (int64_t k = s1 - 1; k >= s0; --k) {
+    if (!POF_IN(k, n)) break;
     fq_step<PS, T, TS, D>(tm, fq, sm, k, true, 0);
     for (int i = tm.r; i < D; i += TS) ws_.mnext[i] = w.g1[i];
     t_load_smo<T, TS, D>(tm, selems, n, k, w.g2, w.E2, w.D2m);

@@ -19,8 +19,13 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(ROOT, "csrc")
 BUILD = os.path.join(ROOT, "_build")
+BUILD_CHECKED = os.path.join(ROOT, "_build_checked")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 LIB = os.path.join(PKG_DIR, "libpof.so")
+# the same sources with the runtime bounds checks (POF_CHECKS; relocatable
+# device code, so every unit shares the check word)
+LIB_CHECKED = os.path.join(PKG_DIR, "libpof_checked.so")
+CHECK_FLAGS = ["-DPOF_CHECKS", "-rdc=true"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
@@ -42,41 +47,47 @@ def _deps():
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
-def up_to_date():
-    if not os.path.exists(LIB):
+def up_to_date(lib=LIB):
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(p) <= t for p in _deps())
 
 
-def _compile(src):
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-    cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+def _compile(src, build_dir=BUILD, extra=()):
+    obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
+    cmd = [nvcc()] + NVCC_FLAGS + list(extra) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-4000:]))
     return obj
 
 
-def build(force=False, jobs=None, verbose=True):
-    """Compile every CUDA source and link libpof.so; returns its path."""
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, jobs=None, verbose=True, checks=False):
+    """Compile every CUDA source and link libpof.so (checks=True:
+    libpof_checked.so, with the runtime bounds checks); returns its path."""
+    lib = LIB_CHECKED if checks else LIB
+    build_dir = BUILD_CHECKED if checks else BUILD
+    extra = CHECK_FLAGS if checks else []
+    if not force and up_to_date(lib):
+        return lib
+    os.makedirs(build_dir, exist_ok=True)
     srcs = sources()
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 1))
     if verbose:
-        print("[pof build] nvcc %d units, %d jobs" % (len(srcs), jobs), file=sys.stderr)
+        print("[pof build] nvcc %d units, %d jobs%s" % (len(srcs), jobs, " (bounds checks)" if checks else ""),
+              file=sys.stderr)
     with cf.ThreadPoolExecutor(jobs) as ex:
-        objs = list(ex.map(_compile, srcs))
-    tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"]
+        objs = list(ex.map(lambda src: _compile(src, build_dir, extra), srcs))
+    tmp = lib + ".tmp"
+    # relocatable device code is device-linked here
+    cmd = [nvcc(), "-shared"] + ARCH + (["-rdc=true"] if checks else []) + ["-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv))
+    print(build(force="--force" in sys.argv, checks="--checks" in sys.argv))

@@ -92,6 +92,8 @@ _SIGS = {
         [_i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _f64, _f64, _i64, _i32, _dp, _vp, _sz,
          _vp],
     ),
+    "pof_checks_compiled": (_c.c_int, []),
+    "pof_checks_read": (_c.c_int, [_vp, _i32]),
     "pof_profile_enable": (None, [_i32]),
     "pof_profile_read": (_c.c_int, [_vp, _vp, _i32, _i32]),
     "pof_fp64_probe": (_c.c_int, [_i64, _i32, _i32, _dp, _vp]),
@@ -140,6 +142,16 @@ def profile_read(reset=True):
     return {k: (ms[i], cnt[i]) for i, k in enumerate(PROFILE_KINDS)}
 
 
+def load(path):
+    """A libpof build at `path` with the C ABI's signatures set (ctypes)."""
+    l = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(l, name)
+        fn.restype = res
+        fn.argtypes = args
+    return l
+
+
 def lib():
     """The loaded libpof.so (raises if it was not built)."""
     global _lib
@@ -149,12 +161,7 @@ def lib():
                 "libpof.so not found at %s; build it with `python -m pof._build` "
                 "(or __graft_entry__.build())" % LIB_PATH
             )
-        l = ctypes.CDLL(LIB_PATH)
-        for name, (res, args) in _SIGS.items():
-            fn = getattr(l, name)
-            fn.restype = res
-            fn.argtypes = args
-        _lib = l
+        _lib = load(LIB_PATH)
     return _lib
 
 
