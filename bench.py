@@ -1088,31 +1088,37 @@ def cpu_sample_batch(problems, q, its, budget_s=20.0):
 # ---------------------------------------------------------------------------
 
 SWEEP_WORKLOADS = {
-    # name: (cases (field, kwargs, t1 or None for the IVP's own span, q, N values), largest N of the
-    # sequential pass, maxiters)
-    "scan_sweep": ([("logistic", {"r": 3.0}, 10.0, q, [2**10, 2**12, 2**14, 2**16, 2**18, 2**20]) for q in (1, 2, 3, 5)]
-                   + [("fhn_classic", {}, 100.0, 3, [2**10, 2**12, 2**14, 2**16])], 2**14, MAXITERS),
+    # name: (cases (field, kwargs, t1 or None for the IVP's own span, q, N values, largest N of the
+    # sequential solves), unused, maxiters)
+    "scan_sweep": ([("logistic", {"r": 3.0}, 10.0, q, [2**10, 2**12, 2**14, 2**16, 2**18, 2**20], 2**14)
+                    for q in (1, 2, 3, 5)]
+                   + [("fhn_classic", {}, 100.0, q, [2**10, 2**12, 2**14, 2**16], 2**10) for q in (1, 2, 3, 5)],
+                   None, MAXITERS),
     # the rows of the reference's published V100 benchmark (pof.ivp default problems, constant init,
     # maxiters 1000) that fit the compiled shapes
-    "v100_table": ([("logistic", {}, None, 3, [2**10, 2**14, 2**19]),
-                    ("fitzhughnagumo", {}, None, 3, [2**10, 2**14, 2**19]),
-                    ("vanderpol", {"stiffness_constant": 1.0}, None, 3, [2**19]),
-                    ("henonheiles", {}, None, 1, [2**19])], 0, 1000),
+    "v100_table": ([("logistic", {}, None, 3, [2**10, 2**14, 2**19], 0),
+                    ("fitzhughnagumo", {}, None, 3, [2**10, 2**14, 2**19], 0),
+                    ("vanderpol", {"stiffness_constant": 1.0}, None, 3, [2**19], 0),
+                    ("rigid_body", {}, None, 3, [2**19], 0),
+                    ("henonheiles", {}, None, 1, [2**19], 0)], None, 1000),
 }
 
 
 def run_sweep(args, workload):
-    """Wall time (device synchronized on both sides) of one full parallel
-    IEKS solve (pof.solver.solve, the reference's criterion) and of one
-    sequential extended Kalman smoother pass (pof.solver.sequential_eks_solve,
-    one GPU thread running the square-root EKF + RTS recursion) per (IVP, q,
-    N).  The sequential pass is one linearization, not an iterated solve."""
+    """Wall time (device synchronized on both sides) per (IVP, q, N), one IVP
+    per launch: the full parallel IEKS solve (pof.solver.solve, the
+    reference's criterion), the full sequential IEKS solve on the same GPU
+    (solve(sequential=True): the same loop with the square-root Kalman
+    filter and RTS smoother run step after step by one team of the level-0
+    kernels over a chunk spanning the grid) and one sequential extended
+    Kalman smoother pass (pof.solver.sequential_eks_solve, one GPU thread
+    running the EKF + RTS recursion; one linearization, not a solve)."""
     import torch
 
     from pof import _build, ivp as pivp, solver as psolver
 
     _build.build(verbose=False)
-    cases, seq_max, maxiters = SWEEP_WORKLOADS[workload]
+    cases, _, maxiters = SWEEP_WORKLOADS[workload]
     rows = []
 
     def wall(fn):
@@ -1122,7 +1128,7 @@ def run_sweep(args, workload):
         torch.cuda.synchronize()
         return time.perf_counter() - t0, out
 
-    for name, kw, t1, q, Ns in cases:
+    for name, kw, t1, q, Ns, seq_max in cases:
         p = getattr(pivp, name)(**kw)
         for N in Ns:
             ts = np.linspace(p.t0, p.tmax, N) if t1 is None else np.linspace(0.0, t1, N)
@@ -1131,16 +1137,25 @@ def run_sweep(args, workload):
                 wall(par)
             tp, (_, info) = wall(par)
             it = int(info["iterations"])
-            row = {"ivp": name, "q": q, "N": N, "parallel_ieks_ms": tp * 1e3, "iterations": it,
-                   "parallel_ms_per_iteration": tp * 1e3 / max(it, 1)}
+            row = {"ivp": name, "q": q, "D": int(p.y0.shape[0]) * (q + 1), "N": N, "parallel_ieks_ms": tp * 1e3,
+                   "iterations": it, "parallel_ms_per_iteration": tp * 1e3 / max(it, 1),
+                   "status": int(info["status"])}
             if N <= seq_max:
-                seq = lambda: psolver.sequential_eks_solve(f=p.f, y0=p.y0, ts=ts, order=q)  # noqa: E731
-                wall(seq)
-                tsq, _ = wall(seq)
-                row["sequential_eks_ms"] = tsq * 1e3
-                row["parallel_iteration_vs_sequential_pass"] = row["parallel_ms_per_iteration"] / (tsq * 1e3)
+                sq = lambda: psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant",  # noqa: E731
+                                           maxiters=maxiters, sequential=True)
+                tsi, (_, sinfo) = wall(sq)
+                sit = int(sinfo["iterations"])
+                row.update({"sequential_ieks_ms": tsi * 1e3, "sequential_iterations": sit,
+                            "sequential_ms_per_iteration": tsi * 1e3 / max(sit, 1),
+                            "parallel_speedup_per_iteration": (tsi / max(sit, 1)) / (tp / max(it, 1))})
+                eks = lambda: psolver.sequential_eks_solve(f=p.f, y0=p.y0, ts=ts, order=q)  # noqa: E731
+                wall(eks)
+                te, _ = wall(eks)
+                row["sequential_eks_pass_ms"] = te * 1e3
             rows.append(row)
-    jprint({"metric": "ms per solve, parallel IEKS vs sequential EKS pass (float64, one IVP per launch)",
+            print(json.dumps(row), file=sys.stderr, flush=True)
+    jprint({"metric": "ms per solve and per IEKS iteration, parallel vs sequential IEKS on the same GPU (float64, "
+                      "one IVP per launch)",
             "value": None, "unit": "ms", "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
             "data": "synthetic", "config": {"workload": workload, "init": "constant", "maxiters": maxiters,
                                             "timing": "wall clock, device synchronized, 1 warm-up for N <= 2^16"},

@@ -381,6 +381,27 @@ int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_po
                       const double* F, const double* QL, int32_t calibrate, void* workspace, size_t workspace_bytes,
                       pof_server** out);
 int pof_server_destroy(pof_server* s);
+
+/* The engine with float32 bulk iterations and float64 polish per request
+ * (no reference counterpart): every admitted request first runs float32 IEKS
+ * iterations -- float64 EK1 linearization at its float64 iterate, float32
+ * filter/smoother, the change judged in float64 -- under the float32-phase
+ * rules of pof_ieks_solve_batch_mixed (maxiters_f32, rtol_f32, settle_f32,
+ * the same discard rule), then the float64 loop with its own maxiters and
+ * rtol, as on pof_server_create's engine.  Both phases of all requests run
+ * in the same ticks.  A request's result is that of
+ * pof_ieks_solve_batch_mixed with C0 = its own chunk length, alone and in
+ * any mix.  Workspace from pof_server_mixed_workspace_bytes. */
+size_t pof_server_mixed_workspace_bytes(int32_t D, int32_t d, int64_t max_requests, int64_t max_points,
+                                        size_t level_bytes);
+int pof_server_create_mixed(int32_t D, int32_t d, int64_t max_requests, int64_t max_points, size_t level_bytes,
+                            const double* F, const double* QL, int32_t calibrate, int64_t maxiters_f32,
+                            double rtol_f32, double settle_f32, void* workspace, size_t workspace_bytes,
+                            pof_server** out);
+/* A finished request of a mixed engine (before pof_server_fetch): device
+ * array info_f32 (2 doubles) <- the float32 iterations it kept and the
+ * smallest relative change its float32 phase reached. */
+int pof_server_mixed_info(pof_server* s, int64_t slot, double* info_f32);
 /* Admit a request (host arrays): field, params (4), step h, x0 (D) and its
  * chol (D, D, NULL = 0) in preconditioned coordinates, the initial
  * trajectory's row (D, repeated over the N = n_steps + 1 grid points:

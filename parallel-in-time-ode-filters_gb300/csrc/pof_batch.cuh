@@ -627,7 +627,7 @@ static __global__ void kb_ctl32(BView v, double* __restrict__ mst, int32_t* __re
   const int b = v.ap[k];
   if (done32[b]) return;
   double* m = mst + (int64_t)M_COUNT * b;
-  if (m[M_BAD] != 0.0) {
+  if (m[M_BAD] != 0.0 || (v.cancel && v.cancel[b] != 0)) {  // non-finite candidate, or a cancelled request
     m[M_ACCEPT] = 0.0;
     done32[b] = 1;
     return;

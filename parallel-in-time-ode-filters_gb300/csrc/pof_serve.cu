@@ -116,9 +116,79 @@ __global__ void ks_fetch(int32_t b, int parity0, const int64_t* __restrict__ gb,
 
 struct Slot {
   bool used = false, finished = false;
+  bool phase32 = false;  // in its float32 phase (mixed-precision engine)
   int64_t g0 = 0, ns = 0;
   int parity0 = 0;
 };
+
+// Workspace of a mixed-precision engine after the float64 engine's: the
+// float32 batch state (persistent part and a level part of the same cap),
+// float32 chols and copies of x0, F, QL, the float64 iterate of the requests
+// in their float32 phase (mcur), their input trajectories (keep, for the
+// discard rule) and the per-request float32-phase state (mst).
+struct MixedServe {
+  BatchPersist P32;
+  size_t p32, lw32, chols32, x0m32, x0L32, F32, QL32, mcur, keep, mst, total;
+};
+
+MixedServe mixed_serve_layout(int D, int d, int64_t maxB, int64_t maxG, size_t level_cap) {
+  MixedServe m;
+  m.P32 = batch_persist(maxB, maxG, D, d, 4);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes);
+    return o;
+  };
+  m.p32 = take(m.P32.total);
+  m.lw32 = take(level_cap);
+  m.chols32 = take(sizeof(float) * D * D * maxG);
+  m.x0m32 = take(sizeof(float) * D * maxB);
+  m.x0L32 = take(sizeof(float) * D * D * maxB);
+  m.F32 = take(sizeof(float) * D * D);
+  m.QL32 = take(sizeof(float) * D * D);
+  m.mcur = take(sizeof(double) * D * maxG);
+  m.keep = take(sizeof(double) * D * maxG);
+  m.mst = take(sizeof(double) * M_COUNT * maxB);
+  m.total = off;
+  return m;
+}
+
+// A request of a mixed-precision engine starts in its float32 phase: its
+// float64 iterate (mcur) and the copy the discard rule returns to (keep)
+// get the initial rows, x0 goes to float32, its float32-phase state is
+// reset, and the float64 plan skips it (frozen) until the phase ends.
+__global__ void ks_admit_mixed(int32_t b, const AdmitBlock* __restrict__ blk, const double* __restrict__ rows, int D,
+                               double* mcur, double* keep, float* x0m32, float* x0L32, double* mst, int32_t* done32,
+                               int32_t* frozen64) {
+  const AdmitBlock& a = *blk;
+  const int64_t N = a.ns + 1;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N * D; i += (int64_t)gridDim.x * blockDim.x) {
+    mcur[a.gb * D + i] = rows[i % D];
+    keep[a.gb * D + i] = rows[i % D];
+  }
+  if (blockIdx.x != 0) return;
+  for (int i = threadIdx.x; i < D; i += blockDim.x) x0m32[(int64_t)b * D + i] = (float)rows[D + i];
+  for (int i = threadIdx.x; i < D * D; i += blockDim.x) x0L32[(int64_t)b * D * D + i] = (float)rows[2 * D + i];
+  for (int f = threadIdx.x; f < M_COUNT; f += blockDim.x)
+    mst[(int64_t)M_COUNT * b + f] = (f == M_BEST || f == M_PREV) ? 1e300 : 0.0;
+  if (threadIdx.x == 0) {
+    done32[b] = 0;
+    frozen64[b] = 1;
+  }
+}
+
+static __global__ void ks_d2f(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
+static __global__ void ks_mixed_info(const double* __restrict__ mst, int32_t b, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    out[0] = mst[(int64_t)M_COUNT * b + M_IT];
+    out[1] = mst[(int64_t)M_COUNT * b + M_BEST];
+  }
+}
 
 }  // namespace
 
@@ -151,12 +221,71 @@ struct pof_server {
   int cur = 0;  // bufs[cur] holds the current iterates
   bool dirty = true;
   int64_t ticks = 0;
+  // mixed precision: requests start with float32 IEKS iterations (the rules
+  // of pof_ieks_solve_batch_mixed's float32 phase), then go on in float64
+  bool mixed = false;
+  int64_t maxiters_f32 = 0;
+  double rtol_f32 = 1e-5, settle_f32 = 1e300;
+  const BatchOps* ops32 = nullptr;
+  BatchShape sh32;
+  MixedServe M;
+  char* mw = nullptr;  // mixed part of the workspace
+  BatchRaw a32{};
+  BatchLevels L32;
+  std::vector<unsigned char> tab32;
+  std::vector<int32_t> active32, h_done32;
+
+  double* mcur() const { return reinterpret_cast<double*>(mw + M.mcur); }
+  double* mst() const { return reinterpret_cast<double*>(mw + M.mst); }
+
+  int replan32() {
+    active32.clear();
+    for (int64_t b = 0; b < maxB; ++b)
+      if (slots[b].used && !slots[b].finished && slots[b].phase32) active32.push_back((int32_t)b);
+    if (active32.empty()) return POF_OK;
+    L32 = batch_levels(sh32, active32, h_ns.data(), h_gb.data(), h_c0.data(), &tab32);
+    char* lw32 = mw + M.lw32;
+    int rc = cuda_status(cudaMemcpyAsync(lw32, tab32.data(), L32.tab_bytes, cudaMemcpyHostToDevice, st));
+    if (!rc) rc = cuda_status(cudaStreamSynchronize(st));
+    a32.L = &L32;
+    BView& v = a32.v;
+    v.ap = reinterpret_cast<const int32_t*>(lw32 + L32.ap);
+    v.pc = reinterpret_cast<const int64_t*>(lw32 + L32.pc);
+    v.cs = reinterpret_cast<const int64_t*>(lw32 + L32.cs);
+    v.ce = reinterpret_cast<const int64_t*>(lw32 + L32.ce);
+    v.cp = reinterpret_cast<const int32_t*>(lw32 + L32.cp);
+    v.n1 = L32.cnt[1];
+    v.Ba = L32.Ba;
+    v.C0 = L32.C0max;
+    return rc;
+  }
+
+  // One float32 iteration of every request in its float32 phase: float64
+  // linearization at its float64 iterate, float32 filter/smoother, the
+  // change judged in float64, the phase's stopping rules, kept candidates
+  // into the float64 iterate.
+  void tick32() {
+    BatchRaw& a = a32;
+    cudaMemsetAsync(a.nactive, 0, sizeof(int32_t), st);
+    ops32->lin_mixed(a.v, static_cast<const double*>(this->a.params), mcur(), static_cast<float*>(a.H),
+                     static_cast<float*>(a.c), st);
+    float* m32 = reinterpret_cast<float*>(mw + M.p32 + M.P32.means2);
+    ops32->filtsmooth(a, nullptr, m32, st);
+    ops32->ychange(a.v, m32, mcur(), mst(), st);
+    kb_ctl32<<<(unsigned)((a.v.Ba + 255) / 256), 256, 0, st>>>(a.v, mst(), a.frozen, maxiters_f32, rtol_f32,
+                                                                settle_f32, a.nactive);
+    ops32->accept(a.v, m32, mcur(), mst(), st);
+  }
 
   int replan() {
     active.clear();
     for (int64_t b = 0; b < maxB; ++b)
-      if (slots[b].used && !slots[b].finished) active.push_back((int32_t)b);
+      if (slots[b].used && !slots[b].finished && !slots[b].phase32) active.push_back((int32_t)b);
     dirty = false;
+    if (mixed) {
+      const int rc = replan32();
+      if (rc) return rc;
+    }
     if (active.empty()) return POF_OK;
     L = batch_levels(sh, active, h_ns.data(), h_gb.data(), h_c0.data(), &tab);
     int rc = cuda_status(cudaMemcpyAsync(lw, tab.data(), L.tab_bytes, cudaMemcpyHostToDevice, st));
@@ -184,16 +313,31 @@ size_t pof_server_workspace_bytes(int32_t D, int32_t d, int64_t max_requests, in
   return align_up(P.total) + align_up(level_bytes) + serve_extras(D, max_requests, max_points).total + 256;
 }
 
-int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_points, size_t level_bytes,
-                      const double* F, const double* QL, int32_t calibrate, void* workspace, size_t workspace_bytes,
-                      pof_server** out) {
+size_t pof_server_mixed_workspace_bytes(int32_t D, int32_t d, int64_t max_requests, int64_t max_points,
+                                        size_t level_bytes) {
+  const size_t base = pof_server_workspace_bytes(D, d, max_requests, max_points, level_bytes);
+  if (!base || !find_batch_shape(POF_F32, D, d)) return 0;
+  return base + mixed_serve_layout(D, d, max_requests, max_points, align_up(level_bytes)).total;
+}
+
+}  // extern "C"
+
+namespace {
+
+int server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_points, size_t level_bytes,
+                  const double* F, const double* QL, int32_t calibrate, bool mixed, int64_t maxiters_f32,
+                  double rtol_f32, double settle_f32, void* workspace, size_t workspace_bytes, pof_server** out) {
   if (!out || !F || !QL || !workspace) return POF_ERR_ARG;
   *out = nullptr;
   const BatchOps* ops = find_batch_shape(POF_F64, D, d);
   if (!ops) return POF_ERR_SHAPE;
+  const BatchOps* ops32 = mixed ? find_batch_shape(POF_F32, D, d) : nullptr;
+  if (mixed && !ops32) return POF_ERR_SHAPE;
   if (max_requests < 1 || max_requests > (int64_t)0x7fffffff || max_points < 2) return POF_ERR_ARG;
-  if (workspace_bytes < pof_server_workspace_bytes(D, d, max_requests, max_points, level_bytes))
-    return POF_ERR_WORKSPACE;
+  if (mixed && (maxiters_f32 < 0 || !(rtol_f32 > 0) || !(settle_f32 > 0))) return POF_ERR_ARG;
+  const size_t need = mixed ? pof_server_mixed_workspace_bytes(D, d, max_requests, max_points, level_bytes)
+                            : pof_server_workspace_bytes(D, d, max_requests, max_points, level_bytes);
+  if (workspace_bytes < need) return POF_ERR_WORKSPACE;
   pof_server* s = new pof_server();
   s->D = D;
   s->d = d;
@@ -281,8 +425,80 @@ int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_po
   v.nb = max_requests;
   s->bufs[0] = x + s->X.means;
   s->bufs[1] = w + P.means2;
+  if (mixed) {
+    s->mixed = true;
+    s->ops32 = ops32;
+    s->maxiters_f32 = maxiters_f32;
+    s->rtol_f32 = rtol_f32;
+    s->settle_f32 = settle_f32;
+    s->sh32 = s->sh;
+    s->sh32.esz = 4;
+    s->sh32.team = ops32->tsn;
+    s->sh32.team_up = ops32->tsw;
+    s->M = mixed_serve_layout(D, d, max_requests, max_points, s->level_cap);
+    s->mw = x + align_up(s->X.total);
+    s->h_done32.assign(max_requests, 1);
+    const MixedServe& M = s->M;
+    char* w32 = s->mw + M.p32;
+    BatchRaw& b = s->a32;
+    b.params = nullptr;  // the float64 parameters go to lin_mixed
+    b.x0m = s->mw + M.x0m32;
+    b.x0L = s->mw + M.x0L32;
+    b.F = s->mw + M.F32;
+    b.QL = s->mw + M.QL32;
+    b.H = w32 + M.P32.H;
+    b.c = w32 + M.P32.c;
+    b.selem = w32 + M.P32.selem;
+    b.chols = s->mw + M.chols32;
+    b.pscal = reinterpret_cast<double*>(w32 + M.P32.pscal);
+    b.pscale = reinterpret_cast<double*>(w32 + M.P32.pscale);
+    b.frozen = reinterpret_cast<int32_t*>(w32 + M.P32.frozen);  // the float32 phase is over (done32)
+    b.nactive = reinterpret_cast<int32_t*>(w32 + M.P32.nactive);
+    b.maxiters = 0;
+    b.rtol = 1e-6;
+    b.atol = 1e-9;
+    b.mrtol = 1e-13;
+    b.matol = 1e-8;
+    b.calibrate = false;
+    b.team = s->sh32.team;
+    b.lw = s->mw + M.lw32;
+    BView& u = b.v;
+    u = v;  // the float64 engine's per-request tables (offsets, fields, Nordsieck scales)
+    u.frozen = b.frozen;
+    u.rtol = nullptr;
+    u.maxit = nullptr;
+    const unsigned gq = (unsigned)((D * D + 255) / 256);
+    ks_d2f<<<gq, 256, 0, s->st>>>(F, reinterpret_cast<float*>(s->mw + M.F32), (int64_t)D * D);
+    ks_d2f<<<gq, 256, 0, s->st>>>(QL, reinterpret_cast<float*>(s->mw + M.QL32), (int64_t)D * D);
+    int rc2 = cuda_status(cudaMemsetAsync(b.frozen, 0xff, sizeof(int32_t) * max_requests, s->st));
+    if (!rc2) rc2 = launch_status();
+    if (!rc2) rc2 = cuda_status(cudaStreamSynchronize(s->st));
+    if (rc2) {
+      pof_server_destroy(s);
+      return rc2;
+    }
+  }
   *out = s;
   return POF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pof_server_create(int32_t D, int32_t d, int64_t max_requests, int64_t max_points, size_t level_bytes,
+                      const double* F, const double* QL, int32_t calibrate, void* workspace, size_t workspace_bytes,
+                      pof_server** out) {
+  return server_create(D, d, max_requests, max_points, level_bytes, F, QL, calibrate, false, 0, 1e-5, 1e300,
+                       workspace, workspace_bytes, out);
+}
+
+int pof_server_create_mixed(int32_t D, int32_t d, int64_t max_requests, int64_t max_points, size_t level_bytes,
+                            const double* F, const double* QL, int32_t calibrate, int64_t maxiters_f32,
+                            double rtol_f32, double settle_f32, void* workspace, size_t workspace_bytes,
+                            pof_server** out) {
+  return server_create(D, d, max_requests, max_points, level_bytes, F, QL, calibrate, true, maxiters_f32, rtol_f32,
+                       settle_f32, workspace, workspace_bytes, out);
 }
 
 int pof_server_destroy(pof_server* s) {
@@ -361,6 +577,14 @@ int64_t pof_server_submit(pof_server* s, int64_t n_steps, int32_t field, const d
       reinterpret_cast<double*>(x + s->X.x0L), reinterpret_cast<double*>(w + P.pscal),
       reinterpret_cast<double*>(w + P.pscale), reinterpret_cast<int32_t*>(w + P.frozen),
       static_cast<double*>(s->bufs[s->cur]));
+  const bool phase32 = s->mixed && s->maxiters_f32 > 0;
+  if (phase32) {
+    const MixedServe& M = s->M;
+    ks_admit_mixed<<<grid, 256, 0, s->st>>>(
+        (int32_t)b, reinterpret_cast<const AdmitBlock*>(x + s->X.admit), reinterpret_cast<const double*>(x + s->X.row),
+        D, s->mcur(), reinterpret_cast<double*>(s->mw + M.keep), reinterpret_cast<float*>(s->mw + M.x0m32),
+        reinterpret_cast<float*>(s->mw + M.x0L32), s->mst(), s->a32.frozen, reinterpret_cast<int32_t*>(w + P.frozen));
+  }
   rc = launch_status();
   // blk and rows are host memory of this frame, and the staging area is
   // reused by the next admission
@@ -376,7 +600,9 @@ int64_t pof_server_submit(pof_server* s, int64_t n_steps, int32_t field, const d
   sl.g0 = g0;
   sl.ns = n_steps;
   sl.parity0 = s->cur;
-  s->h_frozen[b] = 0;
+  sl.phase32 = phase32;
+  s->h_frozen[b] = phase32 ? 1 : 0;
+  if (phase32) s->h_done32[b] = 0;
   s->dirty = true;
   return b;
 }
@@ -388,9 +614,12 @@ int pof_server_launch(pof_server* s, int64_t iterations) {
       int rc = s->replan();
       if (rc) return rc;
     }
-    if (s->active.empty()) return POF_OK;
-    s->ops->iteration(s->a, s->bufs[s->cur], s->bufs[s->cur ^ 1], s->st);
-    s->cur ^= 1;
+    if (s->active.empty() && s->active32.empty()) return POF_OK;
+    if (!s->active32.empty()) s->tick32();
+    if (!s->active.empty()) {
+      s->ops->iteration(s->a, s->bufs[s->cur], s->bufs[s->cur ^ 1], s->st);
+      s->cur ^= 1;
+    }
     ++s->ticks;
   }
   return launch_status();
@@ -400,6 +629,9 @@ int pof_server_sync(pof_server* s, int64_t* n_running) {
   if (!s) return POF_ERR_ARG;
   int rc = cuda_status(cudaMemcpyAsync(s->h_frozen.data(), s->a.frozen, sizeof(int32_t) * s->maxB,
                                        cudaMemcpyDeviceToHost, s->st));
+  if (!rc && s->mixed)
+    rc = cuda_status(cudaMemcpyAsync(s->h_done32.data(), s->a32.frozen, sizeof(int32_t) * s->maxB,
+                                     cudaMemcpyDeviceToHost, s->st));
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s->st));
   if (rc) return rc;
   if (prof_on()) prof_flush();
@@ -407,6 +639,27 @@ int pof_server_sync(pof_server* s, int64_t* n_running) {
   for (int64_t b = 0; b < s->maxB; ++b) {
     Slot& sl = s->slots[b];
     if (!sl.used || sl.finished) continue;
+    if (sl.phase32) {
+      ++running;
+      if (!s->h_done32[b]) continue;
+      // float32 phase over: back to the input trajectory when float32 never
+      // came within 100 rtol_f32 (pof_ieks_solve_batch_mixed's discard
+      // rule), then the float64 iterations from the kept iterate
+      const MixedServe& M = s->M;
+      const int D = s->D;
+      s->ops32->revert(1, s->a.v.gb + b, s->a.v.ns + b, s->mst() + (int64_t)M_COUNT * b, s->rtol_f32,
+                       reinterpret_cast<const double*>(s->mw + M.keep), s->mcur(), s->st);
+      rc = cuda_status(cudaMemcpyAsync(static_cast<double*>(s->bufs[s->cur]) + sl.g0 * D, s->mcur() + sl.g0 * D,
+                                       sizeof(double) * D * (sl.ns + 1), cudaMemcpyDeviceToDevice, s->st));
+      if (!rc) rc = cuda_status(cudaMemsetAsync(s->a.frozen + b, 0, sizeof(int32_t), s->st));
+      if (!rc) rc = launch_status();
+      if (rc) return rc;
+      sl.phase32 = false;
+      sl.parity0 = s->cur;
+      s->h_frozen[b] = 0;
+      s->dirty = true;
+      continue;
+    }
     if (s->h_frozen[b]) {
       sl.finished = true;
       s->done.push_back(b);
@@ -459,6 +712,14 @@ int pof_server_fetch(pof_server* s, int64_t slot, double* means, double* chols, 
   sl = Slot();
   s->h_frozen[slot] = 1;
   return POF_OK;
+}
+
+int pof_server_mixed_info(pof_server* s, int64_t slot, double* info_f32) {
+  if (!s || !s->mixed || slot < 0 || slot >= s->maxB || !info_f32) return POF_ERR_ARG;
+  const Slot& sl = s->slots[slot];
+  if (!sl.used || !sl.finished) return POF_ERR_ARG;
+  ks_mixed_info<<<1, 32, 0, s->st>>>(s->mst(), (int32_t)slot, info_f32);
+  return launch_status();
 }
 
 void* pof_server_stream(pof_server* s) { return s ? static_cast<void*>(s->st) : nullptr; }

@@ -107,6 +107,10 @@ _SIGS = {
     "pof_server_workspace_bytes": (_sz, [_i32, _i32, _i64, _i64, _sz]),
     "pof_server_create": (_c.c_int, [_i32, _i32, _i64, _i64, _sz, _vp, _vp, _i32, _vp, _sz, _vp]),
     "pof_server_destroy": (_c.c_int, [_vp]),
+    "pof_server_mixed_workspace_bytes": (_sz, [_i32, _i32, _i64, _i64, _sz]),
+    "pof_server_create_mixed": (_c.c_int, [_i32, _i32, _i64, _i64, _sz, _vp, _vp, _i32, _i64, _f64, _f64, _vp, _sz,
+                                           _vp]),
+    "pof_server_mixed_info": (_c.c_int, [_vp, _i64, _dp]),
     "pof_server_submit": (_i64, [_vp, _i64, _i32, _vp, _f64, _vp, _vp, _vp, _i64, _f64]),
     "pof_server_launch": (_c.c_int, [_vp, _i64]),
     "pof_server_sync": (_c.c_int, [_vp, _vp]),

@@ -40,23 +40,35 @@ class Request(NamedTuple):
 class Engine:
     """One libpof engine: requests of state shape (D, d) = (d (q+1), d)."""
 
-    def __init__(self, d, q, max_requests, max_points, level_bytes=None, device=None, calibrate=True):
+    def __init__(self, d, q, max_requests, max_points, level_bytes=None, device=None, calibrate=True,
+                 precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, settle_f32=float("inf")):
         self.dev = device or default_device()
         self.d, self.q = d, q
         self.D = d * (q + 1)
+        self.mixed = precision == "mixed"
+        if precision not in ("float64", "mixed"):
+            raise ValueError("precision must be 'float64' or 'mixed'")
         lib = _lib.lib()
         if level_bytes is None:  # scan levels for chunks of >= 4 steps (about 56 D^2 bytes per chunk, x 2)
             level_bytes = 28 * self.D * self.D * max_points + (64 << 20)
-        wsb = lib.pof_server_workspace_bytes(self.D, d, max_requests, max_points, int(level_bytes))
+        query = lib.pof_server_mixed_workspace_bytes if self.mixed else lib.pof_server_workspace_bytes
+        wsb = query(self.D, d, max_requests, max_points, int(level_bytes))
         if wsb == 0:
             raise _lib.PofError("no batched kernels for (D, d) = (%d, %d)" % (self.D, d))
         self.ws = _lib.workspace(wsb, self.dev)
         F, QL = preconditioned_discretize(IWP(num_derivatives=q, wiener_process_dimension=d), device=self.dev)
         self.F, self.QL = F.contiguous(), QL.contiguous()
         h = ctypes.c_void_p()
-        _lib.check(lib.pof_server_create(self.D, d, max_requests, max_points, int(level_bytes), _lib.ptr(self.F),
-                                         _lib.ptr(self.QL), int(bool(calibrate)), _lib.ptr(self.ws), int(wsb),
-                                         ctypes.byref(h)), "pof_server_create")
+        if self.mixed:
+            settle = min(float(settle_f32), 1e300)
+            _lib.check(lib.pof_server_create_mixed(self.D, d, max_requests, max_points, int(level_bytes),
+                                                   _lib.ptr(self.F), _lib.ptr(self.QL), int(bool(calibrate)),
+                                                   int(maxiters_f32), float(rtol_f32), settle, _lib.ptr(self.ws),
+                                                   int(wsb), ctypes.byref(h)), "pof_server_create_mixed")
+        else:
+            _lib.check(lib.pof_server_create(self.D, d, max_requests, max_points, int(level_bytes),
+                                             _lib.ptr(self.F), _lib.ptr(self.QL), int(bool(calibrate)),
+                                             _lib.ptr(self.ws), int(wsb), ctypes.byref(h)), "pof_server_create")
         self.h = h
         self.slots = {}  # slot -> (request, p0)
         self.running = 0
@@ -124,7 +136,10 @@ class Engine:
                 N = len(req.ts)
                 m = torch.empty((N, self.D), dtype=torch.float64, device=self.dev)
                 L = torch.empty((N, self.D, self.D), dtype=torch.float64, device=self.dev)
-                info = torch.empty(_lib.I_COUNT, dtype=torch.float64, device=self.dev)
+                info = torch.empty(_lib.I_COUNT + (2 if self.mixed else 0), dtype=torch.float64, device=self.dev)
+                if self.mixed:  # float32 iterations kept, smallest float32 change (before the slot is freed)
+                    _lib.check(lib.pof_server_mixed_info(self.h, slot, _lib.ptr(info[_lib.I_COUNT:])),
+                               "pof_server_mixed_info")
                 _lib.check(lib.pof_server_fetch(self.h, slot, _lib.ptr(m), _lib.ptr(L), _lib.ptr(info)),
                            "pof_server_fetch")
                 idx = torch.arange(self.d, device=self.dev) * (self.q + 1)
@@ -139,10 +154,17 @@ class Server:
     """Host side of continuous batching: a FIFO of requests, one Engine per
     (d, q), admission each tick as memory allows."""
 
-    def __init__(self, max_requests=1024, max_points=1 << 21, device=None):
+    def __init__(self, max_requests=1024, max_points=1 << 21, device=None, precision="float64", maxiters_f32=10_000,
+                 rtol_f32=1e-5, settle_f32=float("inf")):
+        """precision="mixed": every request runs float32 IEKS iterations first
+        and float64 ones after (pof_server_create_mixed; the float32 phase's
+        rules and discard rule are those of pof.solver.solve's
+        precision="mixed")."""
         self.dev = device or default_device()
         self.max_requests = max_requests
         self.max_points = max_points
+        self.precision = dict(precision=precision, maxiters_f32=maxiters_f32, rtol_f32=rtol_f32,
+                              settle_f32=settle_f32)
         self.engines = {}
         self.queue = deque()
         self.results = {}
@@ -155,7 +177,7 @@ class Server:
     def engine(self, d, q):
         key = (d, q)
         if key not in self.engines:
-            self.engines[key] = Engine(d, q, self.max_requests, self.max_points, device=self.dev)
+            self.engines[key] = Engine(d, q, self.max_requests, self.max_points, device=self.dev, **self.precision)
         return self.engines[key]
 
     def submit(self, field, params, y0, ts, order, rtol=1e-6, maxiters=10_000, t_arrival=None, timeout=None):
@@ -266,9 +288,12 @@ class Server:
         status = _lib.solve_status(float(info[_lib.I_STATUS]))
         if status == "cancelled":
             status = self.stop_reason.get(rid, status)
-        return ys, {"iterations": info[_lib.I_ITERATIONS].to(torch.int64), "nll": info[_lib.I_NLL],
-                    "obj": info[_lib.I_OBJ], "sigma_squared": info[_lib.I_SSQ], "status": status,
-                    "calibrated": True}
+        out = {"iterations": info[_lib.I_ITERATIONS].to(torch.int64), "nll": info[_lib.I_NLL],
+               "obj": info[_lib.I_OBJ], "sigma_squared": info[_lib.I_SSQ], "status": status, "calibrated": True}
+        if info.shape[0] > _lib.I_COUNT:  # a mixed-precision engine's request
+            out["iterations_float32"] = info[_lib.I_COUNT].to(torch.int64)
+            out["best_change_float32"] = info[_lib.I_COUNT + 1]
+        return ys, out
 
     def close(self):
         for e in self.engines.values():

@@ -111,3 +111,61 @@ def test_admission_waits_for_memory():
     tight = _serve_mix(reqs, max_points=700, max_requests=2, stagger=0)
     for i, r in enumerate(reqs):
         _same(tight[i], _serve_mix([r])[0])
+
+
+# well-conditioned requests (one IEKS fixed point each) for the float32 + float64 form
+MIXED_REQUESTS = [
+    ("vanderpol", (1.0,), [2.0, 0.0], 6.3, 600, 3, 1e-6),
+    ("logistic", (1.0,), [0.01], 10.0, 300, 3, 1e-6),
+    ("vanderpol", (1.2,), [1.9, 0.1], 5.0, 1100, 4, 1e-6),
+]
+
+
+def _serve_mixed(reqs, stagger=2):
+    srv = serve.Server(max_requests=16, max_points=1 << 15, precision="mixed")
+    rids = []
+    for r in reqs:
+        nm, p, y0, t1, N, q, rtol = r
+        rids.append(srv.submit(nm, p, y0, np.linspace(0.0, t1, N), q, rtol=rtol, maxiters=1000))
+        for _ in range(stagger):
+            srv.tick()
+    guard = 0
+    while srv.busy():
+        srv.tick()
+        guard += 1
+        assert guard < 20000
+    out = [srv.result(rid) for rid in rids]
+    srv.close()
+    return out
+
+
+def test_served_mixed_precision():
+    """The served float32 + float64-polish form: each request runs float32
+    IEKS iterations, then float64 ones, in the same ticks as the others.
+    Its result is the batched mixed solve of that problem with its chunk
+    length, bit for bit, alone and in the mix (float32 iterations and their
+    count included), and within 1e-6 of the served float64 result."""
+    mix = _serve_mixed(MIXED_REQUESTS)
+    f64 = _serve_mix(MIXED_REQUESTS)
+    for i, r in enumerate(MIXED_REQUESTS):
+        nm, p, y0, t1, N, q, rtol = r
+        (gm, gL), gi = mix[i]
+        assert gi["status"] == "converged" and int(gi["iterations_float32"]) > 0, (nm, gi)
+        alone = _serve_mixed([r])[0]
+        assert torch.equal(gm, alone[0][0]) and torch.equal(gL, alone[0][1])
+        assert int(gi["iterations_float32"]) == int(alone[1]["iterations_float32"])
+        n = N - 1
+        c0 = 4
+        while c0 < 64 and c0 * 2 * 256 <= n:
+            c0 *= 2
+        res = pbatch.solve_batch([(nm, p, y0, np.linspace(0.0, t1, N))], order=q, maxiters=1000, C0=c0, Cg=2,
+                                 precision="mixed")
+        (bm, bL), bi = res.problem(0)
+        assert torch.equal(gm, bm) and torch.equal(gL, bL), nm
+        assert int(gi["iterations"]) == int(bi["iterations"])
+        assert int(gi["iterations_float32"]) == int(bi["iterations_float32"])
+        (fm, _), fi = f64[i]
+        err = float((gm - fm).abs().max() / fm.abs().max())
+        print("[served mixed %s] float32 %d + float64 %d iterations (float64 alone %d), %.3g from float64" % (
+            nm, int(gi["iterations_float32"]), int(gi["iterations"]), int(fi["iterations"]), err))
+        assert err <= 1e-6
