@@ -760,40 +760,62 @@ def served_block(args):
         torch.cuda.synchronize()
         plain_t.append(time.perf_counter() - t0)
         del ws, m, c
-    srv = serve.Server(max_requests=256, max_points=1 << 21, device=dev)
-    for r in reqs[:6]:  # engines built and warmed
-        nm, p, y0, ts, q, tol = r
-        srv.submit(nm, p, y0, ts[: min(len(ts), 300)], q, rtol=tol, maxiters=maxiters)
-    while srv.busy():
-        srv.tick()
-    srv.results.clear()
     arrivals = np.cumsum(np.random.default_rng(seed + 1000).exponential(1.0 / rate, size=R))
     fin, lat_plain = 0.0, []
     for a, t in zip(arrivals, plain_t):
         fin = max(a, fin) + t
         lat_plain.append(fin - a)
-    t_start = time.perf_counter()
-    rid_of, k = {}, 0
-    while k < R or srv.busy():
-        now = time.perf_counter() - t_start
-        while k < R and arrivals[k] <= now:
-            nm, p, y0, ts, q, tol = reqs[k]
-            rid_of[srv.submit(nm, p, y0, ts, q, rtol=tol, maxiters=maxiters, t_arrival=t_start + arrivals[k])] = k
-            k += 1
-        if srv.busy():
+
+    def stream(precision):
+        srv = serve.Server(max_requests=256, max_points=1 << 21, device=dev, precision=precision,
+                           settle_f32=args.f32_settle)
+        for r in reqs[:6]:  # engines built and warmed
+            nm, p, y0, ts, q, tol = r
+            srv.submit(nm, p, y0, ts[: min(len(ts), 300)], q, rtol=tol, maxiters=maxiters)
+        while srv.busy():
             srv.tick()
-        elif k < R:
-            time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t_start))))
-    lat = [srv.t_done[rid] - srv.t_submit[rid] for rid in rid_of]
-    statuses = [srv.result(rid)[1]["status"] for rid in rid_of]
-    makespan = max(srv.t_done[rid] for rid in rid_of) - (t_start + arrivals[0])
-    srv.close()
+        srv.results.clear()
+        t_start = time.perf_counter()
+        rid_of, k = {}, 0
+        while k < R or srv.busy():
+            now = time.perf_counter() - t_start
+            while k < R and arrivals[k] <= now:
+                nm, p, y0, ts, q, tol = reqs[k]
+                rid_of[srv.submit(nm, p, y0, ts, q, rtol=tol, maxiters=maxiters,
+                                  t_arrival=t_start + arrivals[k])] = k
+                k += 1
+            if srv.busy():
+                srv.tick()
+            elif k < R:
+                time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t_start))))
+        lat = [srv.t_done[rid] - srv.t_submit[rid] for rid in rid_of]
+        res = {rid_of[rid]: srv.result(rid) for rid in rid_of}
+        makespan = max(srv.t_done[rid] for rid in rid_of) - (t_start + arrivals[0])
+        srv.close()
+        statuses = [res[i][1]["status"] for i in range(R)]
+        return res, {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                     "ivp_steps_per_s": steps_total / makespan, "makespan_s": makespan,
+                     "status_counts": {s_: statuses.count(s_) for s_ in sorted(set(statuses))}}
+
+    res64, served64 = stream("float64")
+    resmx, servedmx = stream("mixed")
+    errs = []
+    for i in range(R):
+        (a, _), ia = resmx[i]
+        (b, _), ib = res64[i]
+        if ia["status"] == ib["status"] == "converged":
+            errs.append(float((a - b).abs().max() / b.abs().max()))
+    errs = np.array(errs) if errs else np.array([np.nan])
+    servedmx["float32_iterations_total"] = int(sum(int(resmx[i][1]["iterations_float32"]) for i in range(R)))
+    servedmx["rel_err_vs_served_float64"] = {"requests_both_converged": int(np.isfinite(errs).sum()),
+                                             "max": float(np.nanmax(errs)), "median": float(np.nanmedian(errs)),
+                                             "fraction_within_1e-6": float((errs <= 1e-6).mean())}
+    servedmx["speedup_vs_plain_fifo"] = servedmx["ivp_steps_per_s"] / (steps_total / (fin - arrivals[0]))
     return {"workload": "%d requests at %.0f/s (Poisson), logistic / FitzHugh-Nagumo / Lotka-Volterra / Van der Pol "
                         "mu = 10, +-20 %% parameters, N log-uniform in [2^8, 2^16], q in {2, 3, 4}, tolerance in "
                         "{1e-4, 1e-6}, maxiters %d" % (R, rate, maxiters, maxiters),
-            "served": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-                       "ivp_steps_per_s": steps_total / makespan, "makespan_s": makespan,
-                       "status_counts": {s: statuses.count(s) for s in sorted(set(statuses))}},
+            "served": served64,
+            "served_mixed": servedmx,
             "plain_fifo": {"p50_s": float(np.percentile(lat_plain, 50)), "p99_s": float(np.percentile(lat_plain, 99)),
                            "ivp_steps_per_s": steps_total / (fin - arrivals[0])},
             "omitted": "reaction-diffusion d = 128 requests (the dense D >= 128 path is not built)"}
