@@ -813,7 +813,7 @@ def served_block(args):
     servedmx["speedup_vs_plain_fifo"] = servedmx["ivp_steps_per_s"] / (steps_total / (fin - arrivals[0]))
     return {"workload": "%d requests at %.0f/s (Poisson), logistic / FitzHugh-Nagumo / Lotka-Volterra / Van der Pol "
                         "mu = 10, +-20 %% parameters, N log-uniform in [2^8, 2^16], q in {2, 3, 4}, tolerance in "
-                        "{1e-4, 1e-6}, maxiters %d" % (R, rate, maxiters, maxiters),
+                        "{1e-4, 1e-6}, maxiters %d" % (R, rate, maxiters),
             "served": served64,
             "served_mixed": servedmx,
             "plain_fifo": {"p50_s": float(np.percentile(lat_plain, 50)), "p99_s": float(np.percentile(lat_plain, 99)),

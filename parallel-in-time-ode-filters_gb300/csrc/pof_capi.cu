@@ -63,7 +63,7 @@ int env_int(const char* name, int dflt = 0) {
 
 Plan plan_for(int dtype, int64_t n, int D, int DY, bool solver) {
   return make_plan(n, D, DY, esz(dtype), solver, env_int("POF_C0"), env_int("POF_CG"),
-                   env_int("POF_TEAM_WIDE_L0") != 0, env_int("POF_KS", 0), env_int("POF_L0_TEAM", 0));
+                   env_int("POF_TEAM_WIDE_L0") != 0, env_int("POF_KS", 0));
 }
 
 // The sequential filter/smoother as a plan: one level-0 chunk spanning all

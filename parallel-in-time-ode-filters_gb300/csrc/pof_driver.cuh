@@ -155,10 +155,6 @@ struct Driver {
   static constexpr int TSW = TeamSize<D>::v;                     // wide teams
   static constexpr int TSN = TSW / 2 >= 4 ? TSW / 2 : 4;          // narrow teams
   static constexpr int TSX = TSW < 32 ? 2 * TSW : 32;             // widest teams (latency-bound levels)
-  // quarter teams (4 lanes) at level 0, D = 8 only (tuning: POF_L0_TEAM=4):
-  // one warp instruction serves twice as many chunks' one-lane reflector
-  // chains, each lane updates twice as many rows
-  static constexpr int TSQ = (D == 8 && TSN > 4) ? 4 : TSN;
   static constexpr bool kTeamL0 = D >= 6;  // pof_plan.h l0_lanes
   using FWS = FiltTeamWs<T, D>;
   using SWS = SmoTeamWs<T, D>;
@@ -174,18 +170,14 @@ struct Driver {
 
   static void filter(const Plan& p, char* ws, const StepModel& sm, const T* x0m, const T* x0L, T* means, T* chols,
                      cudaStream_t st) {
-    if (p.team == TSQ && TSQ != TSN)
-      filter_ts<TSQ, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
-    else if (p.team == TSN && TSN != TSW)
+    if (p.team == TSN && TSN != TSW)
       filter_ts<TSN, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
     else
       filter_ts<TSW, TSW>(p, ws, sm, x0m, x0L, means, chols, st);
   }
   static void smoother(const Plan& p, char* ws, const T* F, const T* QL, int64_t ft_stride, T* means, T* chols,
                        bool calibrate, const T* means_old, cudaStream_t st) {
-    if (p.team == TSQ && TSQ != TSN)
-      smoother_ts<TSQ, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);
-    else if (p.team == TSN && TSN != TSW)
+    if (p.team == TSN && TSN != TSW)
       smoother_ts<TSN, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);
     else
       smoother_ts<TSW, TSW>(p, ws, F, QL, ft_stride, means, chols, calibrate, means_old, st);

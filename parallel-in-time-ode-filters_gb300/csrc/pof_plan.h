@@ -94,14 +94,13 @@ inline int64_t ks_limit(int D, int ks_max) {
 // with_solver: also reserve the EK1 (H, c) buffers, a second means buffer
 // and a parameter slot used by the IEKS loop.
 inline Plan make_plan(int64_t n, int D, int DY, int esz, bool with_solver, int C0 = 0, int Cg = 0,
-                      bool narrow = false, int ks_max = 0, int l0_team = 0) {
+                      bool narrow = false, int ks_max = 0) {
   Plan p;
   p.n = n;
   p.D = D;
   p.DY = DY;
   p.esz = esz;
   p.team = team_lanes(D, !narrow);  // level 0: narrow unless told otherwise
-  if (l0_team == 4 && D == 8) p.team = 4;  // quarter teams (Driver::TSQ)
   p.team_up = team_lanes(D, false);
   p.C0 = C0 > 0 ? C0 : pick_c0(n, l0_lanes(D, !narrow));
   // binary tree above level 0: the critical path holds one combine per level

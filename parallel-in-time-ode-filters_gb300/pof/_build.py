@@ -25,7 +25,10 @@ LIB = os.path.join(PKG_DIR, "libpof.so")
 # the same sources with the runtime bounds checks (POF_CHECKS; relocatable
 # device code, so every unit shares the check word)
 LIB_CHECKED = os.path.join(PKG_DIR, "libpof_checked.so")
-CHECK_FLAGS = ["-DPOF_CHECKS", "-rdc=true"]
+CHECK_FLAGS = ["-DPOF_CHECKS", "-rdc=true", "-DPOF_SHAPE_SUBSET"]
+# shapes of the checked build (the registries' POF_SHAPE_SUBSET lists)
+CHECK_SHAPES = ("pof_inst_D3_d1.cu", "pof_inst_D8_d2.cu", "pof_inst_D12_d3.cu", "pof_inst_D3_d4.cu",
+                "pof_binst_D8_d2.cu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE] + ARCH
@@ -38,8 +41,12 @@ def nvcc():
     raise RuntimeError("nvcc not found: libpof.so needs the CUDA toolkit to build")
 
 
-def sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+def sources(checks=False):
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    if checks:
+        srcs = [p for p in srcs if not os.path.basename(p).startswith(("pof_inst_", "pof_binst_"))
+                or os.path.basename(p) in CHECK_SHAPES]
+    return srcs
 
 
 def _deps():
@@ -72,7 +79,7 @@ def build(force=False, jobs=None, verbose=True, checks=False):
     if not force and up_to_date(lib):
         return lib
     os.makedirs(build_dir, exist_ok=True)
-    srcs = sources()
+    srcs = sources(checks)
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 1))
     if verbose:
         print("[pof build] nvcc %d units, %d jobs%s" % (len(srcs), jobs, " (bounds checks)" if checks else ""),

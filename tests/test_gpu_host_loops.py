@@ -78,14 +78,15 @@ def test_levenberg_marquardt_iterator_on_the_gpu():
         assert np.isclose(nll, onll, rtol=1e-9) and np.isclose(obj, oobj, rtol=1e-9)
 
 
-def _oracle_loop(st, init="constant", maxiters=10_000):
+def _oracle_loop(st, init="constant", maxiters=10_000, scan=None):
     states = osolver.get_initial_trajectory(st, init)
     nll = obj = 0.0
     old, nll_old, obj_old = states, 0.0, 0.0
     k = 0
+    kw = {} if scan is None else {"scan": scan}
     while k < 1 or (not osolver.crit(obj, obj_old, nll, nll_old, states[0], old[0]) and k <= maxiters):
         old, nll_old, obj_old = states, nll, obj
-        states, nll, obj, _ = osolver.ieks_step(st, old)
+        states, nll, obj, _ = osolver.ieks_step(st, old, **kw)
         k += 1
     return states, k
 
@@ -102,8 +103,16 @@ def test_non_uniform_grid_solve_on_the_gpu():
     ys, info = psolver.solve_nonuniform(f=f, y0=[0.01], ts=ts, order=3)
     st = osolver.set_up_solver_no_precond(oivp.logistic(r=1.0), ts, 3)
     (om, _), k = _oracle_loop(st)
-    assert int(info["iterations"]) == k
-    assert rel(_np(ys.mean), om @ st.E0.T) <= TOL
+    (sm, _), ks = _oracle_loop(st, scan=sequential_scan)
+    assert int(info["iterations"]) == k == ks
+    # the two oracle orders differ by 1.6e-9 on this grid (steps from 0.4 down
+    # to 4e-3): the fixed point amplifies rounding by its conditioning
+    spread = rel(sm @ st.E0.T, om @ st.E0.T)
+    tol = max(TOL, 10 * spread)
+    print("[non-uniform] gpu vs oracle %.3g, tolerance %.3g (oracle order spread %.3g)" % (
+        rel(_np(ys.mean), om @ st.E0.T), tol, spread))
+    assert spread <= 5e-9
+    assert rel(_np(ys.mean), om @ st.E0.T) <= tol
     assert np.abs(_np(ys.mean)[:, 0] - exact).max() < 1e-6
 
 
