@@ -41,14 +41,16 @@ CAP = 1e-8
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "config_goldens.npz")
 
 # Cases whose two oracle orders disagree by more than CAP / 10 from the same
-# input, with the spread measured by the oracle (tree vs sequential order):
-# on FitzHugh-Nagumo over t in [0, 100] one IEKS iteration from an iterate of
-# the solve is itself ill-conditioned (the orders' next iterates differ by
-# up to O(1)), so the GPU's is checked against that spread only.
+# input, with the spread measured by the oracle (tree vs sequential order).
+# FitzHugh-Nagumo over t in [0, 100]: one IEKS iteration from the oracle's
+# iterates 20 and 400 of its solve is ill-conditioned (at its converged
+# iterate 656 the orders agree to 4e-14 and the 1e-10 bound holds).  The
+# logistic sweep: two grids whose IEKS fixed point amplifies rounding.
 ILL_CONDITIONED = {
-    "fhn_n1000_step_20": "oracle orders differ by ~3e-4 after one iteration",
-    "fhn_n1000_step_400": "oracle orders differ by ~5e-2 after one iteration",
-    "fhn_n1000_step_656": "oracle orders differ by O(1) after one iteration",
+    "fhn_n1000_step_20": "oracle orders differ by 2.6e-6 after one iteration",
+    "fhn_n1000_step_400": "oracle orders differ by 4.1e-4 after one iteration",
+    "log_q2_N4096": "oracle orders' solutions differ by 2.8e-9",
+    "log_q3_N4096": "oracle orders' solutions differ by 5.0e-8",
 }
 
 
@@ -156,27 +158,37 @@ def test_fhn_n1000_solve(gold):
     that differ by up to O(1), so the iteration count and the fixed point
     reached are decided by rounding, differently in each order.  Checked:
     the loop stops on the reference's criterion (status converged, finite
-    results), the orders' own traces agree at iteration 1 and part at
-    iteration 2; the counts, criterion margins and distances are printed."""
+    results), and the oracle's two orders agree at iteration 1 and part at
+    iteration 2; the counts, objectives and distances are printed."""
     o, ts, st = _fhn_setup()
     p = pivp.fhn_classic()
     out, info = psolver.solve(f=p.f, y0=p.y0, ts=ts, order=3, init="constant")
     it = int(info["iterations"])
-    it_tree, it_seq = (int(x) for x in gold["fhn_iterations"])
-    print("[fhn_n1000] iterations: gpu %d, oracle tree %d, oracle sequential %d" % (it, it_tree, it_seq))
-    print("[fhn_n1000] objective change at the stop: tree %.3g, sequential %.3g (crit: 1e-6)" % (
-        obj_margin(gold["fhn_trace_tree"], it_tree), obj_margin(gold["fhn_trace_seq"], it_seq)))
+    it_tree, it_seq = (int(x) for x in gold["fhn_iterations"])  # it_seq -1: not in the fixture
     y = N_(out.mean)
-    print("[fhn_n1000] final y vs oracle tree: gpu %.3g, oracle sequential %.3g" % (
-        rel(y, gold["fhn_y_tree"]), rel(gold["fhn_y_seq"], gold["fhn_y_tree"])))
+    print("[fhn_n1000] iterations: gpu %d, oracle tree %d, oracle sequential %s" % (
+        it, it_tree, it_seq if it_seq >= 0 else "n/a"))
+    print("[fhn_n1000] final objective: gpu %.6g, oracle tree %.6g (its last change %.3g; crit 1e-6)" % (
+        float(info["obj"]), gold["fhn_trace_tree"][it_tree - 1][0], obj_margin(gold["fhn_trace_tree"], it_tree)))
+    print("[fhn_n1000] final y vs oracle tree: gpu %.3g" % rel(y, gold["fhn_y_tree"]))
+    if "fhn_y_seq" in gold:
+        print("[fhn_n1000] oracle sequential vs tree %.3g" % rel(gold["fhn_y_seq"], gold["fhn_y_tree"]))
     assert _lib.solve_status(int(info["status"])) == "converged"
     assert np.isfinite(y).all() and np.isfinite(N_(out.chol)).all()
     assert 1 <= it <= 10_001
     if it_tree == it_seq:
         assert it == it_tree
-    tr, sq = gold["fhn_trace_tree"], gold["fhn_trace_seq"]
-    assert abs(tr[0][0] - sq[0][0]) <= 1e-12 * abs(tr[0][0])
-    assert abs(tr[1][0] - sq[1][0]) > 1e-3 * abs(tr[1][0])
+    # the reference's own two orders agree after the first iteration and
+    # part after the second (the reason the count is rounding-decided here)
+    states = osolver.get_initial_trajectory(st, "constant")
+    a1, _, oa1, _ = osolver.ieks_step(st, states)
+    b1, _, ob1, _ = osolver.ieks_step(st, states, sequential=True)
+    _, _, oa2, _ = osolver.ieks_step(st, a1)
+    _, _, ob2, _ = osolver.ieks_step(st, b1, sequential=True)
+    print("[fhn_n1000] oracle objectives, tree / sequential: iteration 1 %.9g / %.9g, iteration 2 %.6g / %.6g" % (
+        oa1, ob1, oa2, ob2))
+    assert abs(oa1 - ob1) <= 1e-12 * abs(oa1)
+    assert abs(oa2 - ob2) > 1e-3 * abs(oa2)
 
 
 def test_fhn_bench_shape_filtsmooth_matches_oracle():
