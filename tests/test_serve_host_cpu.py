@@ -52,6 +52,22 @@ class FakeEngines:
     def pof_server_destroy(self, h):
         return 0
 
+    def pof_server_mixed_workspace_bytes(self, D, d, max_requests, max_points, level_bytes):
+        return 8192
+
+    def pof_server_create_mixed(self, D, d, max_requests, max_points, level_bytes, F, QL, calibrate, maxiters_f32,
+                                rtol_f32, settle_f32, ws, wsb, out):
+        rc = self.pof_server_create(D, d, max_requests, max_points, level_bytes, F, QL, calibrate, ws, wsb, out)
+        self.servers[out._obj.value].update(mixed=(maxiters_f32, rtol_f32, settle_f32))
+        return rc
+
+    def pof_server_mixed_info(self, h, slot, info):
+        s = self._s(h)
+        r = s["slots"][slot]
+        a = np.array([r["n"] % 7 + 1.0, 1e-6])  # a stand-in float32 count per request
+        ctypes.memmove(info.value, a.ctypes.data, a.nbytes)
+        return 0
+
     def pof_server_submit(self, h, n_steps, field, params, step, x0m, x0L, row, maxiters, rtol):
         s = self._s(h)
         free = [i for i in range(s["maxB"]) if i not in s["slots"]]
@@ -248,3 +264,19 @@ def test_stuck_request_times_out(fake, monkeypatch):
     assert y is None and info2["status"] == "timeout"
     ev = [e for e, _, _, _ in fake.log]
     assert ev.count("cancel") == 1 and ev.count("admit") == 1
+
+
+def test_mixed_precision_server(fake):
+    """precision="mixed" creates mixed engines with the float32-phase
+    settings and reports each request's float32 iterations (read before the
+    result is fetched) beside the float64 ones."""
+    srv = serve.Server(max_requests=4, max_points=10**6, precision="mixed", maxiters_f32=50, rtol_f32=1e-4,
+                       settle_f32=0.1)
+    rids = [srv.submit(*logistic(n), order=2) for n in (100, 222)]
+    _run(srv)
+    (h,) = list(fake.servers)
+    assert fake.servers[h]["mixed"] == (50, 1e-4, 0.1)
+    for rid, n in zip(rids, (100, 222)):
+        _, info = srv.result(rid)
+        assert int(info["iterations_float32"]) == n % 7 + 1
+        assert int(info["iterations"]) == 2 + n // 100 and info["status"] == "converged"
