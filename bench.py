@@ -721,7 +721,86 @@ def batched_block(args):
         "batched_mixed": out["batched_mixed"]["step_iterations_per_s"] / plain_rate,
         "unit": "ratio of step-iterations/s under the same budget"}
     del ws[0]
+    out["vanderpol_mixed"] = vdp_mixed_block(args)
     return out
+
+
+def vdp_mixed_block(args):
+    """The float32 + float64-polish form where float32 can carry the bulk of
+    the iterations: 512 Van der Pol IVPs (mu within +-20 % of 1, y0 ~
+    N((2, 0), 0.1^2 I), t in [0, 6.3], N log-uniform in [256, 8192], q = 3),
+    solved to the reference's criterion (no budget): IVP*steps/s of the
+    plain one-solve-per-launch float64 path (8 instances stratified by N),
+    of the batched float64 and of the batched mixed solve, and the
+    per-instance error of mixed against batched float64."""
+    import torch
+
+    from pof import _lib, batch as pbatch
+
+    lib = _lib.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    family, B, seed, q, maxiters = BATCH_WORKLOADS["vdp_batch512"]
+    prep = pbatch.prepare_batch(batch_problems(family, B, seed), q, device=dev)
+    n_steps = prep["n_steps"]
+    D, d = prep["D"], prep["d"]
+    means = torch.empty_like(prep["means0"])
+    chols = torch.empty((means.shape[0], D, D), dtype=torch.float64, device=dev)
+    info = torch.zeros((B, _lib.I_COUNT), dtype=torch.float64, device=dev)
+    info32 = torch.zeros((B, 2), dtype=torch.float64, device=dev)
+    ws = [None]
+
+    def solve(precision):
+        means.copy_(prep["means0"])
+        ws[0] = pbatch.run_batch(prep, means, chols, info, maxiters=maxiters, workspace=ws[0], precision=precision,
+                                 info_f32=info32, maxiters_f32=maxiters, settle_f32=args.f32_settle)
+
+    solve("float64")
+    t64 = float(np.median(_events_ms(torch, lambda: solve("float64"), 3)))
+    ref = means.clone()
+    it64 = info[:, _lib.I_ITERATIONS].cpu().numpy()
+    ws[0] = None
+    solve("mixed")
+    tmx = float(np.median(_events_ms(torch, lambda: solve("mixed"), 3)))
+    err = _project_err(prep, means, ref)
+    it32 = info32[:, 0].cpu().numpy()
+    order = np.argsort(n_steps)
+    plain_ms, plain_steps = 0.0, 0
+    for b in [int(order[int(i)]) for i in np.linspace(0, B - 1, 8)]:
+        n = int(n_steps[b])
+        m = torch.empty((n + 1, D), dtype=torch.float64, device=dev)
+        c = torch.empty((n + 1, D, D), dtype=torch.float64, device=dev)
+        inf = torch.zeros(_lib.I_COUNT, dtype=torch.float64, device=dev)
+        wsb = lib.pof_ieks_workspace_bytes(_lib.POF_F64, n, D, d)
+        pws = _lib.workspace(wsb, dev)
+        m0 = prep["means0"][prep["offsets"][b]:prep["offsets"][b + 1]]
+        x0m, x0L = prep["x0m"][b].contiguous(), prep["x0L"][b].contiguous()
+
+        def one():
+            m.copy_(m0)
+            _lib.check(lib.pof_ieks_solve(_lib.POF_F64, n, D, d, int(prep["fields"][b]), _lib.ptr(prep["params"][b]),
+                                          float(prep["h"][b]), _lib.ptr(x0m), _lib.ptr(x0L), _lib.ptr(prep["F"]),
+                                          _lib.ptr(prep["QL"]), _lib.ptr(m), _lib.ptr(c), maxiters, 1,
+                                          _lib.ptr(inf), _lib.ptr(pws), wsb, _lib.stream_handle()), "pof_ieks_solve")
+
+        one()
+        plain_ms += _events_ms(torch, one, 1)[0]
+        plain_steps += n
+    plain = plain_steps / (plain_ms * 1e-3)
+    steps = float(n_steps.sum())
+    return {"workload": "vdp_batch512: 512 Van der Pol IVPs, mu within +-20% of 1, y0 ~ N((2, 0), 0.1^2 I), "
+                        "t in [0, 6.3], N log-uniform in [256, 8192] (default_rng(0)), q = 3, the reference's "
+                        "criterion (maxiters %d)" % maxiters,
+            "plain_float64_ivp_steps_per_s": plain,
+            "batched_float64": {"ms": t64, "ivp_steps_per_s": steps / (t64 * 1e-3),
+                                "iterations_median": float(np.median(it64))},
+            "batched_mixed": {"ms": tmx, "ivp_steps_per_s": steps / (tmx * 1e-3),
+                              "float32_iterations_median": float(np.median(it32)),
+                              "float64_iterations_median": float(np.median(info[:, _lib.I_ITERATIONS].cpu().numpy())),
+                              "instances_with_float32_kept": int((it32 > 0).sum())},
+            "speedup_vs_plain": {"batched_float64": steps / (t64 * 1e-3) / plain,
+                                 "batched_mixed": steps / (tmx * 1e-3) / plain},
+            "mixed_rel_err_vs_float64": {"max": float(err.max()), "median": float(np.median(err)),
+                                         "fraction_within_1e-6": float((err <= 1e-6).mean())}}
 
 
 def served_block(args):

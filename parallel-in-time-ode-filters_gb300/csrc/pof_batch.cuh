@@ -48,7 +48,7 @@ struct BView {
   using B_ = TeamBlockH<WS, TS, HB_>;                                                    \
   extern __shared__ __align__(16) unsigned char smem_raw_[];                             \
   const int team_in_block = threadIdx.x / TS;                                            \
-  WS& ws_ = reinterpret_cast<WS*>(smem_raw_ + HB_)[team_in_block];                      \
+  WS& ws_ = *reinterpret_cast<WS*>(smem_raw_ + HB_ + team_in_block * B_::stride);     \
   const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;                    \
   Team<TS> tm;                                                                           \
   FQ<T, D>& fq = *reinterpret_cast<FQ<T, D>*>(smem_raw_);                               \

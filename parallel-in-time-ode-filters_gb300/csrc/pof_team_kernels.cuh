@@ -406,14 +406,19 @@ struct FQHeader {
 };
 
 // teams per block of a level-0 kernel with a shared header of HB bytes:
-// up to 64 / TS teams within the default 48 KB of dynamic shared memory
+// up to 64 / TS teams within the default 48 KB of dynamic shared memory.
+// Team workspaces are `stride` bytes apart, stride = 64 (mod 128): the two
+// 8-lane teams of a half-warp then sit 8 doubles apart in the 32 banks, so a
+// column of an odd-leading-dimension matrix read one row per lane (and a row
+// read one column per lane) by both teams at once hits 32 distinct banks.
 template <typename WS, int TS, int HB>
 struct TeamBlockH {
+  static constexpr int stride = (int)(((sizeof(WS) + 63) / 128) * 128 + 64);
   static constexpr int per_warp_max = 64 / TS;
-  static constexpr int fit = (int)((49152 - HB) / sizeof(WS));
+  static constexpr int fit = (int)((49152 - HB) / stride);
   static constexpr int teams = fit < 1 ? 1 : (fit < per_warp_max ? fit : per_warp_max);
   static constexpr int threads = teams * TS;
-  static constexpr int smem = HB + teams * (int)sizeof(WS);
+  static constexpr int smem = HB + teams * stride;
 };
 
 template <typename T, int TS, int D>
@@ -500,7 +505,7 @@ __device__ __forceinline__ T t_objective(const Team<TS>& tm, const T* F, const T
   using B_ = TeamBlockH<WS, TS, HB_>;                                                    \
   extern __shared__ __align__(16) unsigned char smem_raw_[];                             \
   const int team_in_block = threadIdx.x / TS;                                            \
-  WS& ws_ = reinterpret_cast<WS*>(smem_raw_ + HB_)[team_in_block];                      \
+  WS& ws_ = *reinterpret_cast<WS*>(smem_raw_ + HB_ + team_in_block * B_::stride);     \
   const int64_t t = (int64_t)blockIdx.x * B_::teams + team_in_block;                    \
   Team<TS> tm;                                                                           \
   FQ<T, D>& fq = fq_ref<PS, T, D>(ws_, smem_raw_);
