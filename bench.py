@@ -787,7 +787,7 @@ def vdp_mixed_block(args):
         plain_steps += n
     plain = plain_steps / (plain_ms * 1e-3)
     steps = float(n_steps.sum())
-    return {"workload": "vdp_batch512: 512 Van der Pol IVPs, mu within +-20% of 1, y0 ~ N((2, 0), 0.1^2 I), "
+    return {"workload": "vdp_batch512: 512 Van der Pol IVPs, mu within +-20%% of 1, y0 ~ N((2, 0), 0.1^2 I), "
                         "t in [0, 6.3], N log-uniform in [256, 8192] (default_rng(0)), q = 3, the reference's "
                         "criterion (maxiters %d)" % maxiters,
             "plain_float64_ivp_steps_per_s": plain,
@@ -1188,6 +1188,17 @@ def cpu_sample_batch(problems, q, its, budget_s=20.0):
 # the same GPU, one IVP per launch
 # ---------------------------------------------------------------------------
 
+# The reference's published float64 IEKS results on a Tesla V100-SXM2-32GB
+# (experiments/3_work_precision_diagram/data/<setup>_Tesla_V100-SXM2-32GB.csv:
+# ms per solve, min of 3, and iterations), the rows the v100_table workload
+# reruns: (ivp, q, N) -> (ms, iterations).
+V100_PUBLISHED = {
+    ("logistic", 3, 2**10): (55.8, 12), ("logistic", 3, 2**14): (143.4, 12), ("logistic", 3, 2**19): (2680.0, 12),
+    ("fitzhughnagumo", 3, 2**10): (441.0, 62), ("fitzhughnagumo", 3, 2**14): (2523.0, 111),
+    ("fitzhughnagumo", 3, 2**19): (54740.0, 112), ("vanderpol", 3, 2**19): (4829.0, 10),
+    ("rigid_body", 3, 2**19): (11930.0, 10), ("henonheiles", 1, 2**19): (9494.0, 19),
+}
+
 SWEEP_WORKLOADS = {
     # name: (cases (field, kwargs, t1 or None for the IVP's own span, q, N values, largest N of the
     # sequential solves), unused, maxiters)
@@ -1201,7 +1212,7 @@ SWEEP_WORKLOADS = {
                     ("fitzhughnagumo", {}, None, 3, [2**10, 2**14, 2**19], 0),
                     ("vanderpol", {"stiffness_constant": 1.0}, None, 3, [2**19], 0),
                     ("rigid_body", {}, None, 3, [2**19], 0),
-                    ("henonheiles", {}, None, 1, [2**19], 0)], None, 1000),
+                    ("henonheiles", {"tmax": 10.0}, None, 1, [2**19], 0)], None, 1000),
 }
 
 
@@ -1241,6 +1252,11 @@ def run_sweep(args, workload):
             row = {"ivp": name, "q": q, "D": int(p.y0.shape[0]) * (q + 1), "N": N, "parallel_ieks_ms": tp * 1e3,
                    "iterations": it, "parallel_ms_per_iteration": tp * 1e3 / max(it, 1),
                    "status": int(info["status"])}
+            pub = V100_PUBLISHED.get((name, q, N)) if workload == "v100_table" else None
+            if pub:
+                row.update({"v100_published_ms": pub[0], "v100_published_iterations": pub[1],
+                            "speedup_vs_v100_published": pub[0] / (tp * 1e3),
+                            "per_iteration_speedup_vs_v100_published": (pub[0] / pub[1]) / (tp * 1e3 / max(it, 1))})
             if N <= seq_max:
                 sq = lambda: psolver.solve(f=p.f, y0=p.y0, ts=ts, order=q, init="constant",  # noqa: E731
                                            maxiters=maxiters, sequential=True)
