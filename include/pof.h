@@ -97,7 +97,13 @@ enum {
   POF_FIELD_RIGID_BODY = 7,     /* (p0, p1, p2)       pof/ivp.py:82-90  */
   POF_FIELD_SEIR = 8,           /* (p0..p3)           pof/ivp.py:93-108 */
   POF_FIELD_THREEBODY = 9,      /* (mu)               pof/ivp.py:111-126 */
-  POF_FIELD_HENONHEILES = 10    /* (p)                pof/ivp.py:137-152 */
+  POF_FIELD_HENONHEILES = 10,   /* (p)                pof/ivp.py:137-152 */
+  /* (a, b, c, kv, kw): method-of-lines FitzHugh-Nagumo on a periodic 1-D grid
+   * of m = d / 2 cells, y = (v_0..v_{m-1}, w_0..w_{m-1}),
+   *   v_k' = c (v_k - v_k^3 / 3 + w_k) + kv (v_{k-1} - 2 v_k + v_{k+1}),
+   *   w_k' = -(v_k - a + b w_k) / c + kw (w_{k-1} - 2 w_k + w_{k+1});
+   * any even d (pof_linearize; no reference counterpart) */
+  POF_FIELD_FHN_RD = 11
 };
 
 /* Text of a POF_* status; the last CUDA runtime error seen by libpof (for
@@ -141,6 +147,33 @@ int pof_linear_noiseless_filtering(int32_t dtype, int64_t n_steps, int32_t D, in
 int pof_smoothing(int32_t dtype, int64_t n_steps, int32_t D, const void* F, const void* QL, int64_t ft_stride,
                   const void* filt_mean, const void* filt_chol, void* out_mean, void* out_chol, double* out_scalars,
                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* The dense path: the filter and smoother above for large state dimensions.
+ * pof_linear_filtsmooth, pof_linear_noiseless_filtering, pof_smoothing and
+ * pof_filtsmooth_workspace_bytes take it by themselves for every (D, d)
+ * with D >= 32 that pof_shape_supported reports as not compiled; these
+ * entry points reach it for any shape and choose the number of chunks.
+ * The reference's operators work at any D
+ * (pof/parallel_filtsmooth/filter.py:117-142, smoother.py:53-63, tria
+ * pof/utils.py:33-41); the small-D tables do not.  Same schedule as the
+ * batched solve's (chunks fold their steps, the chunk totals are applied
+ * one after the other from x0 / from the terminal state, every chunk then
+ * runs the Kalman filter / RTS recursion from its start), each step a batch
+ * of dense GEMMs, blocked Householder trias and triangular solves over the
+ * chunks.  which: POF_DENSE_FILTER (pof_linear_noiseless_filtering),
+ * POF_DENSE_FILTSMOOTH (pof_linear_filtsmooth), POF_DENSE_SMOOTHING
+ * (pof_smoothing: x0_mean / x0_chol are the filtered means (N, D) / chols
+ * (N, D, D); H, c, R unused).  chunks: the number of chunks (0: 64, or the
+ * POF_DENSE_CHUNKS environment variable; at most n_steps).  Arguments and
+ * outputs otherwise as pof_linear_filtsmooth's. */
+enum { POF_DENSE_FILTER = 0, POF_DENSE_FILTSMOOTH = 1, POF_DENSE_SMOOTHING = 2 };
+size_t pof_dense_workspace_bytes(int32_t dtype, int32_t which, int64_t n_steps, int32_t D, int32_t d,
+                                 int32_t chunks);
+int pof_dense_linear_filtsmooth(int32_t which, int32_t dtype, int64_t n_steps, int32_t D, int32_t d,
+                                const void* x0_mean, const void* x0_chol, const void* F, const void* QL,
+                                int64_t ft_stride, const void* H, const void* c, const void* R, int64_t r_stride,
+                                void* out_mean, void* out_chol, double* out_scalars, int32_t chunks, void* workspace,
+                                size_t workspace_bytes, void* stream);
 
 /* EK1 linearization of a built-in field at means[1:]
  *   (pof/step.py:12-22, pof/observations.py:35-40) with the Nordsieck-scaled

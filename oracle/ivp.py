@@ -7,7 +7,7 @@ list of scalars, usable with floats, arrays and ``Taylor`` series), ``y0``,
 ``t0``, ``tmax``; ``f(t, y)`` evaluates it on arrays.
 """
 
-from typing import Callable, NamedTuple
+from typing import Callable, NamedTuple, Optional
 
 import numpy as np
 
@@ -21,11 +21,18 @@ class IVP(NamedTuple):
     tmax: float
     name: str = ""
     params: tuple = ()
+    # optional array forms of the field and its Jacobian (large systems)
+    f_array: Optional[Callable] = None
+    jac_array: Optional[Callable] = None
 
     def f(self, t, y):
+        if self.f_array is not None:
+            return self.f_array(np.asarray(y, float))
         return taylor.evaluate(self.components, y)
 
     def jac(self, y):
+        if self.jac_array is not None:
+            return self.jac_array(np.asarray(y, float))
         return taylor.jacobian(self.components, y)
 
     @property
@@ -149,3 +156,50 @@ def henonheiles(t0=0.0, tmax=100.0, y0=None, p=None):
         return [y[2], y[3], -y[0] - 2 * p * y[0] * y[1], -y[1] - p * (y[0] ** 2 - y[1] ** 2)]
 
     return IVP(comp, y0, t0, tmax, "henonheiles", (p,))
+
+
+
+def fhn_reaction_diffusion(t0=0.0, tmax=20.0, y0=None, cells=64, a=0.2, b=0.2, c=3.0, kv=0.5, kw=0.05, amp=0.5):
+    """Method-of-lines FitzHugh-Nagumo on a periodic grid of `cells` cells,
+    y = (v_0..v_{m-1}, w_0..w_{m-1}) (the reaction-diffusion configuration;
+    the reference has no such field):
+    v_k' = c (v_k - v_k^3 / 3 + w_k) + kv (v_{k-1} - 2 v_k + v_{k+1}),
+    w_k' = -(v_k - a + b w_k) / c + kw (w_{k-1} - 2 w_k + w_{k+1})."""
+    m = int(cells)
+    if y0 is None:
+        k = np.arange(m)
+        y0 = np.concatenate([-1.0 + amp * np.sin(2.0 * np.pi * k / m), np.ones(m)])
+    y0 = np.asarray(y0, float)
+
+    def comp(Y):
+        out = []
+        for k in range(m):
+            v, w = Y[k], Y[m + k]
+            out.append(c * (v - v * v * v / 3.0 + w) + kv * (Y[(k - 1) % m] - 2.0 * v + Y[(k + 1) % m]))
+        for k in range(m):
+            v, w = Y[k], Y[m + k]
+            out.append(-(v - a + b * w) / c + kw * (Y[m + (k - 1) % m] - 2.0 * w + Y[m + (k + 1) % m]))
+        return out
+
+    def lap(u):
+        return np.roll(u, 1, -1) - 2.0 * u + np.roll(u, -1, -1)
+
+    def f_arr(Y):
+        v, w = Y[..., :m], Y[..., m:]
+        return np.concatenate([c * (v - v * v * v / 3.0 + w) + kv * lap(v), -(v - a + b * w) / c + kw * lap(w)], -1)
+
+    def jac_arr(Y):
+        v = Y[..., :m]
+        J = np.zeros(Y.shape[:-1] + (2 * m, 2 * m))
+        idx = np.arange(m)
+        for r0, kd in ((0, kv), (m, kw)):
+            J[..., r0 + idx, r0 + (idx - 1) % m] += kd
+            J[..., r0 + idx, r0 + (idx + 1) % m] += kd
+            J[..., r0 + idx, r0 + idx] += -2.0 * kd
+        J[..., idx, idx] += c * (1.0 - v * v)
+        J[..., idx, m + idx] += c
+        J[..., m + idx, idx] += -1.0 / c
+        J[..., m + idx, m + idx] += -b / c
+        return J
+
+    return IVP(comp, y0, t0, tmax, "fhn_rd", (a, b, c, kv, kw), f_arr, jac_arr)

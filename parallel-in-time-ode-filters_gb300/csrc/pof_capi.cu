@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/pof.h"
+#include "pof_dense.h"
 #include "pof_table.cuh"
 
 using namespace pof;
@@ -261,8 +262,15 @@ int pof_version(void) { return 2; }
 
 int pof_shape_supported(int32_t D, int32_t d) { return find_ops(POF_F64, D, d) != nullptr ? 1 : 0; }
 
+// Shapes the small-D tables do not compile, with D >= dense::kMinD, run on
+// the dense path (pof_dense.cu).
+static bool dense_shape(int dtype, int D, int d) {
+  return (dtype == POF_F64 || dtype == POF_F32) && D >= dense::kMinD && d >= 1 && !find_ops(dtype, D, d);
+}
+
 size_t pof_filtsmooth_workspace_bytes(int32_t dtype, int64_t n_steps, int32_t D, int32_t d) {
   if (n_steps < 1 || D < 1) return 0;
+  if (dense_shape(dtype, D, d)) return dense::workspace_bytes(dtype, 1, n_steps, D, d, 0);
   return plan_for(dtype, n_steps, D, d, false).total;
 }
 
@@ -277,6 +285,9 @@ static int filtsmooth_impl(int which, int32_t dtype, int64_t n, int32_t D, int32
                            size_t wsb, void* stream) {
   const Ops* ops = nullptr;
   int rc = check_common(dtype, n, D, d, &ops);
+  if (rc == POF_ERR_SHAPE && dense_shape(dtype, D, d))
+    return pof_dense_linear_filtsmooth(which, dtype, n, D, d, x0m, x0L, F, QL, fts, H, c, R, rs, om, oL, osc, 0, ws,
+                                       wsb, stream);
   if (rc) return rc;
   if (!x0m || !x0L || !F || !QL || !H || !c || !om || !oL || !ws) return POF_ERR_ARG;
   if (fts != 0 && fts != (int64_t)D * D) return POF_ERR_ARG;
@@ -329,6 +340,10 @@ int pof_smoothing(int32_t dtype, int64_t n_steps, int32_t D, const void* F, cons
     }
   }
   if (dtype != POF_F64 && dtype != POF_F32) return POF_ERR_DTYPE;
+  if (!ops && D >= dense::kMinD)
+    return pof_dense_linear_filtsmooth(POF_DENSE_SMOOTHING, dtype, n_steps, D, 1, filt_mean, filt_chol, F, QL,
+                                       ft_stride, nullptr, nullptr, nullptr, 0, out_mean, out_chol, out_scalars, 0,
+                                       workspace, workspace_bytes, stream);
   if (!ops) return POF_ERR_SHAPE;
   if (n_steps < 1 || !F || !QL || !filt_mean || !filt_chol || !out_mean || !out_chol || !workspace)
     return POF_ERR_ARG;
@@ -354,12 +369,50 @@ int pof_smoothing(int32_t dtype, int64_t n_steps, int32_t D, const void* F, cons
   return launch_status();
 }
 
+size_t pof_dense_workspace_bytes(int32_t dtype, int32_t which, int64_t n_steps, int32_t D, int32_t d,
+                                 int32_t chunks) {
+  if (dtype != POF_F64 && dtype != POF_F32) return 0;
+  if (which < POF_DENSE_FILTER || which > POF_DENSE_SMOOTHING || d < 1) return 0;
+  return dense::workspace_bytes(dtype, which, n_steps, D, d, chunks);
+}
+
+int pof_dense_linear_filtsmooth(int32_t which, int32_t dtype, int64_t n_steps, int32_t D, int32_t d,
+                                const void* x0_mean, const void* x0_chol, const void* F, const void* QL,
+                                int64_t ft_stride, const void* H, const void* c, const void* R, int64_t r_stride,
+                                void* out_mean, void* out_chol, double* out_scalars, int32_t chunks, void* workspace,
+                                size_t workspace_bytes, void* stream) {
+  if (dtype != POF_F64 && dtype != POF_F32) return POF_ERR_DTYPE;
+  if (which < POF_DENSE_FILTER || which > POF_DENSE_SMOOTHING) return POF_ERR_ARG;
+  if (n_steps < 1 || D < 1 || d < 1 || chunks < 0) return POF_ERR_ARG;
+  if (n_steps > 0x7fffffffLL || (int64_t)D * (D + d) > 0x7fffffffLL) return POF_ERR_ARG;
+  if (!x0_mean || !x0_chol || !F || !QL || !out_mean || !out_chol || !workspace) return POF_ERR_ARG;
+  if (which != POF_DENSE_SMOOTHING && (!H || !c)) return POF_ERR_ARG;
+  if (ft_stride != 0 && ft_stride != (int64_t)D * D) return POF_ERR_ARG;
+  if (R && r_stride != 0 && r_stride != (int64_t)d * d) return POF_ERR_ARG;
+  if (workspace_bytes < dense::workspace_bytes(dtype, which, n_steps, D, d, chunks)) return POF_ERR_WORKSPACE;
+  return dense::filtsmooth(which, dtype, n_steps, D, d, x0_mean, x0_chol, F, QL, ft_stride, H, c, R, r_stride,
+                           out_mean, out_chol, out_scalars, chunks, workspace, workspace_bytes,
+                           static_cast<cudaStream_t>(stream));
+}
+
 static int nordsieck_p01(int D, int d, double h, double* p0, double* p1) {
   return nordsieck_scales(D, d, h, p0, p1) ? POF_OK : POF_ERR_ARG;
 }
 
 int pof_linearize(int32_t dtype, int64_t n_steps, int32_t D, int32_t d, int32_t field, const void* params,
                   double h, const void* means, void* H, void* c, void* stream) {
+  if (field == FIELD_FHN_RD) {
+    // any shape: d = 2 x cells, D = d (q + 1)
+    if (dtype != POF_F64 && dtype != POF_F32) return POF_ERR_DTYPE;
+    if (n_steps < 1 || D < 1 || d < 2 || n_steps > 0x7fffffffLL) return POF_ERR_ARG;
+    if (d % 2) return POF_ERR_FIELD;
+    if (!params || !means || !H || !c) return POF_ERR_ARG;
+    double p0, p1;
+    int rc = nordsieck_p01(D, d, h, &p0, &p1);
+    if (rc) return rc;
+    return dense::linearize(dtype, n_steps, D, d, field, params, p0, p1, means, H, c,
+                            static_cast<cudaStream_t>(stream));
+  }
   const Ops* ops = nullptr;
   int rc = check_common(dtype, n_steps, D, d, &ops);
   if (rc) return rc;

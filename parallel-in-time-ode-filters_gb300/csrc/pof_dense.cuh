@@ -1,0 +1,424 @@
+// Dense linear algebra for large state dimensions (D >= 32): strided batched
+// GEMM, blocked Householder LQ ("tria") and triangular solves, on matrix
+// views with arbitrary row/column strides (a transpose is a view, not a
+// copy).  Every kernel runs one batch of independent matrices (the chunks of
+// the filter/smoother schedule, or the steps of a slab); the filter and
+// smoother of pof_dense.cu are written on top of these primitives.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "pof_dense_views.h"
+
+namespace pof {
+namespace dense {
+
+// ---------------------------------------------------------------------------
+// C = alpha * A B + beta * C, A (M x K), B (K x N), C (M x N) views; beta == 0
+// does not read C.  One CTA per BM x BN tile of one batch entry; the K loop
+// stages BK-deep tiles in shared memory with the loads ordered along
+// whichever index is contiguous in memory; each thread accumulates TM x TN
+// outputs strided across the tile.
+// ---------------------------------------------------------------------------
+template <typename T, int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    k_gemm(int M, int N, int K, T alpha, MV<T> A, MV<T> B, T beta, MV<T> C, int64_t b0) {
+  constexpr int NT = (BM / TM) * (BN / TN);
+  constexpr int TX = BN / TN;
+  constexpr int TY = BM / TM;
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
+  const int t = threadIdx.x;
+  const int64_t b = b0 + blockIdx.z;
+  const T* __restrict__ Ab = A.p + b * A.bs;
+  const T* __restrict__ Bb = B.p + b * B.bs;
+  T* Cb = C.p + b * C.bs;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int tx = t % TX, ty = t / TX;
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+  const bool a_kc = A.cs == 1;
+  const bool b_nc = B.cs == 1;
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int l = t; l < BM * BK; l += NT) {
+      int mm, kk;
+      if (a_kc) {
+        kk = l % BK;
+        mm = l / BK;
+      } else {
+        mm = l % BM;
+        kk = l / BM;
+      }
+      const int gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < M && gk < K) ? Ab[gm * A.rs + gk * A.cs] : T(0);
+    }
+    for (int l = t; l < BK * BN; l += NT) {
+      int nn, kk;
+      if (b_nc) {
+        nn = l % BN;
+        kk = l / BN;
+      } else {
+        kk = l % BK;
+        nn = l / BK;
+      }
+      const int gn = n0 + nn, gk = k0 + kk;
+      Bs[kk][nn] = (gn < N && gk < K) ? Bb[gk * B.rs + gn * B.cs] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[TM], bv[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + i * TY];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) bv[j] = Bs[kk][tx + j * TX];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int gm = m0 + ty + i * TY;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int gn = n0 + tx + j * TX;
+      if (gn >= N) continue;
+      T* c = Cb + gm * C.rs + gn * C.cs;
+      *c = beta == T(0) ? alpha * acc[i][j] : fma(alpha, acc[i][j], beta * *c);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Blocked Householder LQ (tria): W (m x n, n >= m) is overwritten so that its
+// first m columns hold L (lower triangular, zeros above the diagonal) with
+// L L^T = W W^T and columns m..n-1 are zero.  Row reflectors with LAPACK's
+// dlarfg convention (beta = -sign(alpha) * ||x||, tau = (beta - alpha) /
+// beta, tau = 0 when the tail is zero), the signs numpy.linalg.qr of W^T
+// gives.  Panels of nb rows: k_tria_panel factors the panel rows in shared
+// memory and writes V (unit upper trapezoidal, nb x n') and T V (the compact
+// WY factor applied from the right, H_0 ... H_{nb-1} = I - V^T T V); two
+// GEMMs then update the rows below: W_tr <- W_tr - (W_tr V^T)(T V).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ inline T block_sum(T v, T* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T s = T(0);
+  for (int w = 0; w < nw; ++w) s += red[w];
+  return s;
+}
+
+template <typename T>
+__device__ inline T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One CTA per batch entry.  Dynamic shared memory: nbb * np elements.
+// V and TV are nbb x np, row-major, vbs elements apart per batch entry.
+template <typename T>
+__global__ void __launch_bounds__(512)
+    k_tria_panel(MV<T> W, int i0, int nbb, int np, T* __restrict__ V, T* __restrict__ TV, int64_t vbs, int64_t b0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* P = reinterpret_cast<T*>(smem_raw);
+  __shared__ T red[32];
+  __shared__ T tau[kMaxPanel], beta[kMaxPanel];
+  __shared__ T Tm[kMaxPanel][kMaxPanel + 1];
+  __shared__ T G[kMaxPanel][kMaxPanel + 1];
+  const int t = threadIdx.x, bd = blockDim.x;
+  const int lane = t & 31, warp = t >> 5, nw = bd >> 5;
+  const int64_t b = b0 + blockIdx.x;
+  T* Wb = W.p + b * W.bs + i0 * W.rs + i0 * W.cs;
+  for (int l = t; l < nbb * np; l += bd) {
+    const int r = l / np, c = l - r * np;
+    P[l] = Wb[r * W.rs + c * W.cs];
+  }
+  __syncthreads();
+  for (int j = 0; j < nbb; ++j) {
+    T* pr = P + j * np;
+    T s = T(0);
+    for (int c = j + 1 + t; c < np; c += bd) s += pr[c] * pr[c];
+    s = block_sum(s, red);
+    const T alpha = pr[j];
+    T bj, tj, scale;
+    if (s == T(0)) {
+      tj = T(0);
+      bj = alpha;
+      scale = T(0);
+    } else {
+      const T h = hypot(alpha, sqrt(s));
+      bj = alpha >= T(0) ? -h : h;
+      tj = (bj - alpha) / bj;
+      scale = T(1) / (alpha - bj);
+    }
+    __syncthreads();
+    for (int c = j + 1 + t; c < np; c += bd) pr[c] *= scale;
+    if (t == 0) {
+      pr[j] = T(1);
+      tau[j] = tj;
+      beta[j] = bj;
+    }
+    __syncthreads();
+    if (tj != T(0)) {
+      for (int r = j + 1 + warp; r < nbb; r += nw) {
+        T* q = P + r * np;
+        T dsum = T(0);
+        for (int c = j + lane; c < np; c += 32) dsum += q[c] * pr[c];
+        dsum = warp_sum(dsum) * tj;
+        for (int c = j + lane; c < np; c += 32) q[c] -= dsum * pr[c];
+      }
+    }
+    __syncthreads();
+  }
+  // panel rows of W: L entries left of the diagonal, beta on it, zeros right
+  for (int l = t; l < nbb * np; l += bd) {
+    const int r = l / np, c = l - r * np;
+    Wb[r * W.rs + c * W.cs] = c < r ? P[l] : (c == r ? beta[r] : T(0));
+  }
+  __syncthreads();
+  // P -> V (unit upper trapezoidal)
+  for (int l = t; l < nbb * np; l += bd) {
+    const int r = l / np, c = l - r * np;
+    if (c < r) P[l] = T(0);
+  }
+  __syncthreads();
+  // Gram matrix of the reflectors (upper part)
+  for (int pr_ = warp; pr_ < nbb * nbb; pr_ += nw) {
+    const int i = pr_ / nbb, j = pr_ - i * nbb;
+    if (i >= j) continue;
+    T dsum = T(0);
+    for (int c = j + lane; c < np; c += 32) dsum += P[i * np + c] * P[j * np + c];
+    dsum = warp_sum(dsum);
+    if (lane == 0) G[i][j] = dsum;
+  }
+  __syncthreads();
+  // T (upper triangular, forward column recurrence of dlarft)
+  if (warp == 0) {
+    for (int j = 0; j < nbb; ++j) {
+      if (lane < j) {
+        T acc = T(0);
+        for (int k = lane; k < j; ++k) acc += Tm[lane][k] * G[k][j];
+        Tm[lane][j] = -tau[j] * acc;
+      }
+      if (lane == 0) Tm[j][j] = tau[j];
+      if (lane > j && lane < nbb) Tm[lane][j] = T(0);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  T* Vb = V + (int64_t)blockIdx.x * vbs;
+  T* TVb = TV + (int64_t)blockIdx.x * vbs;
+  for (int c = t; c < np; c += bd) {
+    T v[kMaxPanel];
+#pragma unroll
+    for (int k = 0; k < kMaxPanel; ++k) v[k] = k < nbb ? P[k * np + c] : T(0);
+#pragma unroll
+    for (int i = 0; i < kMaxPanel; ++i) {
+      if (i >= nbb) break;
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < kMaxPanel; ++k)
+        if (k >= i && k < nbb) acc += Tm[i][k] * v[k];
+      Vb[i * np + c] = v[i];
+      TVb[i * np + c] = acc;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Triangular solves.  op(L) X = B in place in B (M x K), L an M x M view that
+// is lower triangular (`upper` == false) or upper triangular (a transposed
+// lower view).  Few columns: k_trsv, one CTA per (column, batch entry),
+// substitution with the right-hand side in shared memory.  Many columns:
+// blocks of 32 rows, GEMM updates from the solved blocks and k_trsm_diag on
+// the diagonal block (one thread per column).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_trsv(int M, MV<T> L, bool upper, MV<T> B, int64_t b0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s = reinterpret_cast<T*>(smem_raw);
+  T* x = s + M;
+  const int t = threadIdx.x, bd = blockDim.x;
+  const int64_t b = b0 + blockIdx.y;
+  const T* Lb = L.p + b * L.bs;
+  T* Bb = B.p + b * B.bs + blockIdx.x * B.cs;
+  for (int i = t; i < M; i += bd) s[i] = Bb[i * B.rs];
+  if (!upper) {
+    for (int i = 0; i < M; ++i) {
+      __syncthreads();
+      const T xi = s[i] / Lb[i * L.rs + i * L.cs];
+      for (int j = i + 1 + t; j < M; j += bd) s[j] -= Lb[j * L.rs + i * L.cs] * xi;
+      if (t == 0) x[i] = xi;
+    }
+  } else {
+    for (int i = M - 1; i >= 0; --i) {
+      __syncthreads();
+      const T xi = s[i] / Lb[i * L.rs + i * L.cs];
+      for (int j = t; j < i; j += bd) s[j] -= Lb[j * L.rs + i * L.cs] * xi;
+      if (t == 0) x[i] = xi;
+    }
+  }
+  __syncthreads();
+  for (int i = t; i < M; i += bd) Bb[i * B.rs] = x[i];
+}
+
+constexpr int kTrsmBlock = 32;
+
+template <typename T>
+__global__ void k_trsm_diag(int nbr, MV<T> L, bool upper, MV<T> B, int K, int64_t b0) {
+  __shared__ T Ls[kTrsmBlock][kTrsmBlock + 1];
+  const int t = threadIdx.x;
+  const int64_t b = b0 + blockIdx.y;
+  const T* Lb = L.p + b * L.bs;
+  for (int l = t; l < nbr * nbr; l += blockDim.x) {
+    const int i = l / nbr, j = l - i * nbr;
+    Ls[i][j] = Lb[i * L.rs + j * L.cs];
+  }
+  __syncthreads();
+  const int col = blockIdx.x * blockDim.x + t;
+  if (col >= K) return;
+  T* Bb = B.p + b * B.bs + col * B.cs;
+  T x[kTrsmBlock];
+#pragma unroll
+  for (int i = 0; i < kTrsmBlock; ++i) x[i] = i < nbr ? Bb[i * B.rs] : T(0);
+  if (!upper) {
+#pragma unroll
+    for (int i = 0; i < kTrsmBlock; ++i) {
+      if (i < nbr) {
+        T v = x[i];
+#pragma unroll
+        for (int j = 0; j < i; ++j) v -= Ls[i][j] * x[j];
+        x[i] = v / Ls[i][i];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = kTrsmBlock - 1; i >= 0; --i) {
+      if (i < nbr) {
+        T v = x[i];
+#pragma unroll
+        for (int j = i + 1; j < kTrsmBlock; ++j)
+          if (j < nbr) v -= Ls[i][j] * x[j];
+        x[i] = v / Ls[i][i];
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < kTrsmBlock; ++i)
+    if (i < nbr) Bb[i * B.rs] = x[i];
+}
+
+// ---------------------------------------------------------------------------
+// Elementwise: Y = alpha * X (+ beta * Y when beta != 0), a rows x cols block;
+// fill a block with `v` off the diagonal and `dv` on it.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_axpby2d(int rows, int cols, T alpha, MV<T> X, T beta, MV<T> Y, int64_t b0) {
+  const int64_t b = b0 + blockIdx.y;
+  const int64_t n = (int64_t)rows * cols;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(l / cols), j = (int)(l - (int64_t)i * cols);
+    T* y = Y.p + b * Y.bs + i * Y.rs + j * Y.cs;
+    const T x = X.p[b * X.bs + i * X.rs + j * X.cs];
+    *y = beta == T(0) ? alpha * x : fma(alpha, x, beta * *y);
+  }
+}
+
+template <typename T>
+__global__ void k_fill2d(int rows, int cols, T v, T dv, MV<T> Y, int64_t b0) {
+  const int64_t b = b0 + blockIdx.y;
+  const int64_t n = (int64_t)rows * cols;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(l / cols), j = (int)(l - (int64_t)i * cols);
+    Y.p[b * Y.bs + i * Y.rs + j * Y.cs] = i == j ? dv : v;
+  }
+}
+
+// Per-step filter terms from P11 (d x d lower), w = P11^{-1}(-r) and
+// wq = P11^{-T} r: nll = |w|^2 / 2 + sum log|P11_ii| + d log(2 pi) / 2
+// (pof/utils.py:22-30 negated), ssq = |wq|^2 (the whitened residual).
+template <typename T>
+__global__ void k_step_terms(int d, MV<T> P11, MV<T> w, MV<T> wq, double* __restrict__ nll,
+                             double* __restrict__ ssq, int64_t stride, int64_t b0) {
+  __shared__ double red[32];
+  const int64_t b = b0 + blockIdx.x;
+  double a = 0.0, q = 0.0, ld = 0.0;
+  for (int i = threadIdx.x; i < d; i += blockDim.x) {
+    const double wi = (double)w.p[b * w.bs + i * w.rs];
+    const double qi = (double)wq.p[b * wq.bs + i * wq.rs];
+    a += wi * wi;
+    q += qi * qi;
+    ld += log(fabs((double)P11.p[b * P11.bs + i * P11.rs + i * P11.cs]));
+  }
+  a = block_sum(a, red);
+  q = block_sum(q, red);
+  ld = block_sum(ld, red);
+  if (threadIdx.x == 0) {
+    nll[b * stride] = 0.5 * a + ld + 0.5 * d * 1.8378770664093453;  // log(2 pi)
+    ssq[b * stride] = q;
+  }
+}
+
+// out[b] = |x_b|^2 (x a vector of n entries per batch entry)
+template <typename T>
+__global__ void k_sqnorm(int n, MV<T> x, double* __restrict__ out, int64_t b0) {
+  __shared__ double red[32];
+  const int64_t b = b0 + blockIdx.x;
+  double a = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = (double)x.p[b * x.bs + i * x.rs];
+    a += v * v;
+  }
+  a = block_sum(a, red);
+  if (threadIdx.x == 0) out[b] = a;
+}
+
+// Final scalars: sums of the per-step terms in chunk order (per chunk, then
+// over chunks), written to out[POF_S_*]; ssq is divided by n * d.
+__global__ void k_dense_scalars(const double* __restrict__ nll, const double* __restrict__ ssq,
+                                const double* __restrict__ fobj, const double* __restrict__ sobj, int64_t n,
+                                int64_t C0, int d, double* __restrict__ out, int which) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double sn = 0.0, ss = 0.0, sf = 0.0, so = 0.0;
+  for (int64_t s = 0; s < n; s += C0) {
+    const int64_t e = s + C0 < n ? s + C0 : n;
+    double cn = 0.0, cs = 0.0, cf = 0.0, co = 0.0;
+    for (int64_t k = s; k < e; ++k) {
+      if (nll) cn += nll[k];
+      if (ssq) cs += ssq[k];
+      if (fobj) cf += fobj[k];
+      if (sobj) co += sobj[k];
+    }
+    sn += cn;
+    ss += cs;
+    sf += cf;
+    so += co;
+  }
+  if (which == 2) {  // smoothing alone
+    out[1] = so;
+    return;
+  }
+  out[0] = sn;
+  out[2] = ss / (double)n / (double)d;
+  out[3] = sf;
+  out[1] = which == 0 ? sf : so;
+  out[4] = 0.0;
+}
+
+}  // namespace dense
+}  // namespace pof

@@ -1,0 +1,423 @@
+// The dense filter/smoother schedule (host code), written against a launch
+// context X that provides the batched primitives on strided views:
+//   gemm(batch, M, N, K, alpha, A, B, beta, C)     C = alpha A B + beta C
+//   axpby(batch, rows, cols, alpha, X, beta, Y)    Y = alpha X + beta Y
+//   copy(batch, rows, cols, X, Y), fill(batch, rows, cols, v, diag_v, Y)
+//   tria(batch, m, n, W)                           W (m x n, n >= m) -> L in
+//                                                  its first m columns, zeros
+//                                                  elsewhere (L L^T = W W^T)
+//   trsm(batch, M, K, L, upper, B)                 op(L) X = B in place
+//   step_terms(batch, d, P11, w, wq, nll, ssq, stride), sqnorm(batch, len, x, out),
+//   scalars(nll, ssq, fobj, sobj, n, C0, d, out, which)
+// pof_dense.cu runs it with CUDA kernels; tests/dense_sched_cpu.cpp runs the
+// same code with host loops that check every access against the buffers.
+#pragma once
+
+#include <stdint.h>
+#include <stdlib.h>
+
+#include <algorithm>
+
+#include "pof_dense_views.h"
+
+namespace pof {
+namespace dense {
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+constexpr size_t kSlabBytes = size_t(1) << 30;
+
+// Bump allocation of the workspace; with base == nullptr it only sizes.
+struct Arena {
+  char* base;
+  size_t off = 0;
+  template <typename T>
+  T* take(int64_t count) {
+    off = (off + 255) & ~size_t(255);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += size_t(count) * sizeof(T);
+    return p;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// workspace layout (the same code sizes and carves it)
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Layout {
+  int64_t n;
+  int D, d, P, C0, last, S;
+  int64_t maxbatch;
+  // filter
+  T *Ab[2], *Lc, *eta, *Z, *X1, *X2, *X3, *Gr;
+  T *X4, *Mm, *X5, *v1, *v2, *v3, *v4;
+  T *Sm, *SL, *Lk, *mk[2], *rb, *wb, *wq;
+  double *nll, *ssq, *fobj, *sobj;
+  // smoother
+  T *E, *Dm, *g, *Phi, *tE[2], *tD, *tg, *Xs, *em, *eL, *tm, *ftmp;
+  // objectives
+  T* R;
+  // tria scratch
+  T *V, *TV, *Y;
+  int64_t vbs, ybs;
+  size_t total;
+
+  // active chunks at step offset s of a chunk (only the last can be short)
+  int active(int s) const { return s < last ? P : P - 1; }
+};
+
+inline void plan_chunks(int64_t n, int chunks, int* P, int* C0, int* last) {
+  int64_t p = chunks > 0 ? chunks : 64;
+  const char* e = getenv("POF_DENSE_CHUNKS");
+  if (chunks <= 0 && e && atoi(e) > 0) p = atoi(e);
+  p = std::max<int64_t>(1, std::min<int64_t>(p, n));
+  const int64_t c0 = cdiv(n, p);
+  p = cdiv(n, c0);
+  *P = (int)p;
+  *C0 = (int)c0;
+  *last = (int)(n - (p - 1) * c0);
+}
+
+template <typename T>
+Layout<T> layout(char* base, int which, int64_t n, int D, int d, int chunks) {
+  Layout<T> L{};
+  L.n = n;
+  L.D = D;
+  L.d = d;
+  plan_chunks(n, chunks, &L.P, &L.C0, &L.last);
+  const int64_t P = L.P, DD = (int64_t)D * D;
+  const int64_t es = sizeof(T);
+  int64_t S = std::max<int64_t>(1, (int64_t)(kSlabBytes / (size_t(4 * DD) * es)));
+  S = std::min<int64_t>(std::min<int64_t>(S, n), 4096);
+  L.S = (int)S;
+  Arena a{base};
+  const bool filt = which != 2, smo = which != 0;
+  if (filt) {
+    L.Ab[0] = a.take<T>(P * D * (D + 1));
+    L.Ab[1] = a.take<T>(P * D * (D + 1));
+    L.Lc = a.take<T>(P * DD);
+    L.eta = a.take<T>(P * D);
+    L.Z = a.take<T>(P * DD);
+    L.X1 = a.take<T>(P * D * 2 * D);
+    L.X2 = a.take<T>(P * (int64_t)(D + d) * (D + d));
+    L.X3 = a.take<T>(P * D * (int64_t)(D + d));
+    L.Gr = a.take<T>(P * d * (int64_t)(D + 1));
+    L.X4 = a.take<T>(4 * DD);
+    L.Mm = a.take<T>(DD);
+    L.X5 = a.take<T>(2 * DD);
+    L.v1 = a.take<T>(D);
+    L.v2 = a.take<T>(D);
+    L.v3 = a.take<T>(D);
+    L.v4 = a.take<T>(D);
+    L.Sm = a.take<T>(P * D);
+    L.SL = a.take<T>(P * DD);
+    L.Lk = a.take<T>(P * DD);
+    L.mk[0] = a.take<T>(P * D);
+    L.mk[1] = a.take<T>(P * D);
+    L.rb = a.take<T>(P * d);
+    L.wb = a.take<T>(P * d);
+    L.wq = a.take<T>(P * d);
+    L.nll = a.take<double>(n);
+    L.ssq = a.take<double>(n);
+    L.fobj = a.take<double>(n);
+  }
+  if (smo) {
+    L.E = a.take<T>(n * DD);
+    L.Dm = a.take<T>(n * DD);
+    L.g = a.take<T>(n * D);
+    L.Phi = a.take<T>(S * 4 * DD);
+    L.tE[0] = a.take<T>(P * DD);
+    L.tE[1] = a.take<T>(P * DD);
+    L.tD = a.take<T>(P * DD);
+    L.tg = a.take<T>(P * D);
+    L.Xs = a.take<T>(P * 2 * DD);
+    L.em = a.take<T>(P * D);
+    L.eL = a.take<T>(P * DD);
+    L.tm = a.take<T>(P * D);
+    L.ftmp = a.take<T>(std::max<int64_t>(S, P) * D);
+    L.sobj = a.take<double>(n);
+    if (!filt) {
+      L.X5 = a.take<T>(2 * DD);
+      L.Mm = a.take<T>(DD);
+      L.v1 = a.take<T>(D);
+      L.v2 = a.take<T>(D);
+    }
+  }
+  L.R = a.take<T>(n * D);
+  const int nmax = std::max(2 * D, D + d), mmax = std::max(2 * D, D + d);
+  L.maxbatch = std::max<int64_t>(P, S);
+  L.vbs = (int64_t)kMaxPanel * nmax;
+  L.ybs = (int64_t)mmax * kMaxPanel;
+  L.V = a.take<T>(L.maxbatch * L.vbs);
+  L.TV = a.take<T>(L.maxbatch * L.vbs);
+  L.Y = a.take<T>(L.maxbatch * L.ybs);
+  L.total = a.off + 256;  // alignment slack of aligned_ws
+  return L;
+}
+
+template <typename T>
+struct Model {
+  const T *F, *QL;
+  int64_t fts;
+  const T *H, *c, *R;
+  int64_t rst;
+};
+
+template <typename T>
+MV<T> cv(const T* p, int64_t rs, int64_t cs, int64_t bs) {
+  return MV<T>{const_cast<T*>(p), rs, cs, bs};
+}
+
+// obj[k] = |QL_k^{-1} (M[k] - F_k M[k+1])|^2, k < n (pof/utils.py:97-101).
+template <typename T, typename X>
+void objective(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t fts, const T* M, double* obj) {
+  const int D = L.D;
+  const int64_t n = L.n;
+  MV<T> Rv = rowmajor(L.R, D, 0);
+  cx.copy(1, (int)n, D, cv(M, D, 1, 0), Rv);
+  if (fts == 0) {
+    cx.gemm(1, (int)n, D, D, T(-1), cv(M + D, D, 1, 0), tr(cv(F, D, 1, 0)), T(1), Rv);
+    cx.trsm(1, D, (int)n, cv(QL, D, 1, 0), false, tr(Rv));
+  } else {
+    MV<T> rv{L.R, 1, 1, D};
+    cx.gemm(n, D, 1, D, T(-1), cv(F, D, 1, fts), cv(M + D, 1, 1, D), T(1), rv);
+    cx.trsm(n, D, 1, cv(QL, D, 1, fts), false, rv);
+  }
+  cx.sqnorm(n, D, MV<T>{L.R, 1, 1, D}, obj);
+}
+
+template <typename T, typename X>
+void run_filter(X& cx, const Layout<T>& L, const Model<T>& md, const T* x0m, const T* x0L, T* om, T* oL) {
+  const int D = L.D, d = L.d, P = L.P, C0 = L.C0;
+  const int64_t DD = (int64_t)D * D;
+  const T one(1), zero(0);
+  auto Fv = [&](int s) { return cv(md.F + s * md.fts, D, 1, C0 * md.fts); };
+  auto QLv = [&](int s) { return cv(md.QL + s * md.fts, D, 1, C0 * md.fts); };
+  auto Hv = [&](int s) { return cv(md.H + (int64_t)s * d * D, D, 1, (int64_t)C0 * d * D); };
+  auto cvec = [&](int s) { return cv(md.c + (int64_t)s * d, 1, 1, (int64_t)C0 * d); };
+  auto Rv = [&](int s) { return cv(md.R + s * md.rst, d, 1, C0 * md.rst); };
+  const MV<T> X1v = rowmajor(L.X1, 2 * D, 2 * DD);
+  const MV<T> X2v = rowmajor(L.X2, D + d, (int64_t)(D + d) * (D + d));
+  const MV<T> X3v = rowmajor(L.X3, D + d, (int64_t)D * (D + d));
+  const MV<T> Grv = rowmajor(L.Gr, D + 1, (int64_t)d * (D + 1));
+  const MV<T> Lcv = rowmajor(L.Lc, D, DD), Zv = rowmajor(L.Z, D, DD);
+  const MV<T> etav{L.eta, 1, 1, D};
+  MV<T> Abv[2] = {rowmajor(L.Ab[0], D + 1, (int64_t)D * (D + 1)), rowmajor(L.Ab[1], D + 1, (int64_t)D * (D + 1))};
+  const MV<T> P11 = X2v, P21 = sub(X2v, d, 0), U = sub(X2v, d, d);
+
+  // The X2 assembly [[H Lp, R], [Lp, 0]] from Lp = X1[:, :D] and its tria.
+  auto observe = [&](int Pa, int s) {
+    cx.gemm(Pa, d, D, D, one, Hv(s), X1v, zero, X2v);
+    if (md.R)
+      cx.copy(Pa, d, d, Rv(s), sub(X2v, 0, D));
+    else
+      cx.fill(Pa, d, d, zero, zero, sub(X2v, 0, D));
+    cx.copy(Pa, D, D, X1v, sub(X2v, d, 0));
+    cx.fill(Pa, D, d, zero, zero, sub(X2v, d, D));
+    cx.tria(Pa, d + D, D + d, X2v);
+  };
+  auto predict = [&](int Pa, int s, MV<T> Lprev) {
+    cx.gemm(Pa, D, D, D, one, Fv(s), Lprev, zero, X1v);
+    cx.copy(Pa, D, D, QLv(s), sub(X1v, 0, D));
+    cx.tria(Pa, D, 2 * D, X1v);
+  };
+
+  // phase 1: conditional fold of every chunk
+  cx.fill(P, D, D + 1, zero, one, Abv[0]);
+  cx.fill(P, D, D, zero, zero, Lcv);
+  cx.fill(P, D, 1, zero, zero, etav);
+  cx.fill(P, D, D, zero, zero, Zv);
+  int cur = 0;
+  for (int s = 0; s < C0; ++s) {
+    const int Pa = L.active(s);
+    predict(Pa, s, Lcv);
+    observe(Pa, s);
+    MV<T> FAb = Abv[1 - cur];
+    cx.gemm(Pa, D, D + 1, D, one, Fv(s), Abv[cur], zero, FAb);
+    cx.gemm(Pa, d, D + 1, D, one, Hv(s), FAb, zero, Grv);
+    cx.axpby(Pa, d, 1, one, cvec(s), one, sub(Grv, 0, D));
+    cx.trsm(Pa, d, D + 1, P11, false, Grv);
+    cx.gemm(Pa, D, D + 1, d, T(-1), P21, Grv, one, FAb);
+    // (a short last chunk's total may stay in the other buffer: phase 2
+    // reads the totals of chunks 0..P-2 only, which are active every step)
+    cur = 1 - cur;
+    cx.gemm(Pa, D, 1, d, T(-1), tr(Grv), sub(Grv, 0, D), one, etav);
+    cx.copy(Pa, D, D, Zv, X3v);
+    cx.copy(Pa, D, d, tr(Grv), sub(X3v, 0, D));
+    cx.tria(Pa, D, D + d, X3v);
+    cx.copy(Pa, D, D, X3v, Zv);
+    cx.copy(Pa, D, D, U, Lcv);
+  }
+
+  // phase 2: the state at every chunk start
+  const MV<T> Smv{L.Sm, 1, 1, D}, SLv = rowmajor(L.SL, D, DD);
+  cx.copy(1, D, 1, cv(x0m, 1, 1, 0), Smv);
+  cx.copy(1, D, D, cv(x0L, D, 1, 0), SLv);
+  const MV<T> X4v = rowmajor(L.X4, 2 * D, 0), Mmv = rowmajor(L.Mm, D, 0), X5v = rowmajor(L.X5, 2 * D, 0);
+  const MV<T> v1{L.v1, 1, 1, 0}, v2{L.v2, 1, 1, 0}, v3{L.v3, 1, 1, 0}, v4{L.v4, 1, 1, 0};
+  for (int j = 0; j + 1 < P; ++j) {
+    const MV<T> b1{L.Sm + (int64_t)j * D, 1, 1, 0}, U1 = rowmajor(L.SL + j * DD, D, 0);
+    const MV<T> A2 = rowmajor(L.Ab[cur] + (int64_t)j * D * (D + 1), D + 1, 0), b2 = sub(A2, 0, D);
+    const MV<T> U2 = rowmajor(L.Lc + j * DD, D, 0), Z2 = rowmajor(L.Z + j * DD, D, 0);
+    const MV<T> eta2{L.eta + (int64_t)j * D, 1, 1, 0};
+    cx.gemm(1, D, D, D, one, tr(U1), Z2, zero, X4v);
+    cx.fill(1, D, D, zero, one, sub(X4v, 0, D));
+    cx.copy(1, D, D, Z2, sub(X4v, D, 0));
+    cx.fill(1, D, D, zero, zero, sub(X4v, D, D));
+    cx.tria(1, 2 * D, 2 * D, X4v);
+    const MV<T> Xi11 = X4v, Xi21 = sub(X4v, D, 0);
+    cx.copy(1, D, D, tr(U1), Mmv);
+    cx.trsm(1, D, D, Xi11, false, Mmv);
+    cx.gemm(1, D, 1, D, one, tr(U1), eta2, zero, v1);
+    cx.copy(1, D, 1, b1, v2);
+    cx.gemm(1, D, 1, D, one, U1, v1, one, v2);
+    cx.gemm(1, D, 1, D, one, tr(Xi21), v2, zero, v3);
+    cx.copy(1, D, 1, v2, v4);
+    cx.gemm(1, D, 1, D, T(-1), tr(Mmv), v3, one, v4);
+    const MV<T> bn{L.Sm + (int64_t)(j + 1) * D, 1, 1, 0};
+    cx.copy(1, D, 1, b2, bn);
+    cx.gemm(1, D, 1, D, one, A2, v4, one, bn);
+    cx.gemm(1, D, D, D, one, A2, tr(Mmv), zero, X5v);
+    cx.copy(1, D, D, U2, sub(X5v, 0, D));
+    cx.tria(1, D, 2 * D, X5v);
+    cx.copy(1, D, D, X5v, rowmajor(L.SL + (j + 1) * DD, D, 0));
+  }
+
+  // phase 3: the Kalman filter of every chunk from its start state
+  const MV<T> Lkv = rowmajor(L.Lk, D, DD);
+  MV<T> mkv[2] = {MV<T>{L.mk[0], 1, 1, D}, MV<T>{L.mk[1], 1, 1, D}};
+  const MV<T> rbv{L.rb, 1, 1, d}, wbv{L.wb, 1, 1, d}, wqv{L.wq, 1, 1, d};
+  cx.copy(P, D, D, SLv, Lkv);
+  cx.copy(P, D, 1, Smv, mkv[0]);
+  cx.copy(1, D, 1, cv(x0m, 1, 1, 0), MV<T>{om, 1, 1, 0});
+  cx.copy(1, D, D, cv(x0L, D, 1, 0), rowmajor(oL, D, 0));
+  cur = 0;
+  for (int s = 0; s < C0; ++s) {
+    const int Pa = L.active(s);
+    predict(Pa, s, Lkv);
+    MV<T> mp = mkv[1 - cur];
+    cx.gemm(Pa, D, 1, D, one, Fv(s), mkv[cur], zero, mp);
+    observe(Pa, s);
+    cx.copy(Pa, d, 1, cvec(s), rbv);
+    cx.gemm(Pa, d, 1, D, one, Hv(s), mp, one, rbv);
+    cx.axpby(Pa, d, 1, T(-1), rbv, zero, wbv);
+    cx.trsm(Pa, d, 1, P11, false, wbv);
+    cx.copy(Pa, d, 1, rbv, wqv);
+    cx.trsm(Pa, d, 1, tr(P11), true, wqv);
+    cx.step_terms(Pa, d, P11, wbv, wqv, L.nll + s, L.ssq + s, C0);
+    cx.gemm(Pa, D, 1, d, one, P21, wbv, one, mp);
+    cx.copy(Pa, D, 1, mp, MV<T>{om + (int64_t)(s + 1) * D, 1, 1, (int64_t)C0 * D});
+    cx.copy(Pa, D, D, U, rowmajor(oL + (s + 1) * DD, D, C0 * DD));
+    cx.copy(Pa, D, D, U, Lkv);
+    cur = 1 - cur;
+  }
+  objective(cx, L, md.F, md.QL, md.fts, om, L.fobj);
+}
+
+template <typename T, typename X>
+void run_smoother(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t fts, T* om, T* oL) {
+  const int D = L.D, P = L.P, C0 = L.C0;
+  const int64_t n = L.n, DD = (int64_t)D * D;
+  const T one(1), zero(0);
+  // elements (g, E, D) of every step, in slabs of S steps
+  const MV<T> Phiv = rowmajor(L.Phi, 2 * D, 4 * DD);
+  for (int64_t k0 = 0; k0 < n; k0 += L.S) {
+    const int64_t Sb = std::min<int64_t>(L.S, n - k0);
+    const MV<T> Fk = cv(F + k0 * fts, D, 1, fts), QLk = cv(QL + k0 * fts, D, 1, fts);
+    const MV<T> Lk = rowmajor(oL + k0 * DD, D, DD);
+    const MV<T> mk{om + k0 * D, 1, 1, D};
+    const MV<T> Ek = rowmajor(L.E + k0 * DD, D, DD), Dk = rowmajor(L.Dm + k0 * DD, D, DD);
+    const MV<T> gk{L.g + k0 * D, 1, 1, D}, ft{L.ftmp, 1, 1, D};
+    cx.gemm(Sb, D, D, D, one, Fk, Lk, zero, Phiv);
+    cx.copy(Sb, D, D, QLk, sub(Phiv, 0, D));
+    cx.copy(Sb, D, D, Lk, sub(Phiv, D, 0));
+    cx.fill(Sb, D, D, zero, zero, sub(Phiv, D, D));
+    cx.tria(Sb, 2 * D, 2 * D, Phiv);
+    cx.trsm(Sb, D, D, tr(Phiv), true, tr(sub(Phiv, D, 0)));  // P21 block := E = P21 P11^{-1}
+    cx.copy(Sb, D, D, sub(Phiv, D, 0), Ek);
+    cx.copy(Sb, D, D, sub(Phiv, D, D), Dk);
+    cx.gemm(Sb, D, 1, D, one, Fk, mk, zero, ft);
+    cx.copy(Sb, D, 1, mk, gk);
+    cx.gemm(Sb, D, 1, D, T(-1), Ek, ft, one, gk);
+  }
+  auto Ev = [&](int off) { return rowmajor(L.E + off * DD, D, C0 * DD); };
+  auto Dv = [&](int off) { return rowmajor(L.Dm + off * DD, D, C0 * DD); };
+  auto gv = [&](int off) { return MV<T>{L.g + (int64_t)off * D, 1, 1, (int64_t)C0 * D}; };
+  MV<T> tEv[2] = {rowmajor(L.tE[0], D, DD), rowmajor(L.tE[1], D, DD)};
+  const MV<T> tDv = rowmajor(L.tD, D, DD), tgv{L.tg, 1, 1, D};
+  const MV<T> Xsv = rowmajor(L.Xs, 2 * D, 2 * DD);
+  // composite of every chunk's elements (sqrt_smoothing_operator, later
+  // element first).  The product E_tot E_i goes to scratch and is copied
+  // back, so a short last chunk keeps its total in place while the others
+  // go on.
+  cx.copy(P, D, D, Ev(0), tEv[0]);
+  cx.copy(P, D, D, Dv(0), tDv);
+  cx.copy(P, D, 1, gv(0), tgv);
+  const int ce = 0;
+  for (int off = 1; off < C0; ++off) {
+    const int Pa = L.active(off);
+    cx.gemm(Pa, D, D, D, one, tEv[0], Ev(off), zero, tEv[1]);
+    cx.gemm(Pa, D, 1, D, one, tEv[0], gv(off), one, tgv);
+    cx.gemm(Pa, D, D, D, one, tEv[0], Dv(off), zero, Xsv);
+    cx.copy(Pa, D, D, tDv, sub(Xsv, 0, D));
+    cx.tria(Pa, D, 2 * D, Xsv);
+    cx.copy(Pa, D, D, Xsv, tDv);
+    cx.copy(Pa, D, D, tEv[1], tEv[0]);
+  }
+  // smoothed state at every chunk end, from the terminal (filtered) state
+  const MV<T> emv{L.em, 1, 1, D}, eLv = rowmajor(L.eL, D, DD);
+  const MV<T> cm{L.v2, 1, 1, 0}, cL = rowmajor(L.Mm, D, 0), X5v = rowmajor(L.X5, 2 * D, 0);
+  const MV<T> v1{L.v1, 1, 1, 0};
+  cx.copy(1, D, 1, MV<T>{om + n * D, 1, 1, 0}, cm);
+  cx.copy(1, D, D, rowmajor(oL + n * DD, D, 0), cL);
+  for (int j = P - 1; j >= 0; --j) {
+    cx.copy(1, D, 1, cm, MV<T>{L.em + (int64_t)j * D, 1, 1, 0});
+    cx.copy(1, D, D, cL, rowmajor(L.eL + j * DD, D, 0));
+    if (j == 0) break;
+    const MV<T> Ej = rowmajor(L.tE[ce] + j * DD, D, 0), Dj = rowmajor(L.tD + j * DD, D, 0);
+    const MV<T> gj{L.tg + (int64_t)j * D, 1, 1, 0};
+    cx.copy(1, D, 1, gj, v1);
+    cx.gemm(1, D, 1, D, one, Ej, cm, one, v1);
+    cx.gemm(1, D, D, D, one, Ej, cL, zero, X5v);
+    cx.copy(1, D, D, Dj, sub(X5v, 0, D));
+    cx.tria(1, D, 2 * D, X5v);
+    cx.copy(1, D, 1, v1, cm);
+    cx.copy(1, D, D, X5v, cL);
+  }
+  // backward recursion inside every chunk
+  const MV<T> tmv{L.tm, 1, 1, D};
+  for (int off = C0 - 1; off >= 0; --off) {
+    const int Pa = L.active(off);
+    cx.copy(Pa, D, 1, gv(off), tmv);
+    cx.gemm(Pa, D, 1, D, one, Ev(off), emv, one, tmv);
+    cx.gemm(Pa, D, D, D, one, Ev(off), eLv, zero, Xsv);
+    cx.copy(Pa, D, D, Dv(off), sub(Xsv, 0, D));
+    cx.tria(Pa, D, 2 * D, Xsv);
+    cx.copy(Pa, D, 1, tmv, MV<T>{om + (int64_t)off * D, 1, 1, (int64_t)C0 * D});
+    cx.copy(Pa, D, D, Xsv, rowmajor(oL + off * DD, D, C0 * DD));
+    cx.copy(Pa, D, 1, tmv, emv);
+    cx.copy(Pa, D, D, Xsv, eLv);
+  }
+  objective(cx, L, F, QL, fts, om, L.sobj);
+}
+
+
+// The whole pass: which = 0 filter, 1 filter + smoother, 2 smoother (x0m /
+// x0L are the filtered means / chols, copied to om / oL first).
+template <typename T, typename X>
+void run_schedule(X& cx, const Layout<T>& L, int which, const T* x0m, const T* x0L, const T* F, const T* QL,
+                  int64_t fts, const T* H, const T* c, const T* R, int64_t rst, T* om, T* oL, double* osc) {
+  const int D = L.D;
+  const int64_t n = L.n;
+  if (which != 2) {
+    Model<T> md{F, QL, fts, H, c, R, R ? rst : 0};
+    run_filter(cx, L, md, x0m, x0L, om, oL);
+  } else {
+    if (om != x0m) cx.copy(1, (int)(n + 1), D, cv(x0m, D, 1, 0), rowmajor(om, D, 0));
+    if (oL != x0L) cx.copy(1, (int)((n + 1) * D), D, cv(x0L, D, 1, 0), rowmajor(oL, D, 0));
+  }
+  if (which != 0) run_smoother(cx, L, F, QL, fts, om, oL);
+  if (osc) cx.scalars(L.nll, L.ssq, L.fobj, L.sobj, n, L.C0, L.d, osc, which);
+}
+
+}  // namespace dense
+}  // namespace pof

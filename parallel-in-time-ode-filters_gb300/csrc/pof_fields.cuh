@@ -19,7 +19,10 @@ enum FieldId : int {
   FIELD_SEIR = 8,           // p = (p0, p1, p2, p3)                                  pof/ivp.py:93-108
   FIELD_THREEBODY = 9,      // p = (mu)                                              pof/ivp.py:111-126
   FIELD_HENONHEILES = 10,   // p = (p)                                               pof/ivp.py:137-152
-  FIELD_COUNT = 11,
+  FIELD_FHN_RD = 11,        // p = (a, b, c, kv, kw): FitzHugh-Nagumo on a periodic 1-D grid of d / 2
+                            // cells (method of lines), y = (v_0..v_{m-1}, w_0..w_{m-1}); any even d;
+                            // linearized by the dense path's kernel
+  FIELD_COUNT = 12,
 };
 
 __host__ __device__ inline int field_dim(int id) {
@@ -34,6 +37,7 @@ __host__ __device__ inline int field_dim(int id) {
     case FIELD_SEIR:
     case FIELD_THREEBODY:
     case FIELD_HENONHEILES: return 4;
+    case FIELD_FHN_RD: return 0;  // any even d
     default: return -1;
   }
 }
@@ -50,6 +54,7 @@ __host__ __device__ inline int field_nparams(int id) {
     case FIELD_LOTKAVOLTERRA:
     case FIELD_FITZHUGHNAGUMO:
     case FIELD_SEIR: return 4;
+    case FIELD_FHN_RD: return 5;
     default: return 0;
   }
 }

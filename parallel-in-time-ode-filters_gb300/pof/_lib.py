@@ -36,7 +36,12 @@ FIELDS = {
     "seir": 8,
     "threebody": 9,
     "henonheiles": 10,
+    "fhn_rd": 11,
 }
+# Built-in fields with a state dimension of the caller's choosing: linearized
+# by pof_linearize at any shape, solved by the host-driven IEKS loop
+# (pof.solver), never by the device loops.
+DENSE_FIELDS = frozenset({"fhn_rd"})
 
 
 class PofError(RuntimeError):
@@ -68,6 +73,12 @@ _SIGS = {
         [_i32, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _dp, _vp],
     ),
     "pof_smoothing": (_c.c_int, [_i32, _i64, _i32, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _dp, _vp, _sz, _vp]),
+    "pof_dense_workspace_bytes": (_sz, [_i32, _i32, _i64, _i32, _i32, _i32]),
+    "pof_dense_linear_filtsmooth": (
+        _c.c_int,
+        [_i32, _i32, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _dp, _i32, _vp, _sz,
+         _vp],
+    ),
     "pof_linearize": (_c.c_int, [_i32, _i64, _i32, _i32, _i32, _vp, _f64, _vp, _vp, _vp, _vp]),
     "pof_sequential_linear_filtsmooth": (
         _c.c_int,

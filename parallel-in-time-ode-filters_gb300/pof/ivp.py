@@ -155,3 +155,28 @@ def henonheiles(t0=0.0, tmax=100.0, y0=None, p=None):
         return torch.stack([y[2], y[3], -y[0] - 2 * p * y[0] * y[1], -y[1] - p * (y[0] ** 2 - y[1] ** 2)])
 
     return InitialValueProblem(_tag(f, "henonheiles", (p,)), t0, tmax, _y0(y0, [0.5, 0.0, 0.0, 0.1]))
+
+
+def fhn_reaction_diffusion(t0=0.0, tmax=20.0, y0=None, cells=64, a=0.2, b=0.2, c=3.0, kv=0.5, kw=0.05, amp=0.5):
+    """Method-of-lines FitzHugh-Nagumo reaction-diffusion system on a periodic
+    1-D grid of `cells` cells (d = 2 cells; not in the reference's pof.ivp):
+    v_k' = c (v_k - v_k^3 / 3 + w_k) + kv (v_{k-1} - 2 v_k + v_{k+1}),
+    w_k' = -(v_k - a + b w_k) / c + kw (w_{k-1} - 2 w_k + w_{k+1}),
+    kv, kw the diffusion coefficients over the squared cell width.  Default
+    initial state: v = -1 + amp sin(2 pi k / cells), w = 1 (the FitzHugh-Nagumo
+    y0 = (-1, 1) with a sine perturbation)."""
+    m = int(cells)
+    if y0 is None:
+        k = torch.arange(m, dtype=torch.float64)
+        y0 = torch.cat([-1.0 + amp * torch.sin(2.0 * torch.pi * k / m), torch.ones(m, dtype=torch.float64)])
+
+    def lap(u):
+        return torch.roll(u, 1, -1) - 2.0 * u + torch.roll(u, -1, -1)
+
+    def f(t, Y):
+        v, w = Y[..., :m], Y[..., m:]
+        dv = c * (v - v * v * v / 3.0 + w) + kv * lap(v)
+        dw = -(v - a + b * w) / c + kw * lap(w)
+        return torch.cat([dv, dw], -1)
+
+    return InitialValueProblem(_tag(f, "fhn_rd", (a, b, c, kv, kw)), t0, tmax, _y0(y0, None))

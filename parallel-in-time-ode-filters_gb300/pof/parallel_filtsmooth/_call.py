@@ -40,8 +40,15 @@ def observations(dom, n, D, dtype, device):
     return H, c, R, d * d, d
 
 
-def filtsmooth(which, x0: MVNSqrt, dtm, dom, stream=None):
-    """which = "filtsmooth" | "filter": run the chunked parallel pass in libpof."""
+DENSE_WHICH = {"filter": 0, "filtsmooth": 1, "smoothing": 2}
+
+
+def filtsmooth(which, x0: MVNSqrt, dtm, dom, stream=None, dense_chunks=None):
+    """which = "filtsmooth" | "filter": run the chunked parallel pass in libpof.
+    dense_chunks (an int >= 0): run libpof's dense path
+    (pof_dense_linear_filtsmooth) with that many chunks (0: its default),
+    whatever D is; None: libpof picks (the dense path for uncompiled shapes
+    with D >= 32)."""
     m0 = x0.mean
     device = m0.device if m0.is_cuda else torch.device("cuda", torch.cuda.current_device())
     dtype = m0.dtype if m0.dtype in (torch.float64, torch.float32) else torch.float64
@@ -56,6 +63,16 @@ def filtsmooth(which, x0: MVNSqrt, dtm, dom, stream=None):
     scal = torch.zeros(_lib.S_COUNT, dtype=torch.float64, device=device)
     lib = _lib.lib()
     code = _lib.dtype_code(dtype)
+    if dense_chunks is not None:
+        wh = DENSE_WHICH[which]
+        wsb = lib.pof_dense_workspace_bytes(code, wh, n, D, d, int(dense_chunks))
+        ws = _lib.workspace(wsb, device)
+        rc = lib.pof_dense_linear_filtsmooth(wh, code, n, D, d, _lib.ptr(m0), _lib.ptr(L0), _lib.ptr(F), _lib.ptr(QL),
+                                             fts, _lib.ptr(H), _lib.ptr(c), _lib.ptr(R), rs, _lib.ptr(means),
+                                             _lib.ptr(chols), _lib.ptr(scal), int(dense_chunks), _lib.ptr(ws), wsb,
+                                             _lib.stream_handle(stream))
+        _lib.check(rc, "pof_dense_linear_filtsmooth")
+        return MVNSqrt(means, chols), scal[_lib.S_NLL], scal[_lib.S_OBJ], scal[_lib.S_SSQ], scal
     wsb = lib.pof_filtsmooth_workspace_bytes(code, n, D, d)
     ws = _lib.workspace(wsb, device)
     fn = lib.pof_linear_filtsmooth if which == "filtsmooth" else lib.pof_linear_noiseless_filtering
@@ -66,7 +83,7 @@ def filtsmooth(which, x0: MVNSqrt, dtm, dom, stream=None):
     return MVNSqrt(means, chols), scal[_lib.S_NLL], scal[_lib.S_OBJ], scal[_lib.S_SSQ], scal
 
 
-def smoothing(dtm, filt: MVNSqrt, stream=None):
+def smoothing(dtm, filt: MVNSqrt, stream=None, dense_chunks=None):
     fm, fL = filt
     device = fm.device
     dtype = fm.dtype
@@ -81,6 +98,15 @@ def smoothing(dtm, filt: MVNSqrt, stream=None):
     lib = _lib.lib()
     code = _lib.dtype_code(dtype)
     d = 1  # the smoother's workspace does not depend on d
+    if dense_chunks is not None:
+        wsb = lib.pof_dense_workspace_bytes(code, 2, n, D, d, int(dense_chunks))
+        ws = _lib.workspace(wsb, device)
+        rc = lib.pof_dense_linear_filtsmooth(2, code, n, D, d, _lib.ptr(fm), _lib.ptr(fL), _lib.ptr(F), _lib.ptr(QL),
+                                             fts, None, None, None, 0, _lib.ptr(means), _lib.ptr(chols),
+                                             _lib.ptr(scal), int(dense_chunks), _lib.ptr(ws), wsb,
+                                             _lib.stream_handle(stream))
+        _lib.check(rc, "pof_dense_linear_filtsmooth")
+        return MVNSqrt(means, chols), scal[_lib.S_OBJ]
     wsb = lib.pof_filtsmooth_workspace_bytes(code, n, D, d)
     ws = _lib.workspace(wsb, device)
     rc = lib.pof_smoothing(code, n, D, _lib.ptr(F), _lib.ptr(QL), fts, _lib.ptr(fm), _lib.ptr(fL), _lib.ptr(means),

@@ -6,6 +6,7 @@ from . import _lib
 from . import convergence_criteria
 from .convenience import get_initial_trajectory, set_up_solver, set_up_solver_no_precond
 from .sequential_filtsmooth import filtsmooth as seq_fs
+from .parallel_filtsmooth import linear_filtsmooth as parallel_linear_filtsmooth
 from .step import ieks_step
 from .utils import MVNSqrt, gmul_stack
 
@@ -92,14 +93,74 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     x0 = setup["x0"]
     states = get_initial_trajectory(setup, method=init)
 
-    builtin = om.field is not None and _lib.shape_supported(x0.mean.shape[0], setup["iwp"].wiener_process_dimension)
+    builtin = (om.field is not None and om.field[0] not in _lib.DENSE_FIELDS
+               and _lib.shape_supported(x0.mean.shape[0], setup["iwp"].wiener_process_dimension))
     if builtin and (not sequential or precision == "float64"):
         states, info_dict = _solve_builtin(setup, states, calibrate, maxiters, precision, maxiters_f32, rtol_f32,
                                            settle_f32, sequential=sequential)
         return gmul_stack(setup["E0"], states), info_dict
+    if precision == "mixed" and om.field is not None and not sequential:
+        # fields without a device loop at this shape (the dense path's):
+        # the same float32 phase and float64 polish, driven from the host
+        means, it32, best = _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32)
+        out, info_dict = _solve_loop(setup, MVNSqrt(means, states.chol), calibrate, maxiters, sequential)
+        info_dict["iterations_float32"] = torch.tensor(it32)
+        info_dict["best_change_float32"] = torch.tensor(best, dtype=torch.float64)
+        return out, info_dict
     if precision != "float64":
         raise NotImplementedError("precision=%r needs a built-in field (pof.ivp)" % (precision,))
     return _solve_loop(setup, states, calibrate, maxiters, sequential)
+
+
+def _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32):
+    """The float32 iterations of pof_ieks_solve_mixed, driven from the host
+    (for fields the device loops do not take, e.g. the dense path's): each
+    linearizes in float64 at the current trajectory, scales every observation
+    row to unit norm (the same constraint, a smaller range), filters and
+    smooths in float32 and converts the means back; a non-finite iterate is
+    dropped.  The phase ends when the largest change of y = E0 m falls below
+    rtol_f32 relative to max |y|, after three changes that did not shrink
+    once the smallest change is below settle_f32, or after maxiters_f32
+    iterations; a phase whose smallest change never came within 100 rtol_f32
+    is discarded.  Returns (float64 means, kept iterations, smallest change)."""
+    from .step import linearize_at_previous_states
+
+    dtm, om, x0 = setup["dtm"], setup["om"], setup["x0"]
+    E0 = setup["E0"]
+    F, QL = dtm.F, dtm.QL
+    if F.dim() == 3 and F.stride(0) == 0 and QL.stride(0) == 0:
+        F, QL = F[0], QL[0]  # one pair broadcast over the steps: convert it once
+    dtm32 = (F.to(torch.float32), QL.to(torch.float32))
+    x032 = MVNSqrt(x0.mean.to(torch.float32), x0.chol.to(torch.float32))
+    means = states.mean.to(torch.float64)
+    keep = means
+    it32, prev, best, worse = 0, float("inf"), float("inf"), 0
+    while it32 < maxiters_f32:
+        dom = linearize_at_previous_states(om, MVNSqrt(means, states.chol))
+        inv = 1.0 / torch.linalg.vector_norm(dom.H, dim=-1)
+        inv = torch.where(torch.isfinite(inv), inv, torch.ones_like(inv))
+        H32 = (dom.H * inv[..., None]).to(torch.float32)
+        c32 = (dom.b * inv).to(torch.float32)
+        out, _, _, _ = parallel_linear_filtsmooth(x032, dtm32, (H32, c32, None))
+        cand = out.mean.to(torch.float64)
+        if not bool(torch.isfinite(cand).all()):
+            break
+        y_new, y_old = cand @ E0.T, means @ E0.T
+        dy = float((y_new - y_old).abs().max())
+        ay = float(y_old.abs().max())
+        it32 += 1
+        means = cand
+        rel = dy / ay if ay > 0 else dy
+        best = min(best, rel)
+        if rel < rtol_f32:
+            break
+        worse = worse + 1 if (rel >= prev and best < settle_f32) else (worse if rel >= prev else 0)
+        if worse >= 3:
+            break
+        prev = rel
+    if it32 > 0 and not best < 100.0 * rtol_f32:
+        return keep, 0, best
+    return means, it32, best
 
 
 def _solve_loop(setup, states, calibrate, maxiters, sequential):
