@@ -1571,6 +1571,113 @@ def run_mixed(args, workload):
     })
 
 
+DENSE_WORKLOADS = {
+    # name: (cells, q, N, tmax): the method-of-lines FitzHugh-Nagumo
+    # reaction-diffusion system (pof.ivp.fhn_reaction_diffusion: 64 periodic
+    # cells, d = 128, D = 640 at q = 4), uniform grid of N points
+    "rd_d640": (64, 4, 2 ** 12, 20.0),
+}
+
+
+def run_dense(args, workload):
+    """One IEKS iteration's work on the dense path (D >= 32): EK1
+    linearization of the reaction-diffusion field plus the dense filter +
+    smoother pass, float32 over the whole grid and float64 over its first
+    --dense-f64-steps steps (the per-step cost is uniform: the chunks run
+    their steps one after the other, the top levels add P - 1 boundary
+    steps), from the constant-init trajectory; with --dense-solve also the
+    whole mixed-precision solve (float32 iterations, float64 polish)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from pof import _build, _flops, _lib, ivp as pivp, solver as psolver
+    from pof.convenience import get_initial_trajectory, set_up_solver
+    from pof.parallel_filtsmooth import linear_filtsmooth
+    from pof.step import linearize_at_previous_states
+    from pof.utils import MVNSqrt
+
+    _build.build(verbose=False)
+    lib = _lib.lib()
+    cells, q, N, tmax = DENSE_WORKLOADS[workload]
+    if args.dense_n:
+        N = args.dense_n
+    pv = pivp.fhn_reaction_diffusion(cells=cells, tmax=tmax)
+    ts = torch.linspace(0.0, tmax, N, dtype=torch.float64)
+    setup = set_up_solver(f=pv.f, y0=pv.y0, ts=ts, order=q)
+    states = get_initial_trajectory(setup, method="constant")
+    D = states.mean.shape[1]
+    d = 2 * cells
+    n = N - 1
+    chunks = int(os.environ.get("POF_DENSE_CHUNKS", "64"))
+    x0, dtm = setup["x0"], setup["dtm"]
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts_ = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts_.append(e0.elapsed_time(e1))
+        return float(np.median(ts_))
+
+    out = {}
+    peak64 = fp64_peak(torch, lib, _lib)
+    passes = [("float32", n), ("float64", min(n, args.dense_f64_steps))]
+    passes = [pp for pp in passes if pp[0] in args.dense_precisions.split(",")]
+    for prec, nsteps in passes:
+        dt = torch.float32 if prec == "float32" else torch.float64
+        m = states.mean[: nsteps + 1]
+        sub = MVNSqrt(m, states.chol[: nsteps + 1])
+        F, QL = dtm.F[0].to(dt), dtm.QL[0].to(dt)
+        x0t = MVNSqrt(x0.mean.to(dt), x0.chol.to(dt))
+        res = {}
+
+        def one():
+            dom = linearize_at_previous_states(setup["om"], sub)
+            H, c = dom.H.to(dt), dom.b.to(dt)
+            res["out"] = linear_filtsmooth(x0t, (F, QL), (H, c, None))
+
+        ms = timed(one)
+        fl = _flops.dense_pass_flops(nsteps, D, d, min(chunks, nsteps))
+        finite = bool(torch.isfinite(res["out"][0].mean).all().item())
+        out[prec] = {"steps": nsteps, "ms_per_pass": ms, "ms_per_step": ms / nsteps, "gflops": fl / (ms * 1e-3) / 1e9,
+                     "flop_model_tflop": fl / 1e12, "finite": finite}
+    full64_ms = None
+    if "float64" in out:
+        out["float64"]["frac_of_fp64_probe"] = out["float64"]["gflops"] / peak64
+        full64_ms = out["float64"]["ms_per_step"] * n
+    solve = None
+    if args.dense_solve:
+        t0 = time.time()
+        (ym, yL), info = psolver.solve(f=pv.f, y0=pv.y0, ts=ts, order=q, init="constant", precision="mixed",
+                                       rtol_f32=1e-4, maxiters=100, maxiters_f32=100)
+        torch.cuda.synchronize()
+        solve = {"seconds": time.time() - t0, "iterations_float32": int(info["iterations_float32"]),
+                 "iterations_float64": int(info["iterations"]), "status": int(info["status"])}
+    if rank != 0:
+        return
+    jprint({
+        "metric": "dense filter + smoother pass (one IEKS iteration's work), ms per pass",
+        "value": next(iter(out.values()))["ms_per_pass"],
+        "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": next(iter(out.values()))["ms_per_pass"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (value), f64", "data": "synthetic",
+        "config": {"workload": workload, "cells": cells, "d": d, "D": D, "q": q, "N": N, "tmax": tmax,
+                   "chunks": chunks, "field_params": "a = b = 0.2, c = 3, kv = 0.5, kw = 0.05, "
+                                                     "v0 = -1 + 0.5 sin(2 pi k / 64), w0 = 1"},
+        "float32": out.get("float32"), "float64": out.get("float64"),
+        "float64_full_grid_ms_estimate": full64_ms,
+        "fp64_probe_gflops": peak64,
+        "mixed_solve": solve,
+    })
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1579,7 +1686,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(SERVE_WORKLOADS)
-                    + sorted(MIXED_WORKLOADS) + sorted(SWEEP_WORKLOADS))
+                    + sorted(MIXED_WORKLOADS) + sorted(SWEEP_WORKLOADS) + sorted(DENSE_WORKLOADS))
+    ap.add_argument("--dense-n", type=int, default=0, help="grid points of the dense workload (0: its own)")
+    ap.add_argument("--dense-f64-steps", type=int, default=256,
+                    help="steps of the float64 pass of the dense workload")
+    ap.add_argument("--dense-solve", action="store_true", help="also run the dense workload's mixed solve")
+    ap.add_argument("--dense-precisions", default="float32,float64", help="passes of the dense workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
@@ -1600,6 +1712,8 @@ def main():
         run_mixed(args, args.workload)
     elif args.workload in SWEEP_WORKLOADS:
         run_sweep(args, args.workload)
+    elif args.workload in DENSE_WORKLOADS:
+        run_dense(args, args.workload)
     else:
         run_gpu(args, args.workload)
 

@@ -224,3 +224,45 @@ def kernel_bytes(n, D, d, esz=8):
         # smoother elements, previous means in; chunk end states in; means, chols out
         "smo_l0_down": esz * (n * (selem + D + state) + n1 * state),
     }
+
+
+# ---------------------------------------------------------------------------
+# the dense path (csrc/pof_dense_sched.h): flops as its launches run them,
+# GEMM M N K -> 2 M N K, tria of an m x n block -> 2 m^2 n - 2/3 m^3 (the
+# Householder LQ's arithmetic, without the compact-WY overhead), triangular
+# solve M x K -> M^2 K.  Per step and filter + smoother pass; the top levels
+# (P - 1 sequential combines each way) are added per chunk.
+# ---------------------------------------------------------------------------
+
+
+def _tri(m, n):
+    return 2.0 * m * m * n - 2.0 * m ** 3 / 3.0
+
+
+def dense_step_flops(D, d):
+    """Flops per step of one dense filter + smoother pass (phases 1 and 3 of
+    the filter, the smoother's elements, chunk composites and backward
+    recursion)."""
+    g = lambda m, n, k: 2.0 * m * n * k  # noqa: E731
+    fold = (g(D, D, D) + _tri(D, 2 * D) + g(d, D, D) + _tri(d + D, D + d) + g(D, D + 1, D) + g(d, D + 1, D)
+            + d * d * (D + 1) + g(D, D + 1, d) + g(D, 1, d) + _tri(D, D + d))
+    kf = g(D, D, D) + _tri(D, 2 * D) + g(D, 1, D) + g(d, D, D) + _tri(d + D, D + d) + g(d, 1, D) + 2 * d * d + g(D, 1, d)
+    elem = g(D, D, D) + _tri(2 * D, 2 * D) + D ** 3 + g(D, 1, D) * 2
+    comp = 2 * g(D, D, D) + g(D, 1, D) + _tri(D, 2 * D)
+    back = g(D, 1, D) + g(D, D, D) + _tri(D, 2 * D)
+    objectives = 2 * (g(D, 1, D) + D * D)
+    return fold + kf + elem + comp + back + objectives
+
+
+def dense_top_flops(D, d):
+    """Flops of one chunk boundary of the top levels (a filter propagate and
+    a smoother application)."""
+    g = lambda m, n, k: 2.0 * m * n * k  # noqa: E731
+    prop = g(D, D, D) + _tri(2 * D, 2 * D) + D ** 3 + 6 * g(D, 1, D) + g(D, D, D) + _tri(D, 2 * D)
+    app = g(D, 1, D) + g(D, D, D) + _tri(D, 2 * D)
+    return prop + app
+
+
+def dense_pass_flops(n, D, d, chunks):
+    """Flops of one dense filter + smoother pass over n steps with `chunks` chunks."""
+    return n * dense_step_flops(D, d) + max(chunks - 1, 0) * dense_top_flops(D, d)
