@@ -70,11 +70,38 @@ struct Ctx {
       } else if (M <= 32) {
         k_gemm<T, 32, 128, 16, 2, 8><<<dim3(cdiv(N, 128), cdiv(M, 32), nb), 256, 0, st>>>(M, N, K, alpha, A, B,
                                                                                             beta, C, b0);
+      } else if (tensor_f32()) {
+        gemm_tensor(dim3(cdiv(N, 64), cdiv(M, 64), nb), M, N, K, alpha, A, B, beta, C, b0);
       } else {
         k_gemm<T, 64, 64, 16, 4, 4><<<dim3(cdiv(N, 64), cdiv(M, 64), nb), 256, 0, st>>>(M, N, K, alpha, A, B, beta,
                                                                                           C, b0);
       }
     }
+  }
+
+  // float32 GEMMs of at least 33 x 17 on the tensor cores (3xTF32) unless
+  // POF_DENSE_TF32=0 (read per pass); float64 always on the FP64 pipe.
+  bool tf32;
+  bool tensor_f32() const { return sizeof(T) == 4 && tf32; }
+  // D and, when the transition matrix is block-diagonal with blocks of Q1
+  // (checked once per pass), Q1; 0: products with F are GEMMs.
+  int D, fq1;
+
+  void fmul(int64_t batch, int K, MV<T> F, MV<T> X, T alpha, T beta, MV<T> Yv) {
+    if (batch <= 0 || K <= 0) return;
+    if (fq1 <= 0 || F.bs != 0) {
+      gemm(batch, D, K, D, alpha, F, X, beta, Yv);
+      return;
+    }
+    const int blocks = (int)std::min<int64_t>(cdiv((int64_t)D * K, 256), 1024);
+    for (int64_t b0 = 0; b0 < batch; b0 += kMaxGridYZ) {
+      const int nb = (int)std::min<int64_t>(kMaxGridYZ, batch - b0);
+      k_blockdiag_mm<T><<<dim3(blocks, nb), 256, 0, st>>>(D, fq1, K, F, X, alpha, beta, Yv, b0);
+    }
+  }
+  void gemm_tensor(dim3 grid, int M, int N, int K, T alpha, MV<T> A, MV<T> B, T beta, MV<T> C, int64_t b0) {
+    if constexpr (sizeof(T) == 4)
+      k_gemm_tf32x3<<<grid, 128, 0, st>>>(M, N, K, alpha, A, B, beta, C, b0);
   }
 
   void axpby(int64_t batch, int rows, int cols, T alpha, MV<T> X, T beta, MV<T> Yv) {
@@ -239,7 +266,20 @@ int run(int which, int64_t n, int D, int d, const void* x0m, const void* x0L, co
     if (e != cudaSuccess) return cuda_status(e);
     attr_set = true;
   }
-  Ctx<T> cx{st, L.V, L.TV, L.Y, L.vbs, L.ybs, L.maxbatch};
+  const char* e = getenv("POF_DENSE_TF32");
+  Ctx<T> cx{st, L.V, L.TV, L.Y, L.vbs, L.ybs, L.maxbatch, !(e && e[0] == '0'), D, 0};
+  // one transition matrix: is it block-diagonal (Q1 = D / d, the IWP prior)?
+  if (fts == 0 && d >= 1 && D % d == 0 && D / d < D) {
+    const int q1 = D / d;
+    cudaError_t ce = cudaMemsetAsync(L.flag, 0, sizeof(unsigned int), st);
+    if (ce != cudaSuccess) return cuda_status(ce);
+    k_offblock_count<T><<<64, 256, 0, st>>>(D, q1, static_cast<const T*>(F), L.flag);
+    unsigned int h = 1;
+    ce = cudaMemcpyAsync(&h, L.flag, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return cuda_status(ce);
+    if (h == 0) cx.fq1 = q1;
+  }
   run_schedule<T>(cx, L, which, static_cast<const T*>(x0m), static_cast<const T*>(x0L), static_cast<const T*>(F),
                   static_cast<const T*>(QL), fts, static_cast<const T*>(H), static_cast<const T*>(c),
                   static_cast<const T*>(R), rst, static_cast<T*>(om), static_cast<T*>(oL), osc);

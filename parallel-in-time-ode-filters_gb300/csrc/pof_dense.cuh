@@ -99,6 +99,128 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 }
 
 // ---------------------------------------------------------------------------
+// float32 GEMM on the tensor cores with 3xTF32 products: every operand is
+// split x = hi + lo with hi = tf32(x) and lo = tf32(x - hi), and
+// A B ~ lo_A hi_B + hi_A lo_B + hi_A hi_B accumulated in float32 -- the
+// error-compensated TF32 scheme of Ootomo & Yokota ("Recovering single
+// precision accuracy from Tensor Cores while surpassing the FP32 theoretical
+// peak performance", IJHPCA 2022), float32-level accuracy.  mma.sync
+// m16n8k8 TF32 (fragment layouts of the PTX ISA); 64 x 64 tiles, 4 warps
+// each owning a 32 x 32 quarter (2 x 4 tiles of 16 x 8), BK = 16 staged in
+// shared memory with rows padded to 72 floats so a fragment load touches 32
+// distinct banks.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_bits(x);
+  lo = tf32_bits(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(128)
+    k_gemm_tf32x3(int M, int N, int K, float alpha, MV<float> A, MV<float> B, float beta, MV<float> C, int64_t b0) {
+  constexpr int BM = 64, BN = 64, BK = 16, PAD = 8, NT = 128;
+  __shared__ float As[BK][BM + PAD];
+  __shared__ float Bs[BK][BN + PAD];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int g = lane >> 2, tq = lane & 3;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int64_t b = b0 + blockIdx.z;
+  const float* __restrict__ Ab = A.p + b * A.bs;
+  const float* __restrict__ Bb = B.p + b * B.bs;
+  float* Cb = C.p + b * C.bs;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+  const bool a_kc = A.cs == 1;
+  const bool b_nc = B.cs == 1;
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int l = t; l < BM * BK; l += NT) {
+      int mm, kk;
+      if (a_kc) {
+        kk = l % BK;
+        mm = l / BK;
+      } else {
+        mm = l % BM;
+        kk = l / BM;
+      }
+      const int gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < M && gk < K) ? Ab[gm * A.rs + gk * A.cs] : 0.f;
+    }
+    for (int l = t; l < BK * BN; l += NT) {
+      int nn, kk;
+      if (b_nc) {
+        nn = l % BN;
+        kk = l / BN;
+      } else {
+        kk = l % BK;
+        nn = l / BK;
+      }
+      const int gn = n0 + nn, gk = k0 + kk;
+      Bs[kk][nn] = (gn < N && gk < K) ? Bb[gk * B.rs + gn * B.cs] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 8) {
+      uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int mr = wm + i * 16 + g;
+        split_tf32(As[kk + tq][mr], ah[i][0], al[i][0]);
+        split_tf32(As[kk + tq][mr + 8], ah[i][1], al[i][1]);
+        split_tf32(As[kk + tq + 4][mr], ah[i][2], al[i][2]);
+        split_tf32(As[kk + tq + 4][mr + 8], ah[i][3], al[i][3]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int nc = wn + j * 8 + g;
+        split_tf32(Bs[kk + tq][nc], bh[j][0], bl[j][0]);
+        split_tf32(Bs[kk + tq + 4][nc], bh[j][1], bl[j][1]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          mma_tf32(acc[i][j], al[i], bh[j]);
+          mma_tf32(acc[i][j], ah[i], bl[j]);
+          mma_tf32(acc[i][j], ah[i], bh[j]);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int gm = m0 + wm + i * 16 + g + (r >= 2 ? 8 : 0);
+        const int gn = n0 + wn + j * 8 + 2 * tq + (r & 1);
+        if (gm < M && gn < N) {
+          float* c = Cb + gm * C.rs + gn * C.cs;
+          *c = beta == 0.f ? alpha * acc[i][j][r] : fmaf(alpha, acc[i][j][r], beta * *c);
+        }
+      }
+}
+
+// ---------------------------------------------------------------------------
 // Blocked Householder LQ (tria): W (m x n, n >= m) is overwritten so that its
 // first m columns hold L (lower triangular, zeros above the diagonal) with
 // L L^T = W W^T and columns m..n-1 are zero.  Row reflectors with LAPACK's
@@ -224,17 +346,10 @@ __global__ void __launch_bounds__(512)
   T* Vb = V + (int64_t)blockIdx.x * vbs;
   T* TVb = TV + (int64_t)blockIdx.x * vbs;
   for (int c = t; c < np; c += bd) {
-    T v[kMaxPanel];
-#pragma unroll
-    for (int k = 0; k < kMaxPanel; ++k) v[k] = k < nbb ? P[k * np + c] : T(0);
-#pragma unroll
-    for (int i = 0; i < kMaxPanel; ++i) {
-      if (i >= nbb) break;
+    for (int i = 0; i < nbb; ++i) {
       T acc = T(0);
-#pragma unroll
-      for (int k = 0; k < kMaxPanel; ++k)
-        if (k >= i && k < nbb) acc += Tm[i][k] * v[k];
-      Vb[i * np + c] = v[i];
+      for (int k = i; k < nbb; ++k) acc = fma(Tm[i][k], P[k * np + c], acc);
+      Vb[i * np + c] = P[i * np + c];
       TVb[i * np + c] = acc;
     }
   }
@@ -347,6 +462,40 @@ __global__ void k_fill2d(int rows, int cols, T v, T dv, MV<T> Y, int64_t b0) {
     const int i = (int)(l / cols), j = (int)(l - (int64_t)i * cols);
     Y.p[b * Y.bs + i * Y.rs + j * Y.cs] = i == j ? dv : v;
   }
+}
+
+// Y = alpha F X + beta Y for a block-diagonal F (D x D, diagonal blocks of
+// Q1 x Q1; the IWP transition I_d (x) A_1 in the state order of these
+// kernels): each output sums the Q1 terms of its block, in the order a GEMM
+// over the whole row would add them (the skipped products are exact zeros),
+// so the result equals the dense product bit for bit.
+template <typename T>
+__global__ void k_blockdiag_mm(int D, int Q1, int K, MV<T> F, MV<T> X, T alpha, T beta, MV<T> Y, int64_t b0) {
+  const int64_t b = b0 + blockIdx.y;
+  const int64_t total = (int64_t)D * K;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < total; l += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(l / K), c = (int)(l - (int64_t)i * K);
+    const int k0 = (i / Q1) * Q1;
+    const T* Fr = F.p + b * F.bs + i * F.rs;
+    const T* Xc = X.p + b * X.bs + c * X.cs;
+    T acc = T(0);
+    for (int k = k0; k < k0 + Q1; ++k) acc = fma(Fr[k * F.cs], Xc[k * X.rs], acc);
+    T* y = Y.p + b * Y.bs + i * Y.rs + c * Y.cs;
+    *y = beta == T(0) ? alpha * acc : fma(alpha, acc, beta * *y);
+  }
+}
+
+// out[0] = number of non-zero entries of F (D x D) outside its diagonal
+// Q1 x Q1 blocks (out[0] must be zero on entry).
+template <typename T>
+__global__ void k_offblock_count(int D, int Q1, const T* __restrict__ F, unsigned int* __restrict__ out) {
+  unsigned int cnt = 0;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < (int64_t)D * D;
+       l += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(l / D), j = (int)(l - (int64_t)i * D);
+    if (i / Q1 != j / Q1 && F[l] != T(0)) ++cnt;
+  }
+  if (cnt) atomicAdd(out, cnt);
 }
 
 // Per-step filter terms from P11 (d x d lower), w = P11^{-1}(-r) and

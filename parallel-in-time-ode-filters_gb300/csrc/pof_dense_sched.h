@@ -1,6 +1,10 @@
 // The dense filter/smoother schedule (host code), written against a launch
 // context X that provides the batched primitives on strided views:
 //   gemm(batch, M, N, K, alpha, A, B, beta, C)     C = alpha A B + beta C
+//   fmul(batch, K, F, X, alpha, beta, Y)           Y = alpha F X + beta Y with a
+//                                                  transition matrix F (D x D): a
+//                                                  GEMM, or the block-diagonal
+//                                                  product when F has that form
 //   axpby(batch, rows, cols, alpha, X, beta, Y)    Y = alpha X + beta Y
 //   copy(batch, rows, cols, X, Y), fill(batch, rows, cols, v, diag_v, Y)
 //   tria(batch, m, n, W)                           W (m x n, n >= m) -> L in
@@ -59,6 +63,7 @@ struct Layout {
   // tria scratch
   T *V, *TV, *Y;
   int64_t vbs, ybs;
+  unsigned int* flag;  // the block-structure check (zeroed by the caller)
   size_t total;
 
   // active chunks at step offset s of a chunk (only the last can be short)
@@ -150,6 +155,7 @@ Layout<T> layout(char* base, int which, int64_t n, int D, int d, int chunks) {
   L.V = a.take<T>(L.maxbatch * L.vbs);
   L.TV = a.take<T>(L.maxbatch * L.vbs);
   L.Y = a.take<T>(L.maxbatch * L.ybs);
+  L.flag = reinterpret_cast<unsigned int*>(a.take<double>(1));
   L.total = a.off + 256;  // alignment slack of aligned_ws
   return L;
 }
@@ -175,11 +181,11 @@ void objective(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t fts, 
   MV<T> Rv = rowmajor(L.R, D, 0);
   cx.copy(1, (int)n, D, cv(M, D, 1, 0), Rv);
   if (fts == 0) {
-    cx.gemm(1, (int)n, D, D, T(-1), cv(M + D, D, 1, 0), tr(cv(F, D, 1, 0)), T(1), Rv);
+    cx.fmul(1, (int)n, cv(F, D, 1, 0), tr(cv(M + D, D, 1, 0)), T(-1), T(1), tr(Rv));
     cx.trsm(1, D, (int)n, cv(QL, D, 1, 0), false, tr(Rv));
   } else {
     MV<T> rv{L.R, 1, 1, D};
-    cx.gemm(n, D, 1, D, T(-1), cv(F, D, 1, fts), cv(M + D, 1, 1, D), T(1), rv);
+    cx.fmul(n, 1, cv(F, D, 1, fts), cv(M + D, 1, 1, D), T(-1), T(1), rv);
     cx.trsm(n, D, 1, cv(QL, D, 1, fts), false, rv);
   }
   cx.sqnorm(n, D, MV<T>{L.R, 1, 1, D}, obj);
@@ -216,7 +222,7 @@ void run_filter(X& cx, const Layout<T>& L, const Model<T>& md, const T* x0m, con
     cx.tria(Pa, d + D, D + d, X2v);
   };
   auto predict = [&](int Pa, int s, MV<T> Lprev) {
-    cx.gemm(Pa, D, D, D, one, Fv(s), Lprev, zero, X1v);
+    cx.fmul(Pa, D, Fv(s), Lprev, one, zero, X1v);
     cx.copy(Pa, D, D, QLv(s), sub(X1v, 0, D));
     cx.tria(Pa, D, 2 * D, X1v);
   };
@@ -232,7 +238,7 @@ void run_filter(X& cx, const Layout<T>& L, const Model<T>& md, const T* x0m, con
     predict(Pa, s, Lcv);
     observe(Pa, s);
     MV<T> FAb = Abv[1 - cur];
-    cx.gemm(Pa, D, D + 1, D, one, Fv(s), Abv[cur], zero, FAb);
+    cx.fmul(Pa, D + 1, Fv(s), Abv[cur], one, zero, FAb);
     cx.gemm(Pa, d, D + 1, D, one, Hv(s), FAb, zero, Grv);
     cx.axpby(Pa, d, 1, one, cvec(s), one, sub(Grv, 0, D));
     cx.trsm(Pa, d, D + 1, P11, false, Grv);
@@ -295,7 +301,7 @@ void run_filter(X& cx, const Layout<T>& L, const Model<T>& md, const T* x0m, con
     const int Pa = L.active(s);
     predict(Pa, s, Lkv);
     MV<T> mp = mkv[1 - cur];
-    cx.gemm(Pa, D, 1, D, one, Fv(s), mkv[cur], zero, mp);
+    cx.fmul(Pa, 1, Fv(s), mkv[cur], one, zero, mp);
     observe(Pa, s);
     cx.copy(Pa, d, 1, cvec(s), rbv);
     cx.gemm(Pa, d, 1, D, one, Hv(s), mp, one, rbv);
@@ -327,7 +333,7 @@ void run_smoother(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t ft
     const MV<T> mk{om + k0 * D, 1, 1, D};
     const MV<T> Ek = rowmajor(L.E + k0 * DD, D, DD), Dk = rowmajor(L.Dm + k0 * DD, D, DD);
     const MV<T> gk{L.g + k0 * D, 1, 1, D}, ft{L.ftmp, 1, 1, D};
-    cx.gemm(Sb, D, D, D, one, Fk, Lk, zero, Phiv);
+    cx.fmul(Sb, D, Fk, Lk, one, zero, Phiv);
     cx.copy(Sb, D, D, QLk, sub(Phiv, 0, D));
     cx.copy(Sb, D, D, Lk, sub(Phiv, D, 0));
     cx.fill(Sb, D, D, zero, zero, sub(Phiv, D, D));
@@ -335,7 +341,7 @@ void run_smoother(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t ft
     cx.trsm(Sb, D, D, tr(Phiv), true, tr(sub(Phiv, D, 0)));  // P21 block := E = P21 P11^{-1}
     cx.copy(Sb, D, D, sub(Phiv, D, 0), Ek);
     cx.copy(Sb, D, D, sub(Phiv, D, D), Dk);
-    cx.gemm(Sb, D, 1, D, one, Fk, mk, zero, ft);
+    cx.fmul(Sb, 1, Fk, mk, one, zero, ft);
     cx.copy(Sb, D, 1, mk, gk);
     cx.gemm(Sb, D, 1, D, T(-1), Ek, ft, one, gk);
   }

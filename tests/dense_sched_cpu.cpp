@@ -78,6 +78,10 @@ struct CpuCtx {
         }
     }
   }
+  int D = 0;
+  void fmul(int64_t batch, int K, MV<double> F, MV<double> X, double alpha, double beta, MV<double> Y) {
+    gemm(batch, D, K, D, alpha, F, X, beta, Y);
+  }
   void axpby(int64_t batch, int rows, int cols, double alpha, MV<double> X, double beta, MV<double> Y) {
     op = "axpby";
     for (int64_t b = 0; b < batch; ++b)
@@ -222,6 +226,7 @@ extern "C" int dense_cpu_filtsmooth(int which, int64_t n, int D, int d, const do
   char* al = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 255) & ~uintptr_t(255));
   Layout<double> L = layout<double>(al, which, n, D, d, chunks);
   CpuCtx cx;
+  cx.D = D;
   const int64_t DD = (int64_t)D * D;
   const int64_t ft_count = fts ? n * DD : DD;
   cx.ranges.push_back({"workspace", reinterpret_cast<const double*>(al),

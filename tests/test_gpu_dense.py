@@ -188,14 +188,19 @@ def test_dense_path_at_d640():
     assert abs(sc[0] - nll) <= TOL * abs(nll)
 
 
-def test_dense_float32_against_float64():
-    """The float32 dense pass against the float64 one on the same model."""
-    n, D, d = 48, 64, 8
-    x0, dtm, dom = _random_problem(32, n, D, d, False)
+@pytest.mark.parametrize("tf32", ["1", "0"])
+@pytest.mark.parametrize("n,D,d", [(48, 64, 8), (12, 640, 128)])
+def test_dense_float32_against_float64(monkeypatch, tf32, n, D, d):
+    """The float32 dense pass (GEMMs on the tensor cores with 3xTF32
+    products, or with POF_DENSE_TF32=0 on the FP32 pipe) against the float64
+    one on the same model."""
+    monkeypatch.setenv("POF_DENSE_TF32", tf32)
+    x0, dtm, dom = _random_problem(32 + D, n, D, d, False)
     m64, L64, _ = _gpu("filtsmooth", x0, dtm, dom, 6)
     m32, L32, _ = _gpu("filtsmooth", x0, dtm, dom, 6, dtype=torch.float32)
     tol = 1e-4
-    print("float32 dense vs float64: means %.2e, LL^T %.2e (tolerance %.0e)" % (rel(m32, m64), covrel(L32, L64), tol))
+    print("float32 dense (3xTF32 %s) vs float64, D=%d: means %.2e, LL^T %.2e (tolerance %.0e)"
+          % (tf32, D, rel(m32, m64), covrel(L32, L64), tol))
     assert rel(m32, m64) <= tol and covrel(L32, L64) <= tol
 
 
@@ -263,11 +268,15 @@ def test_rd_solve_matches_oracle():
     (gm, gL), ginfo = psolver.solve(f=pv.f, y0=pv.y0, ts=torch.as_tensor(ts), order=3, init="constant", maxiters=200,
                                     calibrate=False)
     gm, gL = N_(gm), N_(gL)
-    print("RD (32, 8): iterations %d (oracle %d), means %.2e, LL^T %.2e"
-          % (int(ginfo["iterations"]), oinfo["iterations"], rel(gm, om), covrel(gL, oL)))
+    # every ieks_step scales the factors by that iteration's sigma^2
+    # (pof/step.py:33-45); compare L L^T / sigma^2
+    gs, osq = float(ginfo["sigma_squared"]), float(oinfo["sigma_squared"])
+    print("RD (32, 8): iterations %d (oracle %d), means %.2e, LL^T/sigma^2 %.2e, sigma^2 %.2e apart"
+          % (int(ginfo["iterations"]), oinfo["iterations"], rel(gm, om), covrel(gL / gs ** 0.5, oL / osq ** 0.5),
+             abs(gs - osq) / osq))
     assert int(ginfo["iterations"]) == oinfo["iterations"]
     assert int(ginfo["status"]) == 0
-    assert rel(gm, om) <= TOL and covrel(gL, oL) <= TOL
+    assert rel(gm, om) <= TOL and covrel(gL / gs ** 0.5, oL / osq ** 0.5) <= TOL
 
 
 def test_rd_mixed_precision_solve():
