@@ -21,6 +21,8 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <utility>
+#include <vector>
 
 #include "pof_dense_views.h"
 
@@ -34,10 +36,12 @@ constexpr size_t kSlabBytes = size_t(1) << 30;
 struct Arena {
   char* base;
   size_t off = 0;
+  std::vector<std::pair<size_t, size_t>>* regions = nullptr;  // (offset, bytes) of every take, if wanted
   template <typename T>
   T* take(int64_t count) {
     off = (off + 255) & ~size_t(255);
     T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    if (regions) regions->emplace_back(off, size_t(count) * sizeof(T));
     off += size_t(count) * sizeof(T);
     return p;
   }
@@ -53,8 +57,14 @@ struct Layout {
   int64_t maxbatch;
   // filter
   T *Ab[2], *Lc, *eta, *Z, *X1, *X2, *X3, *Gr;
-  T *X4, *Mm, *X5, *v1, *v2, *v3, *v4;
   T *Sm, *SL, *Lk, *mk[2], *rb, *wb, *wq;
+  // top levels (binary tree over the chunks): element and state slots of the
+  // levels above the chunks (sum of the level sizes), and the scratch of one
+  // batched operator application over at most G = ceil(P / 2) pairs
+  T *TAb, *TU, *Teta, *TZ, *Sb, *SU;
+  T *TgS, *TES, *TDS, *Em, *EL;
+  T *OXi, *OM, *OT, *Om, *Oe, *OX5, *OX6, *Ov;
+  int G;
   double *nll, *ssq, *fobj, *sobj;
   // smoother
   T *E, *Dm, *g, *Phi, *tE[2], *tD, *tg, *Xs, *em, *eL, *tm, *ftmp;
@@ -83,7 +93,8 @@ inline void plan_chunks(int64_t n, int chunks, int* P, int* C0, int* last) {
 }
 
 template <typename T>
-Layout<T> layout(char* base, int which, int64_t n, int D, int d, int chunks) {
+Layout<T> layout(char* base, int which, int64_t n, int D, int d, int chunks,
+                 std::vector<std::pair<size_t, size_t>>* regions = nullptr) {
   Layout<T> L{};
   L.n = n;
   L.D = D;
@@ -95,7 +106,12 @@ Layout<T> layout(char* base, int which, int64_t n, int D, int d, int chunks) {
   S = std::min<int64_t>(std::min<int64_t>(S, n), 4096);
   L.S = (int)S;
   Arena a{base};
+  a.regions = regions;
   const bool filt = which != 2, smo = which != 0;
+  // slots of the tree levels above the chunks: sum of n_{l+1} = ceil(n_l / 2)
+  int64_t Tn = 0;
+  for (int64_t m = P; m > 1; m = (m + 1) / 2) Tn += (m + 1) / 2;
+  Tn = std::max<int64_t>(Tn, 1);
   if (filt) {
     L.Ab[0] = a.take<T>(P * D * (D + 1));
     L.Ab[1] = a.take<T>(P * D * (D + 1));
@@ -106,13 +122,12 @@ Layout<T> layout(char* base, int which, int64_t n, int D, int d, int chunks) {
     L.X2 = a.take<T>(P * (int64_t)(D + d) * (D + d));
     L.X3 = a.take<T>(P * D * (int64_t)(D + d));
     L.Gr = a.take<T>(P * d * (int64_t)(D + 1));
-    L.X4 = a.take<T>(4 * DD);
-    L.Mm = a.take<T>(DD);
-    L.X5 = a.take<T>(2 * DD);
-    L.v1 = a.take<T>(D);
-    L.v2 = a.take<T>(D);
-    L.v3 = a.take<T>(D);
-    L.v4 = a.take<T>(D);
+    L.TAb = a.take<T>(Tn * D * (D + 1));
+    L.TU = a.take<T>(Tn * DD);
+    L.Teta = a.take<T>(Tn * D);
+    L.TZ = a.take<T>(Tn * DD);
+    L.Sb = a.take<T>(Tn * D);
+    L.SU = a.take<T>(Tn * DD);
     L.Sm = a.take<T>(P * D);
     L.SL = a.take<T>(P * DD);
     L.Lk = a.take<T>(P * DD);
@@ -140,13 +155,22 @@ Layout<T> layout(char* base, int which, int64_t n, int D, int d, int chunks) {
     L.tm = a.take<T>(P * D);
     L.ftmp = a.take<T>(std::max<int64_t>(S, P) * D);
     L.sobj = a.take<double>(n);
-    if (!filt) {
-      L.X5 = a.take<T>(2 * DD);
-      L.Mm = a.take<T>(DD);
-      L.v1 = a.take<T>(D);
-      L.v2 = a.take<T>(D);
-    }
+    L.TgS = a.take<T>(Tn * D);
+    L.TES = a.take<T>(Tn * DD);
+    L.TDS = a.take<T>(Tn * DD);
+    L.Em = a.take<T>(Tn * D);
+    L.EL = a.take<T>(Tn * DD);
   }
+  const int64_t G = std::max<int64_t>(1, (P + 1) / 2);
+  L.G = (int)G;
+  L.OXi = a.take<T>(G * 4 * DD);
+  L.OM = a.take<T>(G * DD);
+  L.OT = a.take<T>(G * DD);
+  L.Om = a.take<T>(G * DD);
+  L.Oe = a.take<T>(G * DD);
+  L.OX5 = a.take<T>(G * 2 * DD);
+  L.OX6 = a.take<T>(G * 2 * DD);
+  L.Ov = a.take<T>(G * 8 * D);
   L.R = a.take<T>(n * D);
   const int nmax = std::max(2 * D, D + d), mmax = std::max(2 * D, D + d);
   L.maxbatch = std::max<int64_t>(P, S);
@@ -189,6 +213,261 @@ void objective(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t fts, 
     cx.trsm(n, D, 1, cv(QL, D, 1, fts), false, rv);
   }
   cx.sqnorm(n, D, MV<T>{L.R, 1, 1, D}, obj);
+}
+
+// ---------------------------------------------------------------------------
+// the top levels: a binary tree over the P chunk totals, the batched solve's
+// segmented schedule with groups of two (restated by the oracle as
+// blocked._filter_states_segmented / _smoother_states_segmented with Cg = 2).
+// Level l has n_l elements (n_0 = P, n_{l+1} = ceil(n_l / 2)); the up-sweep
+// combines the pairs (2g, 2g+1) of every level into the next, the down-sweep
+// gives member 2g its parent's state and member 2g+1 that state carried
+// through member 2g.  Every level is one batched application over its pairs.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct FElem {  // filter elements (A | b, U, eta, Z), one slot per element
+  MV<T> Ab, U, eta, Z;
+  FElem at(int64_t i) const {
+    return FElem{MV<T>{Ab.p + i * Ab.bs, Ab.rs, Ab.cs, Ab.bs}, MV<T>{U.p + i * U.bs, U.rs, U.cs, U.bs},
+                 MV<T>{eta.p + i * eta.bs, eta.rs, eta.cs, eta.bs}, MV<T>{Z.p + i * Z.bs, Z.rs, Z.cs, Z.bs}};
+  }
+  FElem pairs(int k) const {  // member k of every pair
+    FElem e = at(k);
+    e.Ab.bs *= 2, e.U.bs *= 2, e.eta.bs *= 2, e.Z.bs *= 2;
+    return e;
+  }
+};
+
+template <typename T>
+struct State {  // (mean, chol) slots
+  MV<T> m, L;
+  State at(int64_t i) const {
+    return State{MV<T>{m.p + i * m.bs, m.rs, m.cs, m.bs}, MV<T>{L.p + i * L.bs, L.rs, L.cs, L.bs}};
+  }
+  State pairs(int k) const {
+    State s = at(k);
+    s.m.bs *= 2, s.L.bs *= 2;
+    return s;
+  }
+};
+
+template <typename T>
+struct SElem {  // smoother elements (g, E, D)
+  MV<T> g, E, Dm;
+  SElem at(int64_t i) const {
+    return SElem{MV<T>{g.p + i * g.bs, g.rs, g.cs, g.bs}, MV<T>{E.p + i * E.bs, E.rs, E.cs, E.bs},
+                 MV<T>{Dm.p + i * Dm.bs, Dm.rs, Dm.cs, Dm.bs}};
+  }
+  SElem pairs(int k) const {
+    SElem e = at(k);
+    e.g.bs *= 2, e.E.bs *= 2, e.Dm.bs *= 2;
+    return e;
+  }
+};
+
+template <typename T>
+struct OpScratch {
+  MV<T> Xi, M, Tm, m, e, X5, X6;
+  MV<T> v[8];
+  explicit OpScratch(const Layout<T>& L) {
+    const int D = L.D;
+    const int64_t DD = (int64_t)D * D;
+    Xi = rowmajor(L.OXi, 2 * D, 4 * DD);
+    M = rowmajor(L.OM, D, DD);
+    Tm = rowmajor(L.OT, D, DD);
+    m = rowmajor(L.Om, D, DD);
+    e = rowmajor(L.Oe, D, DD);
+    X5 = rowmajor(L.OX5, 2 * D, 2 * DD);
+    X6 = rowmajor(L.OX6, 2 * D, 2 * DD);
+    for (int i = 0; i < 8; ++i) v[i] = MV<T>{L.Ov + (int64_t)i * L.G * D, 1, 1, D};
+  }
+};
+
+// Xi = tria([[U1^T Z2, I], [Z2, 0]]) and m = Xi11^{-1} U1^T (filter.py:117-142)
+template <typename T, typename X>
+void op_xi(X& cx, int D, int64_t G, MV<T> U1, MV<T> Z2, const OpScratch<T>& o) {
+  const T one(1), zero(0);
+  cx.gemm(G, D, D, D, one, tr(U1), Z2, zero, o.Xi);
+  cx.fill(G, D, D, zero, one, sub(o.Xi, 0, D));
+  cx.copy(G, D, D, Z2, sub(o.Xi, D, 0));
+  cx.fill(G, D, D, zero, zero, sub(o.Xi, D, D));
+  cx.tria(G, 2 * D, 2 * D, o.Xi);
+  cx.copy(G, D, D, tr(U1), o.m);
+  cx.trsm(G, D, D, o.Xi, false, o.m);
+}
+
+// b = A2 (I - m^T Xi21^T)(b1 + U1 U1^T eta2) + b2, written to out
+template <typename T, typename X>
+void op_b(X& cx, int D, int64_t G, MV<T> b1, MV<T> U1, MV<T> A2, MV<T> b2, MV<T> eta2, MV<T> out,
+          const OpScratch<T>& o) {
+  const T one(1), zero(0);
+  const MV<T> Xi21 = sub(o.Xi, D, 0);
+  cx.gemm(G, D, 1, D, one, tr(U1), eta2, zero, o.v[0]);
+  cx.copy(G, D, 1, b1, o.v[1]);
+  cx.gemm(G, D, 1, D, one, U1, o.v[0], one, o.v[1]);
+  cx.gemm(G, D, 1, D, one, tr(Xi21), o.v[1], zero, o.v[2]);
+  cx.copy(G, D, 1, o.v[1], o.v[3]);
+  cx.gemm(G, D, 1, D, T(-1), tr(o.m), o.v[2], one, o.v[3]);
+  cx.copy(G, D, 1, b2, out);
+  cx.gemm(G, D, 1, D, one, A2, o.v[3], one, out);
+}
+
+// out = sqrt_filtering_operator(e1, e2) (filter.py:117-142), G pairs at once
+template <typename T, typename X>
+void op_filter(X& cx, int D, int64_t G, const FElem<T>& e1, const FElem<T>& e2, const FElem<T>& out,
+               const OpScratch<T>& o) {
+  const T one(1), zero(0);
+  const MV<T> A1 = e1.Ab, b1 = sub(e1.Ab, 0, D), A2 = e2.Ab, b2 = sub(e2.Ab, 0, D);
+  op_xi(cx, D, G, e1.U, e2.Z, o);
+  const MV<T> Xi11 = o.Xi, Xi21 = sub(o.Xi, D, 0), Xi22 = sub(o.Xi, D, D);
+  // M = Xi11^{-1} U1^T A2^T;  A = A2 A1 - M^T Xi21^T A1
+  cx.gemm(G, D, D, D, one, tr(e1.U), tr(A2), zero, o.M);
+  cx.trsm(G, D, D, Xi11, false, o.M);
+  cx.gemm(G, D, D, D, one, tr(Xi21), A1, zero, o.Tm);
+  cx.gemm(G, D, D, D, one, A2, A1, zero, out.Ab);
+  cx.gemm(G, D, D, D, T(-1), tr(o.M), o.Tm, one, out.Ab);
+  op_b(cx, D, G, b1, e1.U, A2, b2, e2.eta, sub(out.Ab, 0, D), o);
+  // U = tria([M^T | U2])
+  cx.copy(G, D, D, tr(o.M), o.X5);
+  cx.copy(G, D, D, e2.U, sub(o.X5, 0, D));
+  cx.tria(G, D, 2 * D, o.X5);
+  cx.copy(G, D, D, o.X5, out.U);
+  // eta = A1^T (I - e^T U1^T)(eta2 - Z2 Z2^T b1) + eta1,  e = Xi11^{-T} Xi21^T
+  cx.copy(G, D, D, tr(Xi21), o.e);
+  cx.trsm(G, D, D, tr(Xi11), true, o.e);
+  cx.gemm(G, D, 1, D, one, tr(e2.Z), b1, zero, o.v[4]);
+  cx.copy(G, D, 1, e2.eta, o.v[5]);
+  cx.gemm(G, D, 1, D, T(-1), e2.Z, o.v[4], one, o.v[5]);
+  cx.gemm(G, D, 1, D, one, tr(e1.U), o.v[5], zero, o.v[6]);
+  cx.copy(G, D, 1, o.v[5], o.v[7]);
+  cx.gemm(G, D, 1, D, T(-1), tr(o.e), o.v[6], one, o.v[7]);
+  cx.copy(G, D, 1, e1.eta, out.eta);
+  cx.gemm(G, D, 1, D, one, tr(A1), o.v[7], one, out.eta);
+  // Z = tria([A1^T Xi22 | Z1])
+  cx.gemm(G, D, D, D, one, tr(A1), Xi22, zero, o.X6);
+  cx.copy(G, D, D, e1.Z, sub(o.X6, 0, D));
+  cx.tria(G, D, 2 * D, o.X6);
+  cx.copy(G, D, D, o.X6, out.Z);
+}
+
+// out = the (b, U) part of sqrt_filtering_operator((., b1, U1, ., .), e2):
+// the filtering state after element e2 from the state (b1, U1) before it
+template <typename T, typename X>
+void op_propagate(X& cx, int D, int64_t G, const State<T>& s, const FElem<T>& e2, const State<T>& out,
+                  const OpScratch<T>& o) {
+  const T one(1), zero(0);
+  const MV<T> A2 = e2.Ab, b2 = sub(e2.Ab, 0, D);
+  op_xi(cx, D, G, s.L, e2.Z, o);
+  op_b(cx, D, G, s.m, s.L, A2, b2, e2.eta, out.m, o);
+  cx.gemm(G, D, D, D, one, A2, tr(o.m), zero, o.X5);
+  cx.copy(G, D, D, e2.U, sub(o.X5, 0, D));
+  cx.tria(G, D, 2 * D, o.X5);
+  cx.copy(G, D, D, o.X5, out.L);
+}
+
+// state before every element of a level of n elements, the state before the
+// first being given in st[top]; lev[l] / st[l] the levels' slots
+template <typename T, typename X>
+void filter_tree(X& cx, const Layout<T>& L, const FElem<T>& lev0, const State<T>& st0, const T* x0m, const T* x0L) {
+  const int D = L.D;
+  const int64_t DD = (int64_t)D * D;
+  const OpScratch<T> o(L);
+  std::vector<int64_t> n{L.P};
+  while (n.back() > 1) n.push_back((n.back() + 1) / 2);
+  const int top = (int)n.size() - 1;
+  std::vector<FElem<T>> lev{lev0};
+  std::vector<State<T>> st{st0};
+  int64_t off = 0;
+  for (int l = 1; l <= top; ++l) {
+    lev.push_back(FElem<T>{rowmajor(L.TAb + off * D * (D + 1), D + 1, (int64_t)D * (D + 1)),
+                           rowmajor(L.TU + off * DD, D, DD), MV<T>{L.Teta + off * D, 1, 1, D},
+                           rowmajor(L.TZ + off * DD, D, DD)});
+    st.push_back(State<T>{MV<T>{L.Sb + off * D, 1, 1, D}, rowmajor(L.SU + off * DD, D, DD)});
+    off += n[l];
+  }
+  // up-sweep (the single top element is never needed)
+  for (int l = 0; l + 1 < top; ++l) {
+    const int64_t G2 = n[l] / 2;
+    op_filter(cx, D, G2, lev[l].pairs(0), lev[l].pairs(1), lev[l + 1], o);
+    if (n[l] % 2) {
+      const FElem<T> a = lev[l].at(n[l] - 1), b = lev[l + 1].at(G2);
+      cx.copy(1, D, D + 1, a.Ab, b.Ab);
+      cx.copy(1, D, D, a.U, b.U);
+      cx.copy(1, D, 1, a.eta, b.eta);
+      cx.copy(1, D, D, a.Z, b.Z);
+    }
+  }
+  cx.copy(1, D, 1, cv(x0m, 1, 1, 0), st[top].m);
+  cx.copy(1, D, D, cv(x0L, D, 1, 0), st[top].L);
+  // down-sweep
+  for (int l = top - 1; l >= 0; --l) {
+    const State<T> even = st[l].pairs(0);
+    cx.copy(n[l + 1], D, 1, st[l + 1].m, even.m);
+    cx.copy(n[l + 1], D, D, st[l + 1].L, even.L);
+    op_propagate(cx, D, n[l] / 2, st[l + 1], lev[l].pairs(0), st[l].pairs(1), o);
+  }
+}
+
+// smoothed state right after every chunk (the terminal state after the last)
+template <typename T, typename X>
+void smoother_tree(X& cx, const Layout<T>& L, const SElem<T>& lev0, const State<T>& ends0, const T* mT,
+                   const T* LT) {
+  const int D = L.D;
+  const int64_t DD = (int64_t)D * D;
+  const T one(1), zero(0);
+  const OpScratch<T> o(L);
+  std::vector<int64_t> n{L.P};
+  while (n.back() > 1) n.push_back((n.back() + 1) / 2);
+  const int top = (int)n.size() - 1;
+  std::vector<SElem<T>> lev{lev0};
+  std::vector<State<T>> en{ends0};
+  int64_t off = 0;
+  for (int l = 1; l <= top; ++l) {
+    lev.push_back(SElem<T>{MV<T>{L.TgS + off * D, 1, 1, D}, rowmajor(L.TES + off * DD, D, DD),
+                           rowmajor(L.TDS + off * DD, D, DD)});
+    en.push_back(State<T>{MV<T>{L.Em + off * D, 1, 1, D}, rowmajor(L.EL + off * DD, D, DD)});
+    off += n[l];
+  }
+  // up-sweep: the composite of every pair, sqrt_smoothing_operator(later, earlier)
+  for (int l = 0; l + 1 < top; ++l) {
+    const int64_t G2 = n[l] / 2;
+    const SElem<T> early = lev[l].pairs(0), late = lev[l].pairs(1), out = lev[l + 1];
+    cx.copy(G2, D, 1, early.g, out.g);
+    cx.gemm(G2, D, 1, D, one, early.E, late.g, one, out.g);
+    cx.gemm(G2, D, D, D, one, early.E, late.E, zero, out.E);
+    cx.gemm(G2, D, D, D, one, early.E, late.Dm, zero, o.X5);
+    cx.copy(G2, D, D, early.Dm, sub(o.X5, 0, D));
+    cx.tria(G2, D, 2 * D, o.X5);
+    cx.copy(G2, D, D, o.X5, out.Dm);
+    if (n[l] % 2) {
+      const SElem<T> a = lev[l].at(n[l] - 1), b = lev[l + 1].at(G2);
+      cx.copy(1, D, 1, a.g, b.g);
+      cx.copy(1, D, D, a.E, b.E);
+      cx.copy(1, D, D, a.Dm, b.Dm);
+    }
+  }
+  cx.copy(1, D, 1, cv(mT, 1, 1, 0), en[top].m);
+  cx.copy(1, D, D, cv(LT, D, 1, 0), en[top].L);
+  // down-sweep: member 2g+1 ends where its parent ends, member 2g where
+  // member 2g+1 starts (the parent's end state carried through 2g+1)
+  for (int l = top - 1; l >= 0; --l) {
+    const int64_t G2 = n[l] / 2;
+    const State<T> odd = en[l].pairs(1), even = en[l].pairs(0);
+    const SElem<T> late = lev[l].pairs(1);
+    cx.copy(G2, D, 1, en[l + 1].m, odd.m);
+    cx.copy(G2, D, D, en[l + 1].L, odd.L);
+    cx.copy(G2, D, 1, late.g, even.m);
+    cx.gemm(G2, D, 1, D, one, late.E, en[l + 1].m, one, even.m);
+    cx.gemm(G2, D, D, D, one, late.E, en[l + 1].L, zero, o.X5);
+    cx.copy(G2, D, D, late.Dm, sub(o.X5, 0, D));
+    cx.tria(G2, D, 2 * D, o.X5);
+    cx.copy(G2, D, D, o.X5, even.L);
+    if (n[l] % 2) {  // a last element alone in its pair ends where its parent ends
+      const State<T> a = en[l + 1].at(G2), b = en[l].at(n[l] - 1);
+      cx.copy(1, D, 1, a.m, b.m);
+      cx.copy(1, D, D, a.L, b.L);
+    }
+  }
 }
 
 template <typename T, typename X>
@@ -254,39 +533,9 @@ void run_filter(X& cx, const Layout<T>& L, const Model<T>& md, const T* x0m, con
     cx.copy(Pa, D, D, U, Lcv);
   }
 
-  // phase 2: the state at every chunk start
+  // phase 2: the state at every chunk start (the tree over the chunk totals)
   const MV<T> Smv{L.Sm, 1, 1, D}, SLv = rowmajor(L.SL, D, DD);
-  cx.copy(1, D, 1, cv(x0m, 1, 1, 0), Smv);
-  cx.copy(1, D, D, cv(x0L, D, 1, 0), SLv);
-  const MV<T> X4v = rowmajor(L.X4, 2 * D, 0), Mmv = rowmajor(L.Mm, D, 0), X5v = rowmajor(L.X5, 2 * D, 0);
-  const MV<T> v1{L.v1, 1, 1, 0}, v2{L.v2, 1, 1, 0}, v3{L.v3, 1, 1, 0}, v4{L.v4, 1, 1, 0};
-  for (int j = 0; j + 1 < P; ++j) {
-    const MV<T> b1{L.Sm + (int64_t)j * D, 1, 1, 0}, U1 = rowmajor(L.SL + j * DD, D, 0);
-    const MV<T> A2 = rowmajor(L.Ab[cur] + (int64_t)j * D * (D + 1), D + 1, 0), b2 = sub(A2, 0, D);
-    const MV<T> U2 = rowmajor(L.Lc + j * DD, D, 0), Z2 = rowmajor(L.Z + j * DD, D, 0);
-    const MV<T> eta2{L.eta + (int64_t)j * D, 1, 1, 0};
-    cx.gemm(1, D, D, D, one, tr(U1), Z2, zero, X4v);
-    cx.fill(1, D, D, zero, one, sub(X4v, 0, D));
-    cx.copy(1, D, D, Z2, sub(X4v, D, 0));
-    cx.fill(1, D, D, zero, zero, sub(X4v, D, D));
-    cx.tria(1, 2 * D, 2 * D, X4v);
-    const MV<T> Xi11 = X4v, Xi21 = sub(X4v, D, 0);
-    cx.copy(1, D, D, tr(U1), Mmv);
-    cx.trsm(1, D, D, Xi11, false, Mmv);
-    cx.gemm(1, D, 1, D, one, tr(U1), eta2, zero, v1);
-    cx.copy(1, D, 1, b1, v2);
-    cx.gemm(1, D, 1, D, one, U1, v1, one, v2);
-    cx.gemm(1, D, 1, D, one, tr(Xi21), v2, zero, v3);
-    cx.copy(1, D, 1, v2, v4);
-    cx.gemm(1, D, 1, D, T(-1), tr(Mmv), v3, one, v4);
-    const MV<T> bn{L.Sm + (int64_t)(j + 1) * D, 1, 1, 0};
-    cx.copy(1, D, 1, b2, bn);
-    cx.gemm(1, D, 1, D, one, A2, v4, one, bn);
-    cx.gemm(1, D, D, D, one, A2, tr(Mmv), zero, X5v);
-    cx.copy(1, D, D, U2, sub(X5v, 0, D));
-    cx.tria(1, D, 2 * D, X5v);
-    cx.copy(1, D, D, X5v, rowmajor(L.SL + (j + 1) * DD, D, 0));
-  }
+  filter_tree(cx, L, FElem<T>{Abv[cur], Lcv, etav, Zv}, State<T>{Smv, SLv}, x0m, x0L);
 
   // phase 3: the Kalman filter of every chunk from its start state
   const MV<T> Lkv = rowmajor(L.Lk, D, DD);
@@ -371,24 +620,7 @@ void run_smoother(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t ft
   }
   // smoothed state at every chunk end, from the terminal (filtered) state
   const MV<T> emv{L.em, 1, 1, D}, eLv = rowmajor(L.eL, D, DD);
-  const MV<T> cm{L.v2, 1, 1, 0}, cL = rowmajor(L.Mm, D, 0), X5v = rowmajor(L.X5, 2 * D, 0);
-  const MV<T> v1{L.v1, 1, 1, 0};
-  cx.copy(1, D, 1, MV<T>{om + n * D, 1, 1, 0}, cm);
-  cx.copy(1, D, D, rowmajor(oL + n * DD, D, 0), cL);
-  for (int j = P - 1; j >= 0; --j) {
-    cx.copy(1, D, 1, cm, MV<T>{L.em + (int64_t)j * D, 1, 1, 0});
-    cx.copy(1, D, D, cL, rowmajor(L.eL + j * DD, D, 0));
-    if (j == 0) break;
-    const MV<T> Ej = rowmajor(L.tE[ce] + j * DD, D, 0), Dj = rowmajor(L.tD + j * DD, D, 0);
-    const MV<T> gj{L.tg + (int64_t)j * D, 1, 1, 0};
-    cx.copy(1, D, 1, gj, v1);
-    cx.gemm(1, D, 1, D, one, Ej, cm, one, v1);
-    cx.gemm(1, D, D, D, one, Ej, cL, zero, X5v);
-    cx.copy(1, D, D, Dj, sub(X5v, 0, D));
-    cx.tria(1, D, 2 * D, X5v);
-    cx.copy(1, D, 1, v1, cm);
-    cx.copy(1, D, D, X5v, cL);
-  }
+  smoother_tree(cx, L, SElem<T>{tgv, tEv[ce], tDv}, State<T>{emv, eLv}, om + n * D, oL + n * DD);
   // backward recursion inside every chunk
   const MV<T> tmv{L.tm, 1, 1, D};
   for (int off = C0 - 1; off >= 0; --off) {

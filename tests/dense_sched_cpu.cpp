@@ -37,27 +37,31 @@ struct CpuCtx {
   std::string err;
   const char* op = "";
 
-  bool ok(const double* p, bool write) {
+  // p must lie in the buffer (a workspace region of the layout, an input or
+  // an output) that holds `base`, the first element of the view it is read
+  // through: an index running past its own buffer into a neighbour is caught
+  bool ok(const double* p, bool write, const double* base = nullptr) {
+    if (!base) base = p;
     for (const Range& r : ranges)
-      if (p >= r.lo && p < r.lo + r.count) {
-        if (write && !r.writable) break;
-        return true;
+      if (base >= r.lo && base < r.lo + r.count) {
+        if (p >= r.lo && p < r.lo + r.count && !(write && !r.writable)) return true;
+        break;
       }
     if (err.empty()) {
       char buf[256];
-      snprintf(buf, sizeof buf, "%s: %s access at %p outside every buffer", op, write ? "write" : "read",
-               (const void*)p);
+      snprintf(buf, sizeof buf, "%s: %s access at %p outside the buffer of its view (base %p)", op,
+               write ? "write" : "read", (const void*)p, (const void*)base);
       err = buf;
     }
     return false;
   }
   double get(const MV<double>& a, int64_t b, int64_t i, int64_t j) {
     const double* p = a.p + b * a.bs + i * a.rs + j * a.cs;
-    return ok(p, false) ? *p : std::numeric_limits<double>::quiet_NaN();
+    return ok(p, false, a.p) ? *p : std::numeric_limits<double>::quiet_NaN();
   }
   void put(const MV<double>& a, int64_t b, int64_t i, int64_t j, double v) {
     double* p = a.p + b * a.bs + i * a.rs + j * a.cs;
-    if (ok(p, true)) *p = v;
+    if (ok(p, true, a.p)) *p = v;
   }
 
   void gemm(int64_t batch, int M, int N, int K, double alpha, MV<double> A, MV<double> B, double beta,
@@ -224,13 +228,15 @@ extern "C" int dense_cpu_filtsmooth(int which, int64_t n, int D, int d, const do
   std::vector<double> ws(sz.total / sizeof(double) + 64, std::numeric_limits<double>::quiet_NaN());
   char* base = reinterpret_cast<char*>(ws.data());
   char* al = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 255) & ~uintptr_t(255));
-  Layout<double> L = layout<double>(al, which, n, D, d, chunks);
+  std::vector<std::pair<size_t, size_t>> regions;
+  Layout<double> L = layout<double>(al, which, n, D, d, chunks, &regions);
   CpuCtx cx;
   cx.D = D;
   const int64_t DD = (int64_t)D * D;
   const int64_t ft_count = fts ? n * DD : DD;
-  cx.ranges.push_back({"workspace", reinterpret_cast<const double*>(al),
-                       (int64_t)((base + ws.size() * sizeof(double) - al) / (int64_t)sizeof(double)), true});
+  for (const auto& r : regions)
+    cx.ranges.push_back({"workspace", reinterpret_cast<const double*>(al + r.first),
+                         (int64_t)(r.second / sizeof(double)), true});
   if (which != 2) {
     cx.ranges.push_back({"x0m", x0m, D, false});
     cx.ranges.push_back({"x0L", x0L, DD, false});

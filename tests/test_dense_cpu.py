@@ -104,8 +104,8 @@ def _expected(x0, dtm, dom, C0, P):
     n, d, D = H.shape
     Rs = np.zeros((n, d, d)) if R is None else R
     dom_o = (H, c, Rs)
-    (fm, fL), nll, fobj, ssq, _ = blocked.filter_blocked(x0, (F, QL), dom_o, C0=C0, Cs=(P,), segmented=True)
-    (sm, sL), sobj = blocked.smoother_blocked((F, QL), (fm, fL), C0=C0, Cs=(P,), segmented=True)
+    (fm, fL), nll, fobj, ssq, _ = blocked.filter_blocked(x0, (F, QL), dom_o, C0=C0, Cs=(2,), segmented=True)
+    (sm, sL), sobj = blocked.smoother_blocked((F, QL), (fm, fL), C0=C0, Cs=(2,), segmented=True)
     return (fm, fL), (sm, sL), nll, fobj, sobj, ssq
 
 

@@ -73,8 +73,8 @@ def _expected(x0, dtm, dom, C0, P):
     H, c, R = dom
     n, d, D = H.shape
     Rs = np.zeros((n, d, d)) if R is None else R
-    (fm, fL), nll, fobj, ssq, _ = blocked.filter_blocked(x0, dtm, (H, c, Rs), C0=C0, Cs=(P,), segmented=True)
-    (sm, sL), sobj = blocked.smoother_blocked(dtm, (fm, fL), C0=C0, Cs=(P,), segmented=True)
+    (fm, fL), nll, fobj, ssq, _ = blocked.filter_blocked(x0, dtm, (H, c, Rs), C0=C0, Cs=(2,), segmented=True)
+    (sm, sL), sobj = blocked.smoother_blocked(dtm, (fm, fL), C0=C0, Cs=(2,), segmented=True)
     return (fm, fL), (sm, sL), nll, fobj, sobj, ssq
 
 
