@@ -498,6 +498,8 @@ def run_gpu(args, workload):
         extras["config0"] = config0_block(args)
         extras["batched"] = batched_block(args)
         extras["served"] = served_block(args)
+        if world == 1:
+            extras["dense"] = dense_block(args)
 
     if rank != 0:
         return
@@ -1579,29 +1581,24 @@ DENSE_WORKLOADS = {
 }
 
 
-def run_dense(args, workload):
-    """One IEKS iteration's work on the dense path (D >= 32): EK1
-    linearization of the reaction-diffusion field plus the dense filter +
-    smoother pass, float32 over the whole grid and float64 over its first
-    --dense-f64-steps steps (the per-step cost is uniform: the chunks run
-    their steps one after the other, the top levels add P - 1 boundary
-    steps), from the constant-init trajectory; with --dense-solve also the
-    whole mixed-precision solve (float32 iterations, float64 polish)."""
+def dense_passes(workload, precisions, f64_steps, steps, warmup, n_override=0):
+    """Time one IEKS iteration's work on the dense path (EK1 linearization of
+    the reaction-diffusion field + the dense filter + smoother pass) from the
+    constant-init trajectory: float32 over the whole grid, float64 over its
+    first f64_steps steps (the per-step cost is uniform: the chunks run their
+    steps one after the other, the tree above them adds log2(P) levels).
+    Returns {precision: {...}} and the problem's set-up."""
     import torch
 
-    rank, world, local = dist_info()
-    torch.cuda.set_device(local)
-    from pof import _build, _flops, _lib, ivp as pivp, solver as psolver
+    from pof import _flops, ivp as pivp
     from pof.convenience import get_initial_trajectory, set_up_solver
     from pof.parallel_filtsmooth import linear_filtsmooth
     from pof.step import linearize_at_previous_states
     from pof.utils import MVNSqrt
 
-    _build.build(verbose=False)
-    lib = _lib.lib()
     cells, q, N, tmax = DENSE_WORKLOADS[workload]
-    if args.dense_n:
-        N = args.dense_n
+    if n_override:
+        N = n_override
     pv = pivp.fhn_reaction_diffusion(cells=cells, tmax=tmax)
     ts = torch.linspace(0.0, tmax, N, dtype=torch.float64)
     setup = set_up_solver(f=pv.f, y0=pv.y0, ts=ts, order=q)
@@ -1609,14 +1606,14 @@ def run_dense(args, workload):
     D = states.mean.shape[1]
     d = 2 * cells
     n = N - 1
-    chunks = int(os.environ.get("POF_DENSE_CHUNKS", "64"))
+    env_chunks = int(os.environ.get("POF_DENSE_CHUNKS", "0"))
     x0, dtm = setup["x0"], setup["dtm"]
 
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         ts_ = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -1627,27 +1624,65 @@ def run_dense(args, workload):
         return float(np.median(ts_))
 
     out = {}
-    peak64 = fp64_peak(torch, lib, _lib)
-    passes = [("float32", n), ("float64", min(n, args.dense_f64_steps))]
-    passes = [pp for pp in passes if pp[0] in args.dense_precisions.split(",")]
-    for prec, nsteps in passes:
+    passes = [("float32", n), ("float64", min(n, f64_steps))]
+    for prec, nsteps in [pp for pp in passes if pp[0] in precisions]:
         dt = torch.float32 if prec == "float32" else torch.float64
-        m = states.mean[: nsteps + 1]
-        sub = MVNSqrt(m, states.chol[: nsteps + 1])
+        sub = MVNSqrt(states.mean[: nsteps + 1], states.chol[: nsteps + 1])
         F, QL = dtm.F[0].to(dt), dtm.QL[0].to(dt)
         x0t = MVNSqrt(x0.mean.to(dt), x0.chol.to(dt))
         res = {}
 
         def one():
             dom = linearize_at_previous_states(setup["om"], sub)
-            H, c = dom.H.to(dt), dom.b.to(dt)
-            res["out"] = linear_filtsmooth(x0t, (F, QL), (H, c, None))
+            res["out"] = linear_filtsmooth(x0t, (F, QL), (dom.H.to(dt), dom.b.to(dt), None))
 
         ms = timed(one)
-        fl = _flops.dense_pass_flops(nsteps, D, d, min(chunks, nsteps))
-        finite = bool(torch.isfinite(res["out"][0].mean).all().item())
-        out[prec] = {"steps": nsteps, "ms_per_pass": ms, "ms_per_step": ms / nsteps, "gflops": fl / (ms * 1e-3) / 1e9,
-                     "flop_model_tflop": fl / 1e12, "finite": finite}
+        chunks = min(env_chunks or (256 if prec == "float32" else 64), nsteps)
+        fl = _flops.dense_pass_flops(nsteps, D, d, chunks)
+        out[prec] = {"steps": nsteps, "chunks": chunks, "ms_per_pass": ms, "ms_per_step": ms / nsteps,
+                     "gflops": fl / (ms * 1e-3) / 1e9, "flop_model_tflop": fl / 1e12,
+                     "finite": bool(torch.isfinite(res["out"][0].mean).all().item())}
+        del res
+    info = {"cells": cells, "d": d, "D": D, "q": q, "N": N, "tmax": tmax,
+            "field_params": "a = b = 0.2, c = 3, kv = 0.5, kw = 0.05, v0 = -1 + 0.5 sin(2 pi k / 64), w0 = 1"}
+    return out, info, (pv, ts, q)
+
+
+def dense_block(args):
+    """The default line's dense block: the reaction-diffusion system at
+    (D, d) = (640, 128), N = 2^12 -- a float32 pass over the whole grid and a
+    float64 pass over its first 256 steps (one IEKS iteration's work each)."""
+    import torch
+
+    from pof import _lib
+
+    out, info, _ = dense_passes("rd_d640", ("float32", "float64"), 256, 1, 1)
+    peak64 = fp64_peak(torch, _lib.lib(), _lib)
+    out["float64"]["frac_of_fp64_probe"] = out["float64"]["gflops"] / peak64
+    torch.cuda.empty_cache()
+    return {"workload": "rd_d640: method-of-lines FitzHugh-Nagumo, 64 periodic cells (d = 128), q = 4 (D = 640), "
+                        "N = 4096, t in [0, 20]; one IEKS iteration's work (EK1 + dense filter + smoother) from "
+                        "the constant-init trajectory; float64 over the first 256 steps",
+            "config": info, "float32": out["float32"], "float64": out["float64"], "fp64_probe_gflops": peak64,
+            "flop_model": "pof/_flops.py dense_pass_flops: 12.3 GFLOP per step at (640, 128)"}
+
+
+def run_dense(args, workload):
+    """The dense workload on its own line (python bench.py --workload rd_d640);
+    with --dense-solve also the whole mixed-precision solve (float32
+    iterations, float64 polish)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from pof import _build, _lib, solver as psolver
+
+    _build.build(verbose=False)
+    lib = _lib.lib()
+    out, info, (pv, ts, q) = dense_passes(workload, args.dense_precisions.split(","), args.dense_f64_steps,
+                                          args.steps, args.warmup, args.dense_n)
+    peak64 = fp64_peak(torch, lib, _lib)
+    n = info["N"] - 1
     full64_ms = None
     if "float64" in out:
         out["float64"]["frac_of_fp64_probe"] = out["float64"]["gflops"] / peak64
@@ -1655,26 +1690,22 @@ def run_dense(args, workload):
     solve = None
     if args.dense_solve:
         t0 = time.time()
-        (ym, yL), info = psolver.solve(f=pv.f, y0=pv.y0, ts=ts, order=q, init="constant", precision="mixed",
-                                       rtol_f32=1e-4, maxiters=100, maxiters_f32=100)
+        (ym, yL), sinfo = psolver.solve(f=pv.f, y0=pv.y0, ts=ts, order=q, init="constant", precision="mixed",
+                                        rtol_f32=1e-4, maxiters=100, maxiters_f32=100)
         torch.cuda.synchronize()
-        solve = {"seconds": time.time() - t0, "iterations_float32": int(info["iterations_float32"]),
-                 "iterations_float64": int(info["iterations"]), "status": int(info["status"])}
+        solve = {"seconds": time.time() - t0, "iterations_float32": int(sinfo["iterations_float32"]),
+                 "iterations_float64": int(sinfo["iterations"]), "status": int(sinfo["status"])}
     if rank != 0:
         return
+    first = next(iter(out.values()))
     jprint({
         "metric": "dense filter + smoother pass (one IEKS iteration's work), ms per pass",
-        "value": next(iter(out.values()))["ms_per_pass"],
-        "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": next(iter(out.values()))["ms_per_pass"], "higher_is_better": False, "scaling": "weak",
+        "value": first["ms_per_pass"], "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": first["ms_per_pass"], "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (value), f64", "data": "synthetic",
-        "config": {"workload": workload, "cells": cells, "d": d, "D": D, "q": q, "N": N, "tmax": tmax,
-                   "chunks": chunks, "field_params": "a = b = 0.2, c = 3, kv = 0.5, kw = 0.05, "
-                                                     "v0 = -1 + 0.5 sin(2 pi k / 64), w0 = 1"},
+        "config": dict(info, workload=workload),
         "float32": out.get("float32"), "float64": out.get("float64"),
-        "float64_full_grid_ms_estimate": full64_ms,
-        "fp64_probe_gflops": peak64,
-        "mixed_solve": solve,
+        "float64_full_grid_ms_estimate": full64_ms, "fp64_probe_gflops": peak64, "mixed_solve": solve,
     })
 
 

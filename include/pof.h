@@ -163,8 +163,8 @@ int pof_smoothing(int32_t dtype, int64_t n_steps, int32_t D, const void* F, cons
  * chunks.  which: POF_DENSE_FILTER (pof_linear_noiseless_filtering),
  * POF_DENSE_FILTSMOOTH (pof_linear_filtsmooth), POF_DENSE_SMOOTHING
  * (pof_smoothing: x0_mean / x0_chol are the filtered means (N, D) / chols
- * (N, D, D); H, c, R unused).  chunks: the number of chunks (0: 64, or the
- * POF_DENSE_CHUNKS environment variable; at most n_steps).  Arguments and
+ * (N, D, D); H, c, R unused).  chunks: the number of chunks (0: 64 in float64, 256 in
+ * float32, or the POF_DENSE_CHUNKS environment variable; at most n_steps).  Arguments and
  * outputs otherwise as pof_linear_filtsmooth's. */
 enum { POF_DENSE_FILTER = 0, POF_DENSE_FILTSMOOTH = 1, POF_DENSE_SMOOTHING = 2 };
 size_t pof_dense_workspace_bytes(int32_t dtype, int32_t which, int64_t n_steps, int32_t D, int32_t d,
