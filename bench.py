@@ -899,7 +899,9 @@ def served_block(args):
             "served_mixed": servedmx,
             "plain_fifo": {"p50_s": float(np.percentile(lat_plain, 50)), "p99_s": float(np.percentile(lat_plain, 99)),
                            "ivp_steps_per_s": steps_total / (fin - arrivals[0])},
-            "omitted": "reaction-diffusion d = 128 requests (the dense D >= 128 path is not built)"}
+            "omitted": "reaction-diffusion d = 128 requests: the serving engines batch the small-D kernels; the "
+                       "dense path solves that system on its own (the default line's dense block, --workload "
+                       "rd_d640 --dense-solve)"}
 
 
 # ---------------------------------------------------------------------------
@@ -1421,7 +1423,8 @@ def run_serve(args, workload):
                    "fields": "logistic, fhn_classic, lotkavolterra, vanderpol mu=10 (+-20 % parameters)",
                    "N": "log-uniform in [2^8, 2^16]", "q": [2, 3, 4], "tolerances": [1e-4, 1e-6],
                    "total_steps": steps_total,
-                   "omitted": "reaction-diffusion d = 128 (needs the dense D >= 128 combine, not built)"},
+                   "omitted": "reaction-diffusion d = 128 requests: the serving engines batch the small-D kernels; "
+                              "the dense path solves that system on its own (--workload rd_d640 --dense-solve)"},
         "rates": lines,
         "plain_solve_s_total": float(sum(plain_t)),
     })
@@ -1558,8 +1561,8 @@ def run_mixed(args, workload):
         "ms_per_step": results["batched_mixed"]["ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": workload, "problems": names, "N": N, "q": q, "D": D, "maxiters": maxiters,
-                   "omitted": "the reaction-diffusion system (d = 128) of the configuration: needs the dense D >= 128 "
-                              "combine, not built"},
+                   "omitted": "the reaction-diffusion system (d = 128) of the configuration: its mixed solve runs "
+                              "on the dense path from the host (--workload rd_d640 --dense-solve)"},
         "plain_float64": {"value": steps / (plain64_ms * 1e-3), "ms": plain64_ms},
         "plain_mixed": {"value": steps / (plainmx_ms * 1e-3), "ms": plainmx_ms},
         "batched_float64": {"value": steps / (results["batched_float64"]["ms"] * 1e-3),

@@ -12,6 +12,7 @@ the same request served alone (pof_server_* in include/pof.h).
 """
 
 import ctypes
+import threading
 import time
 from collections import deque
 from typing import Any, NamedTuple
@@ -150,12 +151,141 @@ class Engine:
         return out
 
 
+def dense_field(field, params, y0):
+    """The torch vector field of a request for a field the dense path solves
+    (pof._lib.DENSE_FIELDS)."""
+    from . import ivp as pivp
+
+    if field == "fhn_rd":
+        a, b, c, kv, kw = (float(p) for p in params)
+        return pivp.fhn_reaction_diffusion(cells=len(y0) // 2, a=a, b=b, c=c, kv=kv, kw=kw, y0=y0).f
+    raise ValueError("no dense field %r" % (field,))
+
+
+class _DenseJob:
+    def __init__(self, req, nbytes):
+        self.req = req
+        self.nbytes = nbytes
+        self.stop = threading.Event()
+        self.out = None
+        self.error = None
+        self.thread = None
+
+
+class DenseLane:
+    """Requests of the dense path's fields (state dimension D >= 32, e.g. the
+    reaction-diffusion system of pof.ivp.fhn_reaction_diffusion): each
+    admitted request runs its IEKS loop (pof.solver.solve, the host-driven
+    loop over the dense filter/smoother) on a CUDA stream of its own in a
+    worker thread, so its kernels overlap with the serving engines' and with
+    the other dense requests'.  Admission in arrival order while the sum of
+    the running requests' memory (dense workspace, trajectories, linearized
+    models) stays within budget_bytes; cancellation and timeouts act before
+    the request's next IEKS iteration.  A request's result is the one
+    pof.solver.solve gives for it alone."""
+
+    def __init__(self, device, budget_bytes, precision="float64", maxiters_f32=10_000, rtol_f32=1e-5,
+                 settle_f32=float("inf"), solve=None):
+        self.dev = device
+        self.budget = int(budget_bytes)
+        self.precision = dict(precision=precision, maxiters_f32=maxiters_f32, rtol_f32=rtol_f32,
+                              settle_f32=settle_f32)
+        self.jobs = {}  # rid -> _DenseJob
+        self._solve = solve
+
+    def bytes_for(self, req):
+        """Device memory of one request: the dense workspace (float64, and
+        float32 for mixed precision), three trajectories and the linearized
+        model."""
+        lib = _lib.lib()
+        d = len(req.y0)
+        D = d * (req.order + 1)
+        n = len(req.ts) - 1
+        ws = lib.pof_dense_workspace_bytes(_lib.POF_F64, 1, n, D, d, 0)
+        if self.precision["precision"] == "mixed":
+            ws += lib.pof_dense_workspace_bytes(_lib.POF_F32, 1, n, D, d, 0)
+        return int(ws + 3 * 8 * (n + 1) * D * (D + 1) + 2 * 8 * n * d * (D + d))
+
+    def in_use(self):
+        return sum(j.nbytes for j in self.jobs.values())
+
+    def submit(self, req):
+        """Start request req if the budget allows (the first request always
+        starts); False otherwise."""
+        nb = self.bytes_for(req)
+        if self.jobs and self.in_use() + nb > self.budget:
+            return False
+        job = _DenseJob(req, nb)
+        job.thread = threading.Thread(target=self._run, args=(job,), daemon=True)
+        self.jobs[req.rid] = job
+        job.thread.start()
+        return True
+
+    def _run(self, job):
+        req = job.req
+        try:
+            if self._solve is not None:  # a stand-in for tests without a GPU
+                job.out = self._solve(req, job.stop.is_set)
+                return
+            from . import solver
+
+            torch.cuda.set_device(self.dev)
+            st = torch.cuda.Stream(self.dev)
+            with torch.cuda.stream(st):
+                f = dense_field(req.field, req.params, torch.as_tensor(req.y0, dtype=torch.float64))
+                ys, info = solver.solve(f=f, y0=torch.as_tensor(req.y0, dtype=torch.float64),
+                                        ts=torch.as_tensor(req.ts, dtype=torch.float64), order=req.order,
+                                        init="constant", maxiters=req.maxiters, rtol=req.rtol,
+                                        stop=job.stop.is_set, **self.precision)
+                st.synchronize()
+            job.out = (ys, info)
+        except Exception as e:  # reported by finished()
+            job.error = e
+
+    def cancel(self, rid):
+        job = self.jobs.get(rid)
+        if job is None:
+            return False
+        job.stop.set()
+        return True
+
+    def finished(self):
+        """[(request, (means, chols), info tensor)] of the requests whose
+        loop ended since the last call."""
+        out = []
+        for rid in [r for r, j in self.jobs.items() if not j.thread.is_alive()]:
+            job = self.jobs.pop(rid)
+            if job.error is not None:
+                raise job.error
+            ys, info = job.out
+            t = torch.zeros(_lib.I_COUNT + (2 if "iterations_float32" in info else 0), dtype=torch.float64)
+            t[_lib.I_ITERATIONS] = float(info["iterations"])
+            t[_lib.I_NLL] = float(info["nll"])
+            t[_lib.I_OBJ] = float(info["obj"])
+            t[_lib.I_SSQ] = float(info["sigma_squared"])
+            t[_lib.I_STATUS] = float(info["status"])
+            if "iterations_float32" in info:
+                t[_lib.I_COUNT] = float(info["iterations_float32"])
+                t[_lib.I_COUNT + 1] = float(info["best_change_float32"])
+            out.append((job.req, (ys.mean, ys.chol), t))
+        return out
+
+    def close(self):
+        for job in self.jobs.values():
+            job.stop.set()
+        for job in self.jobs.values():
+            job.thread.join()
+        self.jobs = {}
+
+
 class Server:
     """Host side of continuous batching: a FIFO of requests, one Engine per
-    (d, q), admission each tick as memory allows."""
+    (d, q), admission each tick as memory allows; requests of the dense
+    path's fields go to the DenseLane (dense_budget_bytes of device memory
+    for the running ones)."""
 
     def __init__(self, max_requests=1024, max_points=1 << 21, device=None, precision="float64", maxiters_f32=10_000,
-                 rtol_f32=1e-5, settle_f32=float("inf")):
+                 rtol_f32=1e-5, settle_f32=float("inf"), dense_budget_bytes=64 << 30, dense_solve=None):
         """precision="mixed": every request runs float32 IEKS iterations first
         and float64 ones after (pof_server_create_mixed; the float32 phase's
         rules and discard rule are those of pof.solver.solve's
@@ -173,6 +303,8 @@ class Server:
         self.t_done = {}
         self.prepared = {}
         self.stop_reason = {}  # rid -> "cancelled" | "timeout" for requests stopped by the host
+        self.dense = DenseLane(self.dev, dense_budget_bytes, solve=dense_solve, **self.precision)
+        self.dense_queue = deque()
 
     def engine(self, d, q):
         key = (d, q)
@@ -189,8 +321,9 @@ class Server:
         self.next_rid += 1
         t0 = time.perf_counter() if t_arrival is None else t_arrival
         deadline = float("inf") if timeout is None else t0 + float(timeout)
-        self.queue.append(Request(rid, field, tuple(float(p) for p in params), np.asarray(y0, dtype=np.float64),
-                                  np.asarray(ts, dtype=np.float64), int(order), float(rtol), int(maxiters), deadline))
+        req = Request(rid, field, tuple(float(p) for p in params), np.asarray(y0, dtype=np.float64),
+                      np.asarray(ts, dtype=np.float64), int(order), float(rtol), int(maxiters), deadline)
+        (self.dense_queue if field in _lib.DENSE_FIELDS else self.queue).append(req)
         self.t_submit[rid] = t0
         return rid
 
@@ -201,9 +334,10 @@ class Server:
         is `reason`.  False when rid has already finished."""
         if rid in self.results:
             return False
-        for r in self.queue:
+        for r in list(self.queue) + list(self.dense_queue):
             if r.rid == rid:
                 self.queue = deque(q for q in self.queue if q.rid != rid)
+                self.dense_queue = deque(q for q in self.dense_queue if q.rid != rid)
                 self.prepared.pop(rid, None)
                 info = torch.full((_lib.I_COUNT,), float("nan"), dtype=torch.float64)
                 info[_lib.I_ITERATIONS] = 0.0
@@ -216,19 +350,25 @@ class Server:
             if e.cancel(rid):
                 self.stop_reason[rid] = reason
                 return True
+        if self.dense.cancel(rid):
+            self.stop_reason[rid] = reason
+            return True
         return False
 
     def _expire(self):
         """Cancel the requests whose deadline has passed (status "timeout")."""
         now = time.perf_counter()
-        late = [r.rid for r in self.queue if r.deadline <= now]
+        late = [r.rid for r in list(self.queue) + list(self.dense_queue) if r.deadline <= now]
         for e in self.engines.values():
             late += [req.rid for req, _ in e.slots.values() if req.deadline <= now and req.rid not in self.stop_reason]
+        late += [rid for rid, j in self.dense.jobs.items() if j.req.deadline <= now and rid not in self.stop_reason]
         for rid in late:
             self.cancel(rid, reason="timeout")
 
     def _admit(self):
         """Prepare and admit queued requests in arrival order while engines take them."""
+        while self.dense_queue and self.dense.submit(self.dense_queue[0]):
+            self.dense_queue.popleft()
         if not self.queue:
             return
         reqs = list(self.queue)
@@ -273,10 +413,15 @@ class Server:
                 self.results[req.rid] = (ys, info)
                 self.t_done[req.rid] = time.perf_counter()
                 done.append(req.rid)
+        for req, ys, info in self.dense.finished():
+            self.results[req.rid] = (ys, info)
+            self.t_done[req.rid] = time.perf_counter()
+            done.append(req.rid)
         return done
 
     def busy(self):
-        return bool(self.queue) or any(e.slots for e in self.engines.values())
+        return (bool(self.queue) or bool(self.dense_queue) or bool(self.dense.jobs)
+                or any(e.slots for e in self.engines.values()))
 
     def result(self, rid):
         """((means (N, d), chol_covs (N, d, D)), info) as pof.solver.solve
@@ -296,6 +441,7 @@ class Server:
         return ys, out
 
     def close(self):
+        self.dense.close()
         for e in self.engines.values():
             e.close()
         self.engines = {}

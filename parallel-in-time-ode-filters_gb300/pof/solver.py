@@ -71,7 +71,7 @@ def _solve_builtin(setup, states, calibrate, maxiters, precision="float64", maxi
 
 
 def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, sequential=False,
-          precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, settle_f32=float("inf")):
+          precision="float64", maxiters_f32=10_000, rtol_f32=1e-5, settle_f32=float("inf"), rtol=1e-6, stop=None):
     """Parallel-in-time IEKS (pof/solver.py:11-73).
 
     Returns (MVNSqrt(means (N, d), chol_covs (N, d, D)), info) with
@@ -87,7 +87,13 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     signature): float32 IEKS iterations until the objective's relative change
     is below rtol_f32, then float64 iterations to the reference's criterion;
     info["iterations"] counts the float64 ones, info["iterations_float32"]
-    the others."""
+    the others.
+
+    rtol: the objective tolerance of crit (pof/convergence_criteria.py:4-13,
+    the reference's 1e-6; the device loops take the reference's value).
+    stop: a callable checked before every iteration of the host-driven loops
+    (fields without a device loop at their shape); once it returns True the
+    loop ends with the last iterate and info["status"] 3 (cancelled)."""
     setup = set_up_solver(f=f, y0=y0, ts=ts, order=order)
     om = setup["om"]
     x0 = setup["x0"]
@@ -102,17 +108,24 @@ def solve(*, f, y0, ts, order, init="prior", calibrate=True, maxiters=10_000, se
     if precision == "mixed" and om.field is not None and not sequential:
         # fields without a device loop at this shape (the dense path's):
         # the same float32 phase and float64 polish, driven from the host
-        means, it32, best = _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32)
-        out, info_dict = _solve_loop(setup, MVNSqrt(means, states.chol), calibrate, maxiters, sequential)
+        means, it32, best = _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32, stop)
+        out, info_dict = _solve_loop(setup, MVNSqrt(means, states.chol), calibrate, maxiters, sequential, rtol, stop)
         info_dict["iterations_float32"] = torch.tensor(it32)
         info_dict["best_change_float32"] = torch.tensor(best, dtype=torch.float64)
         return out, info_dict
     if precision != "float64":
         raise NotImplementedError("precision=%r needs a built-in field (pof.ivp)" % (precision,))
-    return _solve_loop(setup, states, calibrate, maxiters, sequential)
+    return _solve_loop(setup, states, calibrate, maxiters, sequential, rtol, stop)
 
 
-def _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32):
+def _wait(dev):
+    """Wait for this thread's current stream before a host read (the wait
+    releases the GIL, so other host threads run meanwhile)."""
+    if dev.type == "cuda":
+        torch.cuda.current_stream(dev).synchronize()
+
+
+def _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32, stop=None):
     """The float32 iterations of pof_ieks_solve_mixed, driven from the host
     (for fields the device loops do not take, e.g. the dense path's): each
     linearizes in float64 at the current trajectory, scales every observation
@@ -136,6 +149,8 @@ def _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32):
     keep = means
     it32, prev, best, worse = 0, float("inf"), float("inf"), 0
     while it32 < maxiters_f32:
+        if stop is not None and stop():
+            break
         dom = linearize_at_previous_states(om, MVNSqrt(means, states.chol))
         inv = 1.0 / torch.linalg.vector_norm(dom.H, dim=-1)
         inv = torch.where(torch.isfinite(inv), inv, torch.ones_like(inv))
@@ -143,6 +158,7 @@ def _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32):
         c32 = (dom.b * inv).to(torch.float32)
         out, _, _, _ = parallel_linear_filtsmooth(x032, dtm32, (H32, c32, None))
         cand = out.mean.to(torch.float64)
+        _wait(cand.device)
         if not bool(torch.isfinite(cand).all()):
             break
         y_new, y_old = cand @ E0.T, means @ E0.T
@@ -163,7 +179,7 @@ def _float32_phase(setup, states, maxiters_f32, rtol_f32, settle_f32):
     return means, it32, best
 
 
-def _solve_loop(setup, states, calibrate, maxiters, sequential):
+def _solve_loop(setup, states, calibrate, maxiters, sequential, rtol=1e-6, stop=None):
     """The IEKS loop of pof/solver.py:24-73 in Python: each iteration
     linearizes (libpof for built-in fields, torch.func otherwise) and runs
     libpof's filter/smoother; crit is read back each iteration."""
@@ -174,11 +190,16 @@ def _solve_loop(setup, states, calibrate, maxiters, sequential):
     states_old, nll_old, obj_old = states, z, z
     k = 0
     conv = False
+    cancelled = False
     while True:
         # cond (solver.py:36-45)
         if k >= 1:
-            conv = bool(convergence_criteria.crit(obj, obj_old, nll, nll_old, states, states_old))
+            _wait(dev)
+            conv = bool(convergence_criteria.crit(obj, obj_old, nll, nll_old, states, states_old, rtol=rtol))
         if not (k < 1 or (not conv and k <= maxiters)):
+            break
+        if stop is not None and stop():
+            cancelled = True
             break
         # body (solver.py:47-55)
         states_old, nll_old, obj_old = states, nll, obj
@@ -186,7 +207,7 @@ def _solve_loop(setup, states, calibrate, maxiters, sequential):
         k += 1
     # the stopping reason (POF_SOLVE_*), as libpof's loop reports it
     finite = bool(torch.isfinite(torch.as_tensor(obj)).item() and torch.isfinite(torch.as_tensor(nll)).item())
-    status = 0 if (finite and conv) else (1 if finite else 2)
+    status = 3 if cancelled else (0 if (finite and conv) else (1 if finite else 2))
     info_dict = {"iterations": torch.tensor(k), "nll": nll, "obj": obj, "sigma_squared": ssq,
                  "status": torch.tensor(status), "calibrated": False}
     if calibrate:

@@ -169,3 +169,31 @@ def test_served_mixed_precision():
         print("[served mixed %s] float32 %d + float64 %d iterations (float64 alone %d), %.3g from float64" % (
             nm, int(gi["iterations_float32"]), int(gi["iterations"]), int(fi["iterations"]), err))
         assert err <= 1e-6
+
+
+def test_served_dense_request_same_as_alone():
+    """A reaction-diffusion request (a field of the dense path) is served by
+    the dense lane -- its own IEKS loop on its own stream in a worker thread
+    -- while small-D requests run in the engines; its result equals
+    pof.solver.solve of the same request alone, bit for bit."""
+    from pof import ivp as pivp, solver as psolver
+
+    cells, q, N = 4, 3, 97
+    pv = pivp.fhn_reaction_diffusion(cells=cells, tmax=3.0)
+    ts = np.linspace(0.0, 3.0, N)
+    params = (0.2, 0.2, 3.0, 0.5, 0.05)
+    srv = serve.Server(max_requests=8, max_points=1 << 16)
+    small = [srv.submit("logistic", (3.0,), [0.01], np.linspace(0.0, 10.0, n), 3) for n in (300, 900, 2000)]
+    rid = srv.submit("fhn_rd", params, pv.y0.numpy(), ts, q, rtol=1e-6, maxiters=200)
+    while srv.busy():
+        srv.tick()
+    (m, L), info = srv.result(rid)
+    (m1, L1), info1 = psolver.solve(f=pv.f, y0=pv.y0, ts=torch.as_tensor(ts), order=q, init="constant",
+                                    maxiters=200)
+    print("served RD: status %s, iterations %d (alone %d)" % (info["status"], int(info["iterations"]),
+                                                               int(info1["iterations"])))
+    assert info["status"] == "converged" and int(info["iterations"]) == int(info1["iterations"])
+    assert torch.equal(m.cpu(), m1.cpu()) and torch.equal(L.cpu(), L1.cpu())
+    for r in small:
+        assert srv.result(r)[1]["status"] == "converged"
+    srv.close()

@@ -12,12 +12,15 @@ gets back.
 """
 
 import ctypes
+import threading
+import time
 
 import numpy as np
 import pytest
 import torch
 
 from pof import _lib, batch as pbatch, serve
+from pof.utils import MVNSqrt
 
 CPU = torch.device("cpu")
 BUSY = -7
@@ -114,6 +117,9 @@ class FakeEngines:
         for i, slot in enumerate(out):
             arr[i] = slot
         return len(out)
+
+    def pof_dense_workspace_bytes(self, dtype, which, n, D, d, chunks):
+        return 1000 * n
 
     def pof_server_fetch(self, h, slot, m, L, info):
         s = self._s(h)
@@ -280,3 +286,108 @@ def test_mixed_precision_server(fake):
         _, info = srv.result(rid)
         assert int(info["iterations_float32"]) == n % 7 + 1
         assert int(info["iterations"]) == 2 + n // 100 and info["status"] == "converged"
+
+
+# ---------------------------------------------------------------------------
+# the dense lane (requests of pof._lib.DENSE_FIELDS, e.g. the reaction-diffusion
+# system): libpof's host-driven solve replaced by a stand-in that "iterates"
+# in its worker thread and checks the stop flag before every iteration
+# ---------------------------------------------------------------------------
+
+class FakeDenseSolve:
+    def __init__(self, iterations):
+        self.iterations = iterations  # n_steps -> iterations to convergence
+        self.lock = threading.Lock()
+        self.running = 0
+        self.max_running = 0
+        self.started = []
+
+    def __call__(self, req, stop):
+        with self.lock:
+            self.running += 1
+            self.max_running = max(self.max_running, self.running)
+            self.started.append(req.rid)
+        n = len(req.ts) - 1
+        k, status = 0, 0
+        while k < self.iterations(n):
+            if stop():
+                status = 3
+                break
+            time.sleep(0.002)
+            k += 1
+        with self.lock:
+            self.running -= 1
+        d = len(req.y0)
+        D = d * (req.order + 1)
+        ys = MVNSqrt(torch.full((n + 1, d), float(req.rid), dtype=torch.float64),
+                     torch.zeros((n + 1, d, D), dtype=torch.float64))
+        return ys, {"iterations": k, "nll": 1.0, "obj": 2.0, "sigma_squared": 3.0, "status": status}
+
+
+def rd(n, cells=4):
+    y0 = np.concatenate([-np.ones(cells), np.ones(cells)])
+    return ("fhn_rd", (0.2, 0.2, 3.0, 0.5, 0.05), y0, np.linspace(0.0, 2.0, n + 1))
+
+
+def _run_until_idle(srv, seconds=20.0):
+    t0 = time.time()
+    while srv.busy():
+        srv.tick()
+        time.sleep(0.001)
+        assert time.time() - t0 < seconds
+    return True
+
+
+def test_dense_lane_overlaps_engines_and_keeps_its_budget(fake):
+    """Dense-field requests run in the dense lane's worker threads while the
+    engines serve the small-D requests; with a budget for one dense request
+    at a time they start one after the other in arrival order; each gets its
+    own result."""
+    ds = FakeDenseSolve(iterations=lambda n: 5 + n // 50)
+    probe = serve.Server(max_requests=4, max_points=10**6, dense_solve=ds)
+    one = probe.dense.bytes_for(serve.Request(0, *rd(100), 3, 1e-6, 100))
+    srv = serve.Server(max_requests=4, max_points=10**6, dense_solve=ds, dense_budget_bytes=one + 1)
+    dr = [srv.submit(*rd(n), order=3) for n in (100, 60, 80)]
+    sr = [srv.submit(*logistic(n), order=2) for n in (300, 120)]
+    _run_until_idle(srv)
+    assert ds.started == dr and ds.max_running == 1
+    for rid, n in zip(dr, (100, 60, 80)):
+        (m, L), info = srv.result(rid)
+        assert m.shape == (n + 1, 8) and float(m[0, 0]) == rid
+        assert info["status"] == "converged" and int(info["iterations"]) == 5 + n // 50
+    for rid in sr:
+        assert srv.result(rid)[1]["status"] == "converged"
+    srv.close()
+
+
+def test_dense_lane_runs_requests_side_by_side_within_budget(fake):
+    ds = FakeDenseSolve(iterations=lambda n: 20)
+    srv = serve.Server(max_requests=4, max_points=10**6, dense_solve=ds, dense_budget_bytes=1 << 40)
+    rids = [srv.submit(*rd(50), order=2) for _ in range(3)]
+    _run_until_idle(srv)
+    assert ds.max_running >= 2
+    assert all(srv.result(r)[1]["status"] == "converged" for r in rids)
+
+
+def test_dense_lane_cancel_and_timeout(fake, monkeypatch):
+    """A running dense request stops before its next iteration once
+    cancelled (its last iterate returned, status "cancelled"), a queued one
+    leaves the queue, and one past its deadline reports "timeout"."""
+    ds = FakeDenseSolve(iterations=lambda n: 10**6 if n == 777 else 3)
+    probe = serve.Server(max_requests=4, max_points=10**6, dense_solve=ds)
+    one = probe.dense.bytes_for(serve.Request(0, *rd(777), 3, 1e-6, 100))
+    srv = serve.Server(max_requests=4, max_points=10**6, dense_solve=ds, dense_budget_bytes=one + 1)
+    a = srv.submit(*rd(777), order=3)           # runs "forever"
+    b = srv.submit(*rd(20), order=3)            # waits behind a
+    srv.tick()
+    time.sleep(0.02)
+    assert srv.cancel(b) and srv.cancel(a)
+    _run_until_idle(srv)
+    (ma, _), ia = srv.result(a)
+    assert ia["status"] == "cancelled" and ma.shape == (778, 8)
+    yb, ib = srv.result(b)
+    assert yb is None and ib["status"] == "cancelled"
+    c = srv.submit(*rd(777), order=3, timeout=0.05)
+    _run_until_idle(srv)
+    assert srv.result(c)[1]["status"] == "timeout"
+    srv.close()
