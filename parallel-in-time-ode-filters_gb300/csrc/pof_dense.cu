@@ -50,6 +50,11 @@ int panel_rows(int n, size_t es) {
   return nb;
 }
 
+// Panels of at least kClusterMinCols columns are factored by a cluster of
+// kClusterSize CTAs (k_tria_panel_cl), each holding a quarter of the columns.
+constexpr int kClusterSize = 4;
+constexpr int kClusterMinCols = 256;
+
 // ---------------------------------------------------------------------------
 // launches
 // ---------------------------------------------------------------------------
@@ -124,17 +129,25 @@ struct Ctx {
   }
 
   // In place: W (m x n, n >= m) -> L in its first m columns, zeros elsewhere.
+  bool cluster_panels;
   void tria(int64_t batch, int m, int n, MV<T> W) {
     if (batch <= 0) return;
-    const int nb = panel_rows(n, sizeof(T));
+    const bool cl = cluster_panels && n >= kClusterMinCols;
+    const int nb = cl ? panel_rows((n + kClusterSize - 1) / kClusterSize, sizeof(T)) : panel_rows(n, sizeof(T));
     for (int i0 = 0; i0 < m; i0 += nb) {
       const int nbb = std::min(nb, m - i0);
       const int np = n - i0;
-      const size_t smem = size_t(nbb) * np * sizeof(T);
       for (int64_t b0 = 0; b0 < batch; b0 += maxbatch) {
         const int64_t nbt = std::min<int64_t>(maxbatch, batch - b0);
         MV<T> Wb{W.p + b0 * W.bs, W.rs, W.cs, W.bs};
-        k_tria_panel<T><<<(unsigned)nbt, 512, smem, st>>>(Wb, i0, nbb, np, V, TV, vbs, 0);
+        if (cl && np >= kClusterMinCols) {
+          const size_t smem = size_t(nbb) * ((np + kClusterSize - 1) / kClusterSize) * sizeof(T);
+          k_tria_panel_cl<T, kClusterSize><<<(unsigned)(nbt * kClusterSize), 256, smem, st>>>(Wb, i0, nbb, np, V, TV,
+                                                                                            vbs, 0);
+        } else {
+          const size_t smem = size_t(nbb) * np * sizeof(T);
+          k_tria_panel<T><<<(unsigned)nbt, 512, smem, st>>>(Wb, i0, nbb, np, V, TV, vbs, 0);
+        }
         const int mt = m - i0 - nbb;
         if (mt > 0) {
           MV<T> Wtr = sub(Wb, i0 + nbb, i0);
@@ -263,11 +276,15 @@ int run(int which, int64_t n, int D, int d, const void* x0m, const void* x0L, co
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(k_tria_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kPanelSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tria_panel_cl<T, kClusterSize>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)kPanelSmem);
     if (e != cudaSuccess) return cuda_status(e);
     attr_set = true;
   }
   const char* e = getenv("POF_DENSE_TF32");
-  Ctx<T> cx{st, L.V, L.TV, L.Y, L.vbs, L.ybs, L.maxbatch, !(e && e[0] == '0'), D, 0};
+  const char* ec = getenv("POF_DENSE_CLUSTER");
+  Ctx<T> cx{st, L.V, L.TV, L.Y, L.vbs, L.ybs, L.maxbatch, !(e && e[0] == '0'), D, 0, !(ec && ec[0] == '0')};
   // one transition matrix: is it block-diagonal (Q1 = D / d, the IWP prior)?
   if (fts == 0 && d >= 1 && D % d == 0 && D / d < D) {
     const int q1 = D / d;

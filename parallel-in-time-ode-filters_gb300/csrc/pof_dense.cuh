@@ -6,6 +6,7 @@
 // smoother of pof_dense.cu are written on top of these primitives.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -353,6 +354,162 @@ __global__ void __launch_bounds__(512)
       TVb[i * np + c] = acc;
     }
   }
+}
+
+// The same panel factorization shared by a thread-block cluster of CS CTAs
+// per matrix: CTA r of the cluster holds the panel columns
+// [r w, (r + 1) w), w = ceil(np / CS), in its shared memory.  Per reflector
+// two cluster-wide reductions through distributed shared memory: the squared
+// norm of the row tail (with alpha from the CTA that holds the diagonal
+// column), then the dot products of the rows below with the reflector; the
+// partial sums are double-buffered by the reflector's parity, so two cluster
+// barriers per reflector order every write after the reads of the previous
+// use.  Every CTA runs the same sequence of barriers (no early exit).  The
+// Gram matrix of the reflectors is reduced the same way; T is formed in
+// every CTA (identical inputs, identical order); each CTA writes its columns
+// of the panel rows, V and T V.  Results equal k_tria_panel's up to the
+// order of the partial sums.
+template <typename T, int CS>
+__global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(256)
+    k_tria_panel_cl(MV<T> W, int i0, int nbb, int np, T* __restrict__ V, T* __restrict__ TV, int64_t vbs,
+                    int64_t b0) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* P = reinterpret_cast<T*>(smem_raw);  // nbb x w, row-major
+  __shared__ T red[32];
+  __shared__ T sq[2], al[2];
+  __shared__ T dots[2][kMaxPanel];
+  __shared__ T tau[kMaxPanel], beta[kMaxPanel];
+  __shared__ T Tm[kMaxPanel][kMaxPanel + 1];
+  __shared__ T G[kMaxPanel][kMaxPanel + 1];
+  const int t = threadIdx.x, bd = blockDim.x;
+  const int lane = t & 31, warp = t >> 5, nw = bd >> 5;
+  const int rank = (int)cluster.block_rank();
+  const int64_t b = b0 + blockIdx.x / CS;
+  const int w = (np + CS - 1) / CS;
+  const int c0 = rank * w;
+  const int wl = max(0, min(np, c0 + w) - c0);  // columns held here
+  T* Wb = W.p + b * W.bs + i0 * W.rs + i0 * W.cs;
+  for (int l = t; l < nbb * wl; l += bd) {
+    const int r = l / wl, c = l - r * wl;
+    P[r * w + c] = Wb[r * W.rs + (c0 + c) * W.cs];
+  }
+  __syncthreads();
+  for (int j = 0; j < nbb; ++j) {
+    const int pb = j & 1;
+    const int own = j / w;  // rank holding column j
+    T* pr = P + j * w;
+    // partial squared norm of row j beyond column j
+    T s = T(0);
+    for (int c = t; c < wl; c += bd)
+      if (c0 + c > j) s += pr[c] * pr[c];
+    s = block_sum(s, red);
+    if (t == 0) {
+      sq[pb] = s;
+      if (rank == own) al[pb] = pr[j - c0];
+    }
+    cluster.sync();
+    T tot = T(0);
+    for (int r = 0; r < CS; ++r) tot += *cluster.map_shared_rank(&sq[pb], r);
+    const T alpha = *cluster.map_shared_rank(&al[pb], own);
+    T bj, tj, scale;
+    if (tot == T(0)) {
+      tj = T(0);
+      bj = alpha;
+      scale = T(0);
+    } else {
+      const T h = hypot(alpha, sqrt(tot));
+      bj = alpha >= T(0) ? -h : h;
+      tj = (bj - alpha) / bj;
+      scale = T(1) / (alpha - bj);
+    }
+    for (int c = t; c < wl; c += bd)
+      if (c0 + c > j) pr[c] *= scale;
+    if (t == 0) {
+      if (rank == own) pr[j - c0] = T(1);
+      tau[j] = tj;
+      beta[j] = bj;
+    }
+    __syncthreads();
+    // partial dot products of the rows below with the reflector
+    for (int r = j + 1 + warp; r < nbb; r += nw) {
+      const T* q = P + r * w;
+      T dsum = T(0);
+      for (int c = lane; c < wl; c += 32)
+        if (c0 + c >= j) dsum += q[c] * pr[c];
+      dsum = warp_sum(dsum);
+      if (lane == 0) dots[pb][r] = dsum;
+    }
+    cluster.sync();
+    if (tj != T(0)) {
+      for (int r = j + 1 + warp; r < nbb; r += nw) {
+        T dsum = T(0);
+        if (lane < CS) dsum = *cluster.map_shared_rank(&dots[pb][r], lane);
+        dsum = warp_sum(dsum) * tj;
+        T* q = P + r * w;
+        for (int c = lane; c < wl; c += 32)
+          if (c0 + c >= j) q[c] -= dsum * pr[c];
+      }
+    }
+    __syncthreads();
+  }
+  // panel rows of W (this CTA's columns)
+  for (int l = t; l < nbb * wl; l += bd) {
+    const int r = l / wl, c = l - r * wl, gc = c0 + c;
+    Wb[r * W.rs + gc * W.cs] = gc < r ? P[r * w + c] : (gc == r ? beta[r] : T(0));
+  }
+  __syncthreads();
+  for (int l = t; l < nbb * wl; l += bd) {
+    const int r = l / wl, c = l - r * wl;
+    if (c0 + c < r) P[r * w + c] = T(0);
+  }
+  __syncthreads();
+  // Gram matrix: partial sums here, summed over the cluster
+  for (int pr_ = warp; pr_ < nbb * nbb; pr_ += nw) {
+    const int i = pr_ / nbb, jj = pr_ - i * nbb;
+    if (i >= jj) continue;
+    T dsum = T(0);
+    for (int c = lane; c < wl; c += 32) dsum += P[i * w + c] * P[jj * w + c];
+    dsum = warp_sum(dsum);
+    if (lane == 0) G[i][jj] = dsum;
+  }
+  cluster.sync();
+  // (Gs sums the cluster's partials; G stays readable until the last barrier)
+  __shared__ T Gs[kMaxPanel][kMaxPanel + 1];
+  for (int l = t; l < nbb * nbb; l += bd) {
+    const int i = l / nbb, jj = l - i * nbb;
+    if (i < jj) {
+      T g = T(0);
+      for (int r = 0; r < CS; ++r) g += cluster.map_shared_rank(&G[0][0], r)[i * (kMaxPanel + 1) + jj];
+      Gs[i][jj] = g;
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    for (int jj = 0; jj < nbb; ++jj) {
+      if (lane < jj) {
+        T acc = T(0);
+        for (int k = lane; k < jj; ++k) acc += Tm[lane][k] * Gs[k][jj];
+        Tm[lane][jj] = -tau[jj] * acc;
+      }
+      if (lane == 0) Tm[jj][jj] = tau[jj];
+      if (lane > jj && lane < nbb) Tm[lane][jj] = T(0);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  T* Vb = V + (int64_t)(blockIdx.x / CS) * vbs;
+  T* TVb = TV + (int64_t)(blockIdx.x / CS) * vbs;
+  for (int c = t; c < wl; c += bd) {
+    for (int i = 0; i < nbb; ++i) {
+      T acc = T(0);
+      for (int k = i; k < nbb; ++k) acc = fma(Tm[i][k], P[k * w + c], acc);
+      Vb[i * np + c0 + c] = P[i * w + c];
+      TVb[i * np + c0 + c] = acc;
+    }
+  }
+  cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
 // ---------------------------------------------------------------------------

@@ -293,3 +293,20 @@ def test_rd_mixed_precision_solve():
           % (int(imx["iterations_float32"]), int(imx["iterations"]), int(i64["iterations"]), err))
     assert int(imx["iterations_float32"]) >= 1
     assert err <= 1e-6
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-4)])
+def test_cluster_panels_match_single_cta_panels(monkeypatch, dtype, tol):
+    """Panels of >= 256 columns factored by a 4-CTA cluster
+    (k_tria_panel_cl) against one CTA per matrix (POF_DENSE_CLUSTER=0), at
+    D = 160 (trias of 320 columns) and D = 640."""
+    for n, D, d in ((20, 160, 16), (4, 640, 128)):
+        x0, dtm, dom = _random_problem(3 * D, n, D, d, False)
+        monkeypatch.setenv("POF_DENSE_CLUSTER", "1")
+        m1, L1, s1 = _gpu("filtsmooth", x0, dtm, dom, 4, dtype=dtype)
+        monkeypatch.setenv("POF_DENSE_CLUSTER", "0")
+        m0, L0, s0 = _gpu("filtsmooth", x0, dtm, dom, 4, dtype=dtype)
+        print("cluster vs single-CTA panels, D=%d %s: means %.2e, LL^T %.2e"
+              % (D, dtype, rel(m1, m0), covrel(L1, L0)))
+        assert rel(m1, m0) <= tol and covrel(L1, L0) <= tol
+        assert abs(s1[0] - s0[0]) <= tol * abs(s0[0])
