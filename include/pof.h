@@ -295,8 +295,9 @@ int pof_ieks_solve_mixed(int64_t n_steps, int32_t D, int32_t d, int32_t field, c
  *    refused with POF_ERR_WORKSPACE before any GPU work.  The largest
  *    n_steps that fit, float64 (float32): D = 3: 34212 (100400); D = 4:
  *    20296 (40112); D = 5: 13408 (26618); D = 6: 5778 (11482); D = 8: 3344
- *    (6660); D = 9: 2664 (5316); D = 10: 2176 (4341).  Bad dtypes, shapes
- *    and sizes get pof_linear_filtsmooth's statuses first.
+ *    (6660); D = 9: 2664 (5316); D = 10: 2176 (4341); the dense path's
+ *    shapes (D >= 32) only small cases.  Bad dtypes, shapes and sizes get
+ *    pof_linear_filtsmooth's statuses first.
  *  - The first call on a device looks up the array's address on that device
  *    (the current device); make that first call before any stream capture.
  *    The address is kept until the process exits: resetting the device

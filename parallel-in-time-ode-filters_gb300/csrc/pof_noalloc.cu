@@ -62,7 +62,8 @@ extern "C" int pof_linear_filtsmooth_noalloc(int32_t dtype, int64_t n_steps, int
   // touching the GPU.
   if (dtype != POF_F64 && dtype != POF_F32) return POF_ERR_DTYPE;
   if (n_steps < 1 || D < 1 || d < 1) return POF_ERR_ARG;
-  if (!pof_shape_supported(D, d)) return POF_ERR_SHAPE;
+  // (uncompiled shapes with D >= 32 take the dense path, as in pof_linear_filtsmooth)
+  if (!pof_shape_supported(D, d) && D < 32) return POF_ERR_SHAPE;
   const size_t need = pof_filtsmooth_workspace_bytes(dtype, n_steps, D, d);
   if (need == 0) return POF_ERR_ARG;
   if (need > (size_t)POF_NOALLOC_SCRATCH_BYTES) return POF_ERR_WORKSPACE;

@@ -231,3 +231,35 @@ def test_reference_api_names_exist(module):
     mod = importlib.import_module(module)
     missing = [n for n in REFERENCE_API[module] if not hasattr(mod, n)]
     assert not missing, missing
+
+
+def test_dense_entry_argument_errors_without_gpu(lib):
+    """The dense path's entry points check their arguments and workspace on
+    the host before any CUDA call; uncompiled shapes with D >= 32 reach it
+    through pof_linear_filtsmooth (a null pointer is then POF_ERR_ARG, not
+    POF_ERR_SHAPE)."""
+    null = ctypes.c_void_p(0)
+    one = ctypes.c_void_p(256)  # never dereferenced: every call below fails its checks first
+    assert lib.pof_shape_supported(48, 6) == 0
+    rc = lib.pof_linear_filtsmooth(0, 10, 48, 6, null, null, null, null, 0, null, null, null, 0, null, null, null,
+                                   null, 0, null)
+    assert rc == -1
+    rc = lib.pof_linear_filtsmooth(0, 10, 31, 6, null, null, null, null, 0, null, null, null, 0, null, null, null,
+                                   null, 0, null)
+    assert rc == -2  # below the dense path's D
+    args = [0, 10, 48, 6] + [one] * 4 + [0] + [one] * 3 + [0] + [one] * 3
+    assert lib.pof_dense_linear_filtsmooth(3, *args, 0, one, 1 << 40, null) == -1     # which
+    assert lib.pof_dense_linear_filtsmooth(1, 7, *args[1:], 0, one, 1 << 40, null) == -6  # dtype
+    assert lib.pof_dense_linear_filtsmooth(1, *args, -1, one, 1 << 40, null) == -1    # chunks
+    bad = list(args)
+    bad[8] = 7  # ft_stride neither 0 nor D * D
+    assert lib.pof_dense_linear_filtsmooth(1, *bad, 0, one, 1 << 40, null) == -1
+    need = lib.pof_dense_workspace_bytes(0, 1, 10, 48, 6, 0)
+    assert need > 0 and lib.pof_filtsmooth_workspace_bytes(0, 10, 48, 6) == need
+    assert lib.pof_dense_linear_filtsmooth(1, *args, 0, one, need - 1, null) == -3   # workspace
+    assert lib.pof_dense_workspace_bytes(0, 5, 10, 48, 6, 0) == 0
+    # more chunks, more per-chunk buffers; float32 half the bytes per element
+    assert lib.pof_dense_workspace_bytes(0, 1, 4096, 64, 8, 256) > lib.pof_dense_workspace_bytes(0, 1, 4096, 64, 8, 16)
+    assert lib.pof_dense_workspace_bytes(1, 1, 4096, 64, 8, 64) < lib.pof_dense_workspace_bytes(0, 1, 4096, 64, 8, 64)
+    rc = lib.pof_linearize(0, 10, 40, 7, 11, one, 0.1, one, one, one, null)
+    assert rc == -5  # the reaction-diffusion field needs an even d
