@@ -50,10 +50,16 @@ int panel_rows(int n, size_t es) {
   return nb;
 }
 
-// Panels of at least kClusterMinCols columns are factored by a cluster of
-// kClusterSize CTAs (k_tria_panel_cl), each holding a quarter of the columns.
+// Panels of at least kClusterMinCols columns in batches of at most
+// kClusterMaxBatch matrices are factored by a cluster of kClusterSize CTAs
+// (k_tria_panel_cl), each holding a quarter of the columns: that puts idle
+// SMs to work in the tree levels above the chunks.  At the chunk loops'
+// batches (64-256) every SM already holds a panel, and the cluster's
+// barriers only add time (reaction-diffusion at D = 640: float32 4.64 s per
+// pass against 4.32 s, float64 10.3 s against 9.2 s for 512 steps).
 constexpr int kClusterSize = 4;
 constexpr int kClusterMinCols = 256;
+constexpr int64_t kClusterMaxBatch = 32;
 
 // ---------------------------------------------------------------------------
 // launches
@@ -132,7 +138,7 @@ struct Ctx {
   bool cluster_panels;
   void tria(int64_t batch, int m, int n, MV<T> W) {
     if (batch <= 0) return;
-    const bool cl = cluster_panels && n >= kClusterMinCols;
+    const bool cl = cluster_panels && n >= kClusterMinCols && batch <= kClusterMaxBatch;
     const int nb = cl ? panel_rows((n + kClusterSize - 1) / kClusterSize, sizeof(T)) : panel_rows(n, sizeof(T));
     for (int i0 = 0; i0 < m; i0 += nb) {
       const int nbb = std::min(nb, m - i0);

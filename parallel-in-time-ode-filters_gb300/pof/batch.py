@@ -17,7 +17,7 @@ import torch
 
 from . import _lib
 from .transitions import IWP, preconditioned_discretize
-from .utils import default_device
+from .utils import FORWARD_AD_LOCK, default_device
 
 # Built-in fields with explicit parameters p (4 slots), the expressions of
 # pof/ivp.py: used for the Taylor-mode initial states of a whole batch at
@@ -137,7 +137,8 @@ def prepare_rows(problems, order):
     for nm in sorted(set(names)):
         idx = torch.tensor([b for b in range(B) if names[b] == nm], dtype=torch.long)
         g = _field(nm)
-        derivs[idx] = torch.func.vmap(lambda yy, pp: _taylor(g, yy, pp, q))(y0[idx], params[idx])
+        with FORWARD_AD_LOCK:
+            derivs[idx] = torch.func.vmap(lambda yy, pp: _taylor(g, yy, pp, q))(y0[idx], params[idx])
     P, PI = _nordsieck(q, hs)  # (B, q+1)
     PI_t = torch.as_tensor(PI, dtype=torch.float64)
     x0m = (derivs.transpose(1, 2) * PI_t[:, None, :]).reshape(B, D)  # dimension-major, times P^-1

@@ -14,7 +14,7 @@ import torch
 
 from .sequential_filtsmooth.filter import _sqrt_predict
 from .transitions import IWP, discretize_transitions
-from .utils import MVNSqrt, default_device
+from .utils import FORWARD_AD_LOCK, MVNSqrt, default_device
 
 
 def _nth_time_derivative(g, n):
@@ -48,7 +48,8 @@ def taylor_derivatives(f, y0, num_derivatives):
 def taylor_mode_init(f, y0, num_derivatives, device=None):
     """x0 = (y0, y0', ..., y0^(q)) per dimension, chol = 0 (pof/initialization.py:15-22)."""
     d = torch.as_tensor(y0).shape[0]
-    derivs = taylor_derivatives(f, y0, num_derivatives)  # (q+1, d)
+    with FORWARD_AD_LOCK:
+        derivs = taylor_derivatives(f, y0, num_derivatives)  # (q+1, d)
     m0 = derivs.T.reshape(-1)
     D = d * (num_derivatives + 1)
     dev = device or default_device()

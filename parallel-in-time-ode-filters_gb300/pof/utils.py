@@ -5,6 +5,7 @@ in libpof (see ``pof.parallel_filtsmooth``).
 """
 
 import math
+import threading
 from typing import Any, NamedTuple
 
 import torch
@@ -130,3 +131,10 @@ def cholesky_update_many(chol_init, update_vectors, multiplier):
     for v in update_vectors:
         chol = _cholesky_update(chol, v, multiplier=multiplier)
     return chol
+
+
+# torch.func.jvp enters forward-AD dual levels through a process-wide level
+# counter, so two host threads in a jvp at once break each other's level
+# ("no level exists").  The Taylor-mode initial values (the only forward AD
+# the server's threads run) hold this lock.
+FORWARD_AD_LOCK = threading.RLock()

@@ -391,3 +391,32 @@ def test_dense_lane_cancel_and_timeout(fake, monkeypatch):
     _run_until_idle(srv)
     assert srv.result(c)[1]["status"] == "timeout"
     srv.close()
+
+
+def test_taylor_mode_initial_values_in_two_threads():
+    """The server's admission (pof.batch.prepare_rows) and a dense-lane worker
+    (pof.solver.solve -> taylor_mode_init) compute Taylor-mode initial values
+    with torch.func.jvp in different host threads; forward AD keeps its dual
+    level in a process-wide counter, so both hold pof.utils.FORWARD_AD_LOCK.
+    Run both side by side many times: no "no level exists" error."""
+    from pof import initialization, ivp as pivp
+
+    rd = pivp.fhn_reaction_diffusion(cells=4)
+    errors = []
+
+    def worker():
+        try:
+            for _ in range(40):
+                initialization.taylor_mode_init(rd.f, rd.y0, 3, device=CPU)
+        except Exception as e:  # noqa: BLE001
+            errors.append(e)
+
+    th = threading.Thread(target=worker)
+    th.start()
+    try:
+        for _ in range(40):
+            pbatch.prepare_rows([logistic(50)], 3)
+            pbatch.prepare_rows([vdp(40)], 3)
+    finally:
+        th.join()
+    assert not errors, errors[0]
