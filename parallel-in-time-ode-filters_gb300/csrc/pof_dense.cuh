@@ -254,12 +254,18 @@ __device__ inline T warp_sum(T v) {
 
 // One CTA per batch entry.  Dynamic shared memory: nbb * np elements.
 // V and TV are nbb x np, row-major, vbs elements apart per batch entry.
+// Row r of the panel belongs to warp r mod (warps): that warp applies every
+// reflector to it and, right after reflector r - 1, computes the squared
+// norm of its tail beyond column r (look-ahead), so each reflector costs one
+// block barrier.  A reflector's vector is v = (1, scale * x) with x the
+// unscaled tail of its row; products with v fold the scale in, and the
+// reflector rows are scaled once at the end.
 template <typename T>
 __global__ void __launch_bounds__(512)
     k_tria_panel(MV<T> W, int i0, int nbb, int np, T* __restrict__ V, T* __restrict__ TV, int64_t vbs, int64_t b0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* P = reinterpret_cast<T*>(smem_raw);
-  __shared__ T red[32];
+  __shared__ T nrm[kMaxPanel], scl[kMaxPanel];
   __shared__ T tau[kMaxPanel], beta[kMaxPanel];
   __shared__ T Tm[kMaxPanel][kMaxPanel + 1];
   __shared__ T G[kMaxPanel][kMaxPanel + 1];
@@ -272,12 +278,16 @@ __global__ void __launch_bounds__(512)
     P[l] = Wb[r * W.rs + c * W.cs];
   }
   __syncthreads();
-  for (int j = 0; j < nbb; ++j) {
-    T* pr = P + j * np;
+  if (warp == 0) {  // squared norm of row 0's tail
     T s = T(0);
-    for (int c = j + 1 + t; c < np; c += bd) s += pr[c] * pr[c];
-    s = block_sum(s, red);
-    const T alpha = pr[j];
+    for (int c = 1 + lane; c < np; c += 32) s += P[c] * P[c];
+    s = warp_sum(s);
+    if (lane == 0) nrm[0] = s;
+  }
+  __syncthreads();
+  for (int j = 0; j < nbb; ++j) {
+    const T* pr = P + j * np;
+    const T alpha = pr[j], s = nrm[j];
     T bj, tj, scale;
     if (s == T(0)) {
       tj = T(0);
@@ -289,21 +299,31 @@ __global__ void __launch_bounds__(512)
       tj = (bj - alpha) / bj;
       scale = T(1) / (alpha - bj);
     }
-    __syncthreads();
-    for (int c = j + 1 + t; c < np; c += bd) pr[c] *= scale;
     if (t == 0) {
-      pr[j] = T(1);
       tau[j] = tj;
       beta[j] = bj;
+      scl[j] = scale;
     }
-    __syncthreads();
-    if (tj != T(0)) {
-      for (int r = j + 1 + warp; r < nbb; r += nw) {
-        T* q = P + r * np;
+    // this warp's rows below j: q <- q - tau (q . v) v
+    for (int r = warp; r < nbb; r += nw) {
+      if (r <= j) continue;
+      T* q = P + r * np;
+      if (tj != T(0)) {
         T dsum = T(0);
-        for (int c = j + lane; c < np; c += 32) dsum += q[c] * pr[c];
-        dsum = warp_sum(dsum) * tj;
-        for (int c = j + lane; c < np; c += 32) q[c] -= dsum * pr[c];
+        for (int c = j + 1 + lane; c < np; c += 32) dsum += q[c] * pr[c];
+        dsum = warp_sum(dsum);
+        const T f = tj * (q[j] + scale * dsum);
+        const T fs = f * scale;
+        __syncwarp();
+        for (int c = j + 1 + lane; c < np; c += 32) q[c] -= fs * pr[c];
+        if (lane == 0) q[j] -= f;
+        __syncwarp();
+      }
+      if (r == j + 1) {  // look-ahead: the next reflector's norm
+        T s2 = T(0);
+        for (int c = j + 2 + lane; c < np; c += 32) s2 += q[c] * q[c];
+        s2 = warp_sum(s2);
+        if (lane == 0) nrm[j + 1] = s2;
       }
     }
     __syncthreads();
@@ -314,10 +334,10 @@ __global__ void __launch_bounds__(512)
     Wb[r * W.rs + c * W.cs] = c < r ? P[l] : (c == r ? beta[r] : T(0));
   }
   __syncthreads();
-  // P -> V (unit upper trapezoidal)
+  // P -> V (unit upper trapezoidal, the tails scaled)
   for (int l = t; l < nbb * np; l += bd) {
     const int r = l / np, c = l - r * np;
-    if (c < r) P[l] = T(0);
+    P[l] = c < r ? T(0) : (c == r ? T(1) : P[l] * scl[r]);
   }
   __syncthreads();
   // Gram matrix of the reflectors (upper part)
