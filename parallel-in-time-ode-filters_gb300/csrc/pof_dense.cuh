@@ -130,11 +130,11 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 4)
     k_gemm_tf32x3(int M, int N, int K, float alpha, MV<float> A, MV<float> B, float beta, MV<float> C, int64_t b0) {
-  constexpr int BM = 64, BN = 64, BK = 16, PAD = 8, NT = 128;
-  __shared__ float As[BK][BM + PAD];
-  __shared__ float Bs[BK][BN + PAD];
+  constexpr int BM = 64, BN = 64, BK = 16, PAD = 8, NT = 128, LPT = BM * BK / NT;  // loads per thread (A and B)
+  __shared__ float As[2][BK][BM + PAD];
+  __shared__ float Bs[2][BK][BN + PAD];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int g = lane >> 2, tq = lane & 3;
   const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
@@ -152,48 +152,73 @@ __global__ void __launch_bounds__(128)
       for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
   const bool a_kc = A.cs == 1;
   const bool b_nc = B.cs == 1;
-  for (int k0 = 0; k0 < K; k0 += BK) {
-    for (int l = t; l < BM * BK; l += NT) {
+  // the next K tile goes through registers while the current one is on the
+  // tensor cores (loads ordered along each view's contiguous index)
+  float ra[LPT], rb[LPT];
+  auto a_idx = [&](int l, int& mm, int& kk) {
+    if (a_kc) {
+      kk = l % BK;
+      mm = l / BK;
+    } else {
+      mm = l % BM;
+      kk = l / BM;
+    }
+  };
+  auto b_idx = [&](int l, int& nn, int& kk) {
+    if (b_nc) {
+      nn = l % BN;
+      kk = l / BN;
+    } else {
+      kk = l % BK;
+      nn = l / BK;
+    }
+  };
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int i = 0; i < LPT; ++i) {
       int mm, kk;
-      if (a_kc) {
-        kk = l % BK;
-        mm = l / BK;
-      } else {
-        mm = l % BM;
-        kk = l / BM;
-      }
+      a_idx(t + i * NT, mm, kk);
       const int gm = m0 + mm, gk = k0 + kk;
-      As[kk][mm] = (gm < M && gk < K) ? Ab[gm * A.rs + gk * A.cs] : 0.f;
+      ra[i] = (gm < M && gk < K) ? Ab[gm * A.rs + gk * A.cs] : 0.f;
+      int nn;
+      b_idx(t + i * NT, nn, kk);
+      const int gn = n0 + nn, gk2 = k0 + kk;
+      rb[i] = (gn < N && gk2 < K) ? Bb[gk2 * B.rs + gn * B.cs] : 0.f;
     }
-    for (int l = t; l < BK * BN; l += NT) {
-      int nn, kk;
-      if (b_nc) {
-        nn = l % BN;
-        kk = l / BN;
-      } else {
-        kk = l % BK;
-        nn = l / BK;
-      }
-      const int gn = n0 + nn, gk = k0 + kk;
-      Bs[kk][nn] = (gn < N && gk < K) ? Bb[gk * B.rs + gn * B.cs] : 0.f;
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int i = 0; i < LPT; ++i) {
+      int mm, kk;
+      a_idx(t + i * NT, mm, kk);
+      As[buf][kk][mm] = ra[i];
+      int nn;
+      b_idx(t + i * NT, nn, kk);
+      Bs[buf][kk][nn] = rb[i];
     }
-    __syncthreads();
+  };
+  load(0);
+  store(0);
+  __syncthreads();
+  for (int k0 = 0, cur = 0; k0 < K; k0 += BK, cur ^= 1) {
+    const bool more = k0 + BK < K;
+    if (more) load(k0 + BK);
 #pragma unroll
     for (int kk = 0; kk < BK; kk += 8) {
       uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
         const int mr = wm + i * 16 + g;
-        split_tf32(As[kk + tq][mr], ah[i][0], al[i][0]);
-        split_tf32(As[kk + tq][mr + 8], ah[i][1], al[i][1]);
-        split_tf32(As[kk + tq + 4][mr], ah[i][2], al[i][2]);
-        split_tf32(As[kk + tq + 4][mr + 8], ah[i][3], al[i][3]);
+        split_tf32(As[cur][kk + tq][mr], ah[i][0], al[i][0]);
+        split_tf32(As[cur][kk + tq][mr + 8], ah[i][1], al[i][1]);
+        split_tf32(As[cur][kk + tq + 4][mr], ah[i][2], al[i][2]);
+        split_tf32(As[cur][kk + tq + 4][mr + 8], ah[i][3], al[i][3]);
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int nc = wn + j * 8 + g;
-        split_tf32(Bs[kk + tq][nc], bh[j][0], bl[j][0]);
-        split_tf32(Bs[kk + tq + 4][nc], bh[j][1], bl[j][1]);
+        split_tf32(Bs[cur][kk + tq][nc], bh[j][0], bl[j][0]);
+        split_tf32(Bs[cur][kk + tq + 4][nc], bh[j][1], bl[j][1]);
       }
 #pragma unroll
       for (int i = 0; i < 2; ++i)
@@ -204,6 +229,7 @@ __global__ void __launch_bounds__(128)
           mma_tf32(acc[i][j], ah[i], bh[j]);
         }
     }
+    if (more) store(cur ^ 1);
     __syncthreads();
   }
 #pragma unroll
