@@ -612,7 +612,6 @@ void run_smoother(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t ft
   cx.copy(P, D, D, Ev(0), tEv[0]);
   cx.copy(P, D, D, Dv(0), tDv);
   cx.copy(P, D, 1, gv(0), tgv);
-  const int ce = 0;
   for (int off = 1; off < C0; ++off) {
     const int Pa = L.active(off);
     cx.gemm(Pa, D, D, D, one, tEv[0], Ev(off), zero, tEv[1]);
@@ -625,7 +624,7 @@ void run_smoother(X& cx, const Layout<T>& L, const T* F, const T* QL, int64_t ft
   }
   // smoothed state at every chunk end, from the terminal (filtered) state
   const MV<T> emv{L.em, 1, 1, D}, eLv = rowmajor(L.eL, D, DD);
-  smoother_tree(cx, L, SElem<T>{tgv, tEv[ce], tDv}, State<T>{emv, eLv}, om + n * D, oL + n * DD);
+  smoother_tree(cx, L, SElem<T>{tgv, tEv[0], tDv}, State<T>{emv, eLv}, om + n * D, oL + n * DD);
   // backward recursion inside every chunk
   const MV<T> tmv{L.tm, 1, 1, D};
   for (int off = C0 - 1; off >= 0; --off) {
