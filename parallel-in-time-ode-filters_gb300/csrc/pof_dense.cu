@@ -73,6 +73,13 @@ struct Ctx {
 
   void gemm(int64_t batch, int M, int N, int K, T alpha, MV<T> A, MV<T> B, T beta, MV<T> C) {
     if (batch <= 0 || M <= 0 || N <= 0) return;
+    // grid.y holds the row tiles (at most 65535): taller products go in row blocks
+    constexpr int64_t kRows = kMaxGridYZ * 32;
+    if (M > kRows) {
+      for (int64_t r0 = 0; r0 < M; r0 += kRows)
+        gemm(batch, (int)std::min<int64_t>(kRows, M - r0), N, K, alpha, sub(A, r0, 0), B, beta, sub(C, r0, 0));
+      return;
+    }
     for (int64_t b0 = 0; b0 < batch; b0 += kMaxGridYZ) {
       const int nb = (int)std::min<int64_t>(kMaxGridYZ, batch - b0);
       if (N <= 16) {
