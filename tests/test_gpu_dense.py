@@ -163,7 +163,8 @@ def test_dense_path_on_random_models(n, D, d, chunks, with_R, per_step):
 
 def test_uncompiled_large_shape_takes_the_dense_path():
     """pof.parallel_filtsmooth at (D, d) = (48, 6), which no small-D table
-    compiles: libpof's own entry points run the dense path."""
+    compiles: libpof's own entry points (filter + smoother, filter alone,
+    smoother alone) run the dense path."""
     assert _lib.lib().pof_shape_supported(48, 6) == 0
     n, D, d = 30, 48, 6
     x0, dtm, dom = _random_problem(5, n, D, d, False)
@@ -173,6 +174,14 @@ def test_uncompiled_large_shape_takes_the_dense_path():
                                                   (T(dom[0]), T(dom[1]), None))
     assert rel(N_(out.mean), sm) <= TOL and covrel(N_(out.chol), sL) <= TOL
     assert abs(float(gnll) - nll) <= TOL * abs(nll) and abs(float(gobj) - sobj) <= TOL * abs(sobj)
+    # the filter alone and the smoother alone through their own entry points
+    fout, fnll, fobj_, _ = pfs.linear_noiseless_filtering(MVNSqrt(T(x0[0]), T(x0[1])), (T(dtm[0]), T(dtm[1])),
+                                                          (T(dom[0]), T(dom[1]), None))
+    assert rel(N_(fout.mean), fm) <= TOL and covrel(N_(fout.chol), fL) <= TOL
+    assert abs(float(fobj_) - fobj) <= TOL * abs(fobj)
+    sout, sobj_ = pfs.smoothing((T(dtm[0]), T(dtm[1])), MVNSqrt(T(fm), T(fL)))
+    assert rel(N_(sout.mean), sm) <= TOL and covrel(N_(sout.chol), sL) <= TOL
+    assert abs(float(sobj_) - sobj) <= TOL * abs(sobj)
 
 
 def test_dense_path_at_d640():
