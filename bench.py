@@ -23,6 +23,15 @@ cpu_baseline the NumPy float64 oracle (the reference's algorithm) on a
              same workload and metric (the reference itself needs JAX, which
              is not installed on these machines).
 
+Blocks of the default line (skipped with --no-extras): config0 (the
+reference's N = 1000 configuration), batched (4096 FitzHugh-Nagumo IVPs and
+512 Van der Pol IVPs, float64 and float32 + float64 polish), served (a
+Poisson stream through pof.serve.Server, p50/p99), dense (the
+reaction-diffusion system at (D, d) = (640, 128): one IEKS iteration's work on
+the dense path, float32 and float64).  Other workloads: --workload
+scan_sweep / v100_table / mixed_lv_vdp / serve_stream / fhn_batch4096 /
+rd_d640.
+
 Multi-GPU: each rank solves its own copy of the workload (replicas; the path
 does not shard a single solve), value = sum over ranks.
 """
