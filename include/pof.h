@@ -113,7 +113,9 @@ const char* pof_status_string(int status);
 const char* pof_last_cuda_error(void);
 int pof_version(void);
 
-/* 1 if the (D, d) pair is compiled into this build, else 0. */
+/* 1 if the (D, d) pair is compiled into this build's small-D tables, else 0
+ * (uncompiled pairs with D >= 32 run on the dense path, see
+ * pof_dense_linear_filtsmooth). */
 int pof_shape_supported(int32_t D, int32_t d);
 
 /* Bytes of the workspace of pof_linear_filtsmooth, pof_linear_noiseless_filtering
