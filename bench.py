@@ -508,7 +508,10 @@ def run_gpu(args, workload):
         extras["batched"] = batched_block(args)
         extras["served"] = served_block(args)
         if world == 1:
-            extras["dense"] = dense_block(args)
+            try:  # a failure here must not cost the line its other numbers
+                extras["dense"] = dense_block(args)
+            except Exception as e:  # noqa: BLE001
+                extras["dense"] = {"error": "%s: %s" % (type(e).__name__, e)}
 
     if rank != 0:
         return
@@ -1668,15 +1671,47 @@ def dense_block(args):
 
     from pof import _lib
 
-    out, info, _ = dense_passes("rd_d640", ("float32", "float64"), 256, 1, 1)
+    out, info, setup = dense_passes("rd_d640", ("float32", "float64"), 256, 1, 1)
     peak64 = fp64_peak(torch, _lib.lib(), _lib)
     out["float64"]["frac_of_fp64_probe"] = out["float64"]["gflops"] / peak64
     torch.cuda.empty_cache()
+    try:
+        cpu = dense_cpu_sample(setup, 4)
+    except Exception as e:  # noqa: BLE001
+        cpu = {"error": "%s: %s" % (type(e).__name__, e), "ms_per_step": float("nan")}
     return {"workload": "rd_d640: method-of-lines FitzHugh-Nagumo, 64 periodic cells (d = 128), q = 4 (D = 640), "
                         "N = 4096, t in [0, 20]; one IEKS iteration's work (EK1 + dense filter + smoother) from "
                         "the constant-init trajectory; float64 over the first 256 steps",
             "config": info, "float32": out["float32"], "float64": out["float64"], "fp64_probe_gflops": peak64,
-            "flop_model": "pof/_flops.py dense_pass_flops: 12.3 GFLOP per step at (640, 128)"}
+            "flop_model": "pof/_flops.py dense_pass_flops: 12.3 GFLOP per step at (640, 128)",
+            "cpu_baseline": cpu,
+            "float64_vs_cpu_per_step": cpu["ms_per_step"] / out["float64"]["ms_per_step"]}
+
+
+def dense_cpu_sample(setup, nsteps):
+    """One IEKS iteration of the reference's algorithm restated in NumPy
+    float64 (the oracle: EK1 linearization at the constant-init trajectory,
+    then the associative-scan filter + smoother of
+    oracle.filtsmooth.linear_filtsmooth) on the first `nsteps` steps of the
+    dense workload's grid, on this host's cores (NumPy's BLAS/LAPACK
+    threads): ms per step."""
+    from oracle import filtsmooth as ofs, ivp as oivp, solver as osolver
+
+    pv, ts, q = setup
+    cells = pv.y0.shape[0] // 2
+    o = oivp.fhn_reaction_diffusion(cells=cells, tmax=float(ts[-1]))
+    grid = np.asarray(ts[: nsteps + 1], dtype=np.float64)
+    st = osolver.set_up_solver(o, grid, q)
+    states = osolver.get_initial_trajectory(st, "constant")
+    t0 = time.perf_counter()
+    dom = osolver.linearize_at_previous_states(st, states[0])
+    ofs.linear_filtsmooth(st.x0, (st.F, st.QL), dom)
+    sec = time.perf_counter() - t0
+    return {"value": sec * 1e3 / nsteps, "ms_per_step": sec * 1e3 / nsteps, "unit": "ms per step (one IEKS iteration)",
+            "kind": "port", "cores": os.cpu_count(),
+            "sample": "the oracle (the reference's algorithm in NumPy float64): EK1 at the constant-init trajectory "
+                      "and the associative-scan filter + smoother on the first %d steps of the same grid (set-up not "
+                      "timed), NumPy's BLAS/LAPACK threads on this host" % nsteps}
 
 
 def run_dense(args, workload):
