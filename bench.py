@@ -1678,14 +1678,15 @@ def dense_block(args):
     try:
         cpu = dense_cpu_sample(setup, 4)
     except Exception as e:  # noqa: BLE001
-        cpu = {"error": "%s: %s" % (type(e).__name__, e), "ms_per_step": float("nan")}
+        cpu = {"error": "%s: %s" % (type(e).__name__, e), "ms_per_step": None}
     return {"workload": "rd_d640: method-of-lines FitzHugh-Nagumo, 64 periodic cells (d = 128), q = 4 (D = 640), "
                         "N = 4096, t in [0, 20]; one IEKS iteration's work (EK1 + dense filter + smoother) from "
                         "the constant-init trajectory; float64 over the first 256 steps",
             "config": info, "float32": out["float32"], "float64": out["float64"], "fp64_probe_gflops": peak64,
             "flop_model": "pof/_flops.py dense_pass_flops: 12.3 GFLOP per step at (640, 128)",
             "cpu_baseline": cpu,
-            "float64_vs_cpu_per_step": cpu["ms_per_step"] / out["float64"]["ms_per_step"]}
+            "float64_vs_cpu_per_step": (cpu["ms_per_step"] / out["float64"]["ms_per_step"]
+                                        if cpu.get("ms_per_step") else None)}
 
 
 def dense_cpu_sample(setup, nsteps):
