@@ -155,6 +155,8 @@ def test_dense_schedule_matches_oracle_on_solver_models(dense_cpu, name, mk, chu
     (33, 16, 2, 4, True, False),   # C0 = 9, last chunk 6 steps
     (29, 10, 2, 8, False, True),   # C0 = 4, last chunk 1 step
     (23, 14, 1, 4, True, True),    # d = 1: sigma^2 compared
+    (300, 10, 2, 256, False, True),  # C0 = 2, 150 chunks: tree levels 150, 75, 38, 19, 10, 5, 3, 2, 1
+    (97, 12, 3, 33, True, False),    # C0 = 3, 33 chunks (odd levels all the way up)
 ])
 def test_dense_schedule_matches_oracle_on_random_models(dense_cpu, n, D, d, chunks, with_R, per_step):
     rng = np.random.default_rng(n * 1000 + D * 10 + d)
