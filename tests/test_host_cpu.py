@@ -339,7 +339,8 @@ def _np_(t):
 
 FIELDS = [("logistic", {}), ("logistic", {"r": 3.0}), ("lotkavolterra", {}), ("vanderpol", {}),
           ("fitzhughnagumo", {}), ("fhn_classic", {}), ("rober", {}), ("rigid_body", {}), ("seir", {}),
-          ("threebody", {}), ("henonheiles", {})]
+          ("threebody", {}), ("henonheiles", {}), ("fhn_reaction_diffusion", {"cells": 6}),
+          ("fhn_reaction_diffusion", {"cells": 2, "kv": 0.7, "kw": 0.1})]
 
 
 @pytest.mark.parametrize("name,kw", FIELDS)
@@ -357,3 +358,26 @@ def test_builtin_fields_match_the_oracle(rng, name, kw):
         assert np.allclose(fy, o.f(None, y), rtol=1e-13, atol=1e-13 * max(1.0, np.abs(fy).max()))
         J = torch.func.jacfwd(lambda yy: p.f(None, yy))(T(y)).numpy()
         assert np.allclose(J, o.jac(y), rtol=1e-12, atol=1e-12 * max(1.0, np.abs(J).max()))
+
+
+@pytest.mark.parametrize("cells", [1, 2, 5])
+def test_reaction_diffusion_forms_agree(rng, cells):
+    """The oracle's reaction-diffusion system in its three forms -- the
+    Taylor components (used for Taylor-mode initial values), the array field
+    and its analytic Jacobian -- agree with each other and with the torch
+    field's torch.func.jacfwd, periodic neighbours included (one and two
+    cells: the neighbours coincide and their couplings add up)."""
+    from oracle import taylor
+
+    o = oivp.fhn_reaction_diffusion(cells=cells, kv=0.3, kw=0.07)
+    p = pivp.fhn_reaction_diffusion(cells=cells, kv=0.3, kw=0.07)
+    for _ in range(3):
+        y = o.y0 + 0.3 * rng.standard_normal(o.y0.shape)
+        f_arr = o.f(None, y)
+        f_cmp = np.asarray(taylor.evaluate(o.components, y), dtype=np.float64)
+        assert np.allclose(f_arr, f_cmp, rtol=1e-14, atol=1e-14)
+        J_arr = o.jac(y)
+        J_cmp = taylor.jacobian(o.components, y)
+        assert np.allclose(J_arr, J_cmp, rtol=1e-13, atol=1e-13)
+        J_t = torch.func.jacfwd(lambda yy: p.f(None, yy))(T(y)).numpy()
+        assert np.allclose(J_t, J_arr, rtol=1e-13, atol=1e-13)
