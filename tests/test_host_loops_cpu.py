@@ -227,3 +227,81 @@ def test_sequential_eks_of_a_user_field(host_only, monkeypatch):
     full, _ = psolver.sequential_eks_solve(f=f, y0=y0, ts=ts, order=3, return_full_states=True)
     (ofull, _), _ = osolver.sequential_eks_solve(o, ts, 3, return_full_states=True)
     assert rel(_np(full.mean), ofull) <= 1e-10
+
+
+# ---------------------------------------------------------------------------
+# the host-driven float32 phase of precision="mixed" (pof.solver._float32_phase,
+# the rules of pof_ieks_solve_mixed): its stopping and discard rules against a
+# scripted sequence of float32 iterates (libpof's linearization and
+# filter/smoother replaced by fakes that move y = E0 m by chosen amounts)
+# ---------------------------------------------------------------------------
+
+def _phase_setup(monkeypatch, rels):
+    from pof.observations import AffineModel
+    from pof.transitions import TransitionModel
+
+    n, D = 6, 2
+    E0 = torch.tensor([[1.0, 0.0]], dtype=torch.float64)
+    F = torch.eye(D, dtype=torch.float64).expand(n, D, D)
+    setup = {"dtm": TransitionModel(F, F), "om": object(), "E0": E0,
+             "x0": MVNSqrt(torch.zeros(D, dtype=torch.float64), torch.zeros((D, D), dtype=torch.float64))}
+    states = MVNSqrt(torch.ones((n + 1, D), dtype=torch.float64), torch.zeros((n + 1, D, D), dtype=torch.float64))
+    cur = {"m": states.mean.clone(), "calls": 0}
+    script = iter(rels)
+
+    def lin(om, st):
+        return AffineModel(torch.ones((n, 1, D), dtype=torch.float64), torch.zeros((n, 1), dtype=torch.float64), None)
+
+    def fs(x0, dtm, dom):
+        cur["calls"] += 1
+        assert dtm[0].dtype == torch.float32 and dom[0].dtype == torch.float32 and dtm[0].dim() == 2
+        r = next(script)
+        m = cur["m"].clone()
+        m[:, 0] = m[:, 0] * (1.0 + r) if np.isfinite(r) else float("nan")
+        if np.isfinite(r):
+            cur["m"] = m
+        return MVNSqrt(m.to(torch.float32), None), None, None, None
+
+    monkeypatch.setattr(pstep, "linearize_at_previous_states", lin)
+    monkeypatch.setattr(psolver, "parallel_linear_filtsmooth", fs)
+    monkeypatch.setattr(psolver, "_wait", lambda dev: None)
+    return setup, states, cur
+
+
+@pytest.mark.parametrize("rels,kw,expect_it,expect_kept", [
+    # converges: the change falls below rtol_f32 at the 5th iteration
+    ([0.5, 0.1, 0.01, 1e-3, 1e-6], dict(rtol_f32=1e-5), 5, True),
+    # three changes that do not shrink (settle_f32 = inf counts from the first): stops, and
+    # the phase never came within 100 rtol_f32 -> discarded
+    ([0.5, 0.6, 0.7, 0.8, 0.9], dict(rtol_f32=1e-5), 4, False),
+    # a non-finite float32 iterate ends the phase; the one kept iteration is within 100 rtol_f32
+    ([0.1, float("nan")], dict(rtol_f32=0.01), 1, True),
+    # non-shrinking changes count only once the smallest change is below settle_f32
+    ([0.5, 0.7, 0.9, 0.01, 0.02, 0.03, 0.04, 0.05], dict(rtol_f32=1e-3, settle_f32=0.05), 7, True),
+    # maxiters_f32
+    ([0.5, 0.4, 0.3, 0.2, 0.1], dict(rtol_f32=1e-3, maxiters_f32=3), 3, False),
+])
+def test_float32_phase_rules(monkeypatch, rels, kw, expect_it, expect_kept):
+    setup, states, cur = _phase_setup(monkeypatch, rels)
+    args = dict(maxiters_f32=100, rtol_f32=1e-5, settle_f32=float("inf"))
+    args.update(kw)
+    means, it32, best = psolver._float32_phase(setup, states, **args)
+    if expect_kept:
+        assert it32 == expect_it
+        assert torch.allclose(means, cur["m"], rtol=1e-6)  # the last finite float32 iterate, in float64
+    else:
+        assert it32 == 0 and torch.equal(means, states.mean)  # discarded: the input trajectory
+    finite = [r for r in rels[:expect_it] if np.isfinite(r)]
+    assert best == pytest.approx(min(finite), rel=1e-3, abs=1e-7)  # measured on float32 iterates
+
+
+def test_float32_phase_stop_hook(monkeypatch):
+    setup, states, cur = _phase_setup(monkeypatch, [0.5, 0.4, 0.3, 0.2, 0.1])
+    calls = {"n": 0}
+
+    def stop():
+        calls["n"] += 1
+        return calls["n"] > 2  # two iterations, then stop
+
+    means, it32, best = psolver._float32_phase(setup, states, 100, 1e-5, float("inf"), stop)
+    assert cur["calls"] == 2
