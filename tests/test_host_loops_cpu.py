@@ -305,3 +305,29 @@ def test_float32_phase_stop_hook(monkeypatch):
 
     means, it32, best = psolver._float32_phase(setup, states, 100, 1e-5, float("inf"), stop)
     assert cur["calls"] == 2
+
+
+def test_solve_loop_stop_hook_and_status(host_only):
+    """solve(..., stop=...) for a field without a device loop: the hook is
+    checked before every iteration; once it returns True the loop ends with
+    the last iterate and status 3 (cancelled).  rtol reaches crit."""
+    f, y0, _, t1 = user_field("vanderpol")
+    ts = np.linspace(0.0, t1, 40)
+    (m_full, _), full = psolver.solve(f=f, y0=y0, ts=ts, order=2, init="constant")
+    assert int(full["status"]) == 0 and int(full["iterations"]) > 3
+    calls = {"n": 0}
+
+    def stop_after(k):
+        def stop():
+            calls["n"] += 1
+            return calls["n"] > k
+        return stop
+
+    _, info0 = psolver.solve(f=f, y0=y0, ts=ts, order=2, init="constant", stop=stop_after(0))
+    assert int(info0["status"]) == 3 and int(info0["iterations"]) == 0
+    calls["n"] = 0
+    _, info2 = psolver.solve(f=f, y0=y0, ts=ts, order=2, init="constant", stop=stop_after(2))
+    assert int(info2["status"]) == 3 and int(info2["iterations"]) == 2
+    # a looser objective tolerance stops no later
+    _, loose = psolver.solve(f=f, y0=y0, ts=ts, order=2, init="constant", rtol=1e-2)
+    assert int(loose["status"]) == 0 and int(loose["iterations"]) <= int(full["iterations"])
